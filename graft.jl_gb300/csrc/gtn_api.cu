@@ -1,0 +1,285 @@
+// C ABI entry points: contexts, maps, one-shot contractions, permutations and vector helpers.
+#include "gtn_internal.h"
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+int set_err(gtn_ctx ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+cudaError_t ctx_workspace(gtn_ctx ctx, size_t bytes, void** out) {
+  if (bytes > ctx->ws_bytes) {
+    if (ctx->ws) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(ctx->ws);
+      ctx->ws = nullptr;
+      ctx->ws_bytes = 0;
+    }
+    const size_t want = bytes + bytes / 4;
+    cudaError_t e = cudaMalloc(&ctx->ws, want);
+    if (e != cudaSuccess) return e;
+    ctx->ws_bytes = want;
+  }
+  *out = ctx->ws;
+  return cudaSuccess;
+}
+
+cudaError_t ctx_red(gtn_ctx ctx, size_t n2) {
+  if (n2 > ctx->red_cap) {
+    if (ctx->d_red) cudaFree(ctx->d_red);
+    ctx->d_red = nullptr;
+    cudaError_t e = cudaMalloc(&ctx->d_red, n2 * sizeof(double2));
+    if (e != cudaSuccess) return e;
+    ctx->red_cap = n2;
+  }
+  if (!ctx->h_red) {
+    cudaError_t e = cudaMallocHost(&ctx->h_red, 256 * sizeof(double2));
+    if (e != cudaSuccess) return e;
+    ctx->hred_cap = 256;
+  }
+  return cudaSuccess;
+}
+
+extern "C" {
+
+int gtn_ctx_create(int device, gtn_ctx* out) {
+  if (!out) return GTN_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GTN_ERR_CUDA;
+  if (device < 0 || device >= ndev) return GTN_ERR_INVALID;
+  gtn_ctx ctx = new (std::nothrow) gtn_ctx_s();
+  if (!ctx) return GTN_ERR_MEMORY;
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return GTN_ERR_CUDA; }
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, device);
+  ctx->sm_count = prop.multiProcessorCount;
+  ctx->cc_major = prop.major;
+  ctx->cc_minor = prop.minor;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return GTN_ERR_CUDA;
+  }
+  ctx->own_stream = true;
+  if (cudaMalloc(&ctx->d_errflag, sizeof(int)) != cudaSuccess ||
+      cudaMemset(ctx->d_errflag, 0, sizeof(int)) != cudaSuccess) {
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GTN_ERR_CUDA;
+  }
+  if (ctx_red(ctx, 4096) != cudaSuccess) {
+    cudaFree(ctx->d_errflag);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GTN_ERR_CUDA;
+  }
+  *out = ctx;
+  return GTN_OK;
+}
+
+int gtn_ctx_destroy(gtn_ctx ctx) {
+  if (!ctx) return GTN_ERR_INVALID;
+  cudaStreamSynchronize(ctx->stream);
+  linalg_release(ctx);
+  if (ctx->ws) cudaFree(ctx->ws);
+  if (ctx->d_red) cudaFree(ctx->d_red);
+  if (ctx->h_red) cudaFreeHost(ctx->h_red);
+  if (ctx->d_errflag) cudaFree(ctx->d_errflag);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GTN_OK;
+}
+
+int gtn_ctx_set_stream(gtn_ctx ctx, void* stream) {
+  if (!ctx) return GTN_ERR_INVALID;
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  ctx->own_stream = false;
+  return GTN_OK;
+}
+
+void* gtn_ctx_stream(gtn_ctx ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+
+const char* gtn_last_error(gtn_ctx ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int64_t gtn_ctx_launch_count(gtn_ctx ctx) { return ctx ? ctx->launches : -1; }
+
+int gtn_ctx_sync(gtn_ctx ctx) {
+  if (!ctx) return GTN_ERR_INVALID;
+  GTN_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  int flag = 0;
+  GTN_CUDA_TRY(ctx, cudaMemcpy(&flag, ctx->d_errflag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag != 0) {
+    cudaMemset(ctx->d_errflag, 0, sizeof(int));
+    return set_err(ctx, GTN_ERR_TIMEOUT, "device wait timed out (code " + std::to_string(flag) + ")");
+  }
+  return GTN_OK;
+}
+
+int gtn_map_create(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dims,
+                   const int* labels, const int* conj, const int* order,
+                   const void* const* statics, int precision, gtn_map* out) {
+  if (!ctx || !out || !ranks || !dims || !labels || !order) return set_err(ctx, GTN_ERR_INVALID, "null argument");
+  *out = nullptr;
+  gtn_map map = new (std::nothrow) gtn_map_s();
+  if (!map) return set_err(ctx, GTN_ERR_MEMORY, "host allocation failed");
+  const int st = plan_build(ctx, n_operands, ranks, dims, labels, conj, order, statics, precision, map);
+  if (st != GTN_OK) {
+    cudaStreamSynchronize(ctx->stream);
+    map_free(map);
+    delete map;
+    return st;
+  }
+  *out = map;
+  return GTN_OK;
+}
+
+int gtn_map_destroy(gtn_map map) {
+  if (!map) return GTN_ERR_INVALID;
+  if (map->ctx) cudaStreamSynchronize(map->ctx->stream);
+  map_free(map);
+  delete map;
+  return GTN_OK;
+}
+
+int gtn_map_apply_prec(gtn_map map, int precision, const void* x, void* y) {
+  if (!map || !x || !y) return GTN_ERR_INVALID;
+  return map_run(map, precision, static_cast<const double2*>(x), static_cast<double2*>(y));
+}
+
+int gtn_map_apply(gtn_map map, const void* x, void* y) {
+  if (!map) return GTN_ERR_INVALID;
+  return gtn_map_apply_prec(map, map->precision, x, y);
+}
+
+int gtn_map_apply_host(gtn_map map, const void* x_host, void* y_host) {
+  if (!map || !x_host || !y_host) return GTN_ERR_INVALID;
+  gtn_ctx ctx = map->ctx;
+  if (!map->dx) {
+    if (cudaMalloc(&map->dx, map->x_elems * sizeof(double2)) != cudaSuccess ||
+        cudaMalloc(&map->dy, map->y_elems * sizeof(double2)) != cudaSuccess)
+      return set_err(ctx, GTN_ERR_MEMORY, "host-apply staging allocation failed");
+    map->owned.push_back(map->dx);
+    map->owned.push_back(map->dy);
+  }
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(map->dx, x_host, map->x_elems * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+  int st = map_run(map, map->precision, static_cast<const double2*>(map->dx), static_cast<double2*>(map->dy));
+  if (st != GTN_OK) return st;
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(y_host, map->dy, map->y_elems * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+  return gtn_ctx_sync(ctx);
+}
+
+int gtn_map_info(gtn_map map, int64_t* x_elems, int64_t* y_elems, double* flops, int* n_steps,
+                 int64_t* bytes) {
+  if (!map) return GTN_ERR_INVALID;
+  if (x_elems) *x_elems = map->x_elems;
+  if (y_elems) *y_elems = map->y_elems;
+  if (flops) *flops = map->flops;
+  if (n_steps) *n_steps = (int)map->steps.size();
+  if (bytes) *bytes = map->bytes;
+  return GTN_OK;
+}
+
+int gtn_map_out_shape(gtn_map map, int* rank, int64_t* dims) {
+  if (!map || !rank) return GTN_ERR_INVALID;
+  *rank = (int)map->y_dims.size();
+  if (dims)
+    for (size_t i = 0; i < map->y_dims.size(); ++i) dims[i] = map->y_dims[i];
+  return GTN_OK;
+}
+
+int gtn_contract(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dims,
+                 const int* labels, const int* conj, const int* order,
+                 const void* const* operands, void* out, int precision) {
+  if (!ctx || !operands || !out) return set_err(ctx, GTN_ERR_INVALID, "null argument");
+  gtn_map map = nullptr;
+  int st = gtn_map_create(ctx, n_operands, ranks, dims, labels, conj, order, operands, precision, &map);
+  if (st != GTN_OK) return st;
+  st = map_run(map, precision, static_cast<const double2*>(operands[0]), static_cast<double2*>(out));
+  gtn_map_destroy(map);
+  return st;
+}
+
+int gtn_permute(gtn_ctx ctx, int rank, const int64_t* dims, const int* perm, const void* in, void* out) {
+  if (!ctx || rank < 1 || rank > 16 || !dims || !perm || !in || !out)
+    return set_err(ctx, GTN_ERR_INVALID, "gtn_permute: bad argument");
+  std::vector<int64_t> strides(rank, 1);
+  for (int i = rank - 2; i >= 0; --i) strides[i] = strides[i + 1] * dims[i + 1];
+  // out legs perm[0..rank-2] -> M group, perm[rank-1] -> K group (strides of the input)
+  std::vector<int64_t> gd, gs;
+  int64_t M = 1;
+  for (int a = 0; a + 1 < rank; ++a) {
+    const int l = perm[a];
+    if (l < 0 || l >= rank) return set_err(ctx, GTN_ERR_INVALID, "gtn_permute: bad permutation");
+    M *= dims[l];
+    if (dims[l] == 1) continue;
+    if (!gd.empty() && gs.back() == strides[l] * dims[l]) {
+      gd.back() *= dims[l];
+      gs.back() = strides[l];
+    } else {
+      gd.push_back(dims[l]);
+      gs.push_back(strides[l]);
+    }
+  }
+  if ((int)gd.size() > GTN_MAXG) return set_err(ctx, GTN_ERR_UNSUPPORTED, "gtn_permute: rank too high");
+  GroupSpec mg, kg;
+  std::memset(&mg, 0, sizeof(mg));
+  std::memset(&kg, 0, sizeof(kg));
+  mg.n = (int)gd.size();
+  for (int i = 0; i < mg.n; ++i) { mg.dim[i] = gd[i]; mg.str[i] = gs[i]; }
+  const int lk = perm[rank - 1];
+  const int64_t K = dims[lk];
+  kg.n = 1;
+  kg.dim[0] = K;
+  kg.str[0] = strides[lk];
+  cudaError_t e = launch_gather_c128_to_c128(static_cast<const double2*>(in), mg, kg, M, K, K,
+                                             static_cast<double2*>(out), ctx->stream);
+  ctx->launches++;
+  if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("gtn_permute: ") + cudaGetErrorString(e));
+  return GTN_OK;
+}
+
+int gtn_dot(gtn_ctx ctx, int64_t n, const void* x, const void* y, double* out2) {
+  if (!ctx || !x || !y || !out2) return set_err(ctx, GTN_ERR_INVALID, "gtn_dot: null argument");
+  const int nblk = multidot_blocks(ctx);
+  GTN_CUDA_TRY(ctx, ctx_red(ctx, (size_t)nblk + 8));
+  GTN_CUDA_TRY(ctx, launch_multidot(static_cast<const double2*>(x), 0, 1, static_cast<const double2*>(y), n,
+                                    ctx->d_red, ctx->d_red + 8, nblk, ctx->stream));
+  ctx->launches += 2;
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_red, ctx->d_red, sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+  int st = gtn_ctx_sync(ctx);
+  if (st != GTN_OK) return st;
+  out2[0] = ctx->h_red[0].x;
+  out2[1] = ctx->h_red[0].y;
+  return GTN_OK;
+}
+
+int gtn_axpby(gtn_ctx ctx, int64_t n, double a_re, double a_im, const void* x, double b_re, double b_im,
+              void* y) {
+  if (!ctx || !x || !y) return set_err(ctx, GTN_ERR_INVALID, "gtn_axpby: null argument");
+  GTN_CUDA_TRY(ctx, launch_axpby(n, make_double2(a_re, a_im), static_cast<const double2*>(x),
+                                 make_double2(b_re, b_im), static_cast<double2*>(y), ctx->stream));
+  ctx->launches++;
+  return GTN_OK;
+}
+
+int gtn_diag_scale(gtn_ctx ctx, int64_t rows, int64_t cols, const double* d_host, int side, void* A) {
+  if (!ctx || !d_host || !A || rows < 0 || cols < 0 || (side != 0 && side != 1))
+    return set_err(ctx, GTN_ERR_INVALID, "gtn_diag_scale: bad argument");
+  const int64_t nd = side == 0 ? cols : rows;
+  void* ws = nullptr;
+  GTN_CUDA_TRY(ctx, ctx_workspace(ctx, (size_t)nd * sizeof(double) + 256, &ws));
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(ws, d_host, nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  GTN_CUDA_TRY(ctx, launch_diag_scale(static_cast<double2*>(A), rows, cols, static_cast<const double*>(ws), side,
+                                      ctx->stream));
+  ctx->launches++;
+  // the host factors are pageable: the copy above is synchronous with respect to the host
+  return GTN_OK;
+}
+
+}  // extern "C"

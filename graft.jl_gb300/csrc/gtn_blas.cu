@@ -1,0 +1,242 @@
+// FP64 vector kernels for the device-resident Krylov solvers (HBM-bound): batched
+// Gram-Schmidt projections h = V^H w, linear combinations w = b*w + s*V*c, and small
+// helpers for the factorisation paths.
+#include "gtn_internal.h"
+
+namespace {
+
+constexpr int kMaxJ = 64;
+constexpr int kDotThreads = 256;
+
+__device__ __forceinline__ double2 cmul_conj(double2 a, double2 b) {  // conj(a) * b
+  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+
+// Per-block partial sums of conj(V_j) . w for j < J, written to part[block * J + j].
+template <int JB>
+__global__ void __launch_bounds__(kDotThreads) multidot_partial_kernel(const double2* __restrict__ V,
+                                                                       int64_t ldv, int J, int j0,
+                                                                       const double2* __restrict__ w,
+                                                                       int64_t n,
+                                                                       double2* __restrict__ part) {
+  double2 acc[JB];
+#pragma unroll
+  for (int j = 0; j < JB; ++j) acc[j] = make_double2(0.0, 0.0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 wi = w[i];
+#pragma unroll
+    for (int j = 0; j < JB; ++j) {
+      if (j0 + j < J) {
+        const double2 v = V[(int64_t)(j0 + j) * ldv + i];
+        const double2 p = cmul_conj(v, wi);
+        acc[j].x += p.x;
+        acc[j].y += p.y;
+      }
+    }
+  }
+  __shared__ double2 red[kDotThreads / 32][JB];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < JB; ++j) {
+    double x = acc[j].x, y = acc[j].y;
+    for (int o = 16; o > 0; o >>= 1) {
+      x += __shfl_down_sync(0xffffffffu, x, o);
+      y += __shfl_down_sync(0xffffffffu, y, o);
+    }
+    if (lane == 0) red[wid][j] = make_double2(x, y);
+  }
+  __syncthreads();
+  if (threadIdx.x < JB && j0 + (int)threadIdx.x < J) {
+    double x = 0, y = 0;
+    for (int q = 0; q < kDotThreads / 32; ++q) {
+      x += red[q][threadIdx.x].x;
+      y += red[q][threadIdx.x].y;
+    }
+    part[(int64_t)blockIdx.x * J + j0 + threadIdx.x] = make_double2(x, y);
+  }
+}
+
+// out[j] = sum over blocks of part[b * J + j] (fixed order: deterministic).
+__global__ void multidot_final_kernel(const double2* __restrict__ part, int nblk, int J,
+                                      double2* __restrict__ out) {
+  const int j = blockIdx.x;
+  double x = 0, y = 0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+    x += part[(int64_t)b * J + j].x;
+    y += part[(int64_t)b * J + j].y;
+  }
+  __shared__ double sx[256], sy[256];
+  sx[threadIdx.x] = x;
+  sy[threadIdx.x] = y;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      sx[threadIdx.x] += sx[threadIdx.x + o];
+      sy[threadIdx.x] += sy[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[j] = make_double2(sx[0], sy[0]);
+}
+
+// w = beta*w + cscale * sum_j coef[j] V_j
+__global__ void lincomb_kernel(double2* __restrict__ w, double2 beta, const double2* __restrict__ V,
+                               int64_t ldv, int J, const double2* __restrict__ coef, double2 cscale,
+                               int64_t n) {
+  __shared__ double2 c[kMaxJ];
+  if ((int)threadIdx.x < J) {
+    const double2 a = coef[threadIdx.x];
+    c[threadIdx.x] = make_double2(a.x * cscale.x - a.y * cscale.y, a.x * cscale.y + a.y * cscale.x);
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double2 acc;
+    if (beta.x == 0.0 && beta.y == 0.0) {
+      acc = make_double2(0.0, 0.0);
+    } else {
+      const double2 wi = w[i];
+      acc = make_double2(beta.x * wi.x - beta.y * wi.y, beta.x * wi.y + beta.y * wi.x);
+    }
+    for (int j = 0; j < J; ++j) {
+      const double2 v = V[(int64_t)j * ldv + i];
+      acc.x += c[j].x * v.x - c[j].y * v.y;
+      acc.y += c[j].x * v.y + c[j].y * v.x;
+    }
+    w[i] = acc;
+  }
+}
+
+__global__ void axpby_kernel(int64_t n, double2 a, const double2* __restrict__ x, double2 b,
+                             double2* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 xi = x[i];
+    double2 yi = make_double2(0.0, 0.0);
+    if (b.x != 0.0 || b.y != 0.0) {
+      const double2 t = y[i];
+      yi = make_double2(b.x * t.x - b.y * t.y, b.x * t.y + b.y * t.x);
+    }
+    yi.x += a.x * xi.x - a.y * xi.y;
+    yi.y += a.x * xi.y + a.y * xi.x;
+    y[i] = yi;
+  }
+}
+
+__global__ void c64_to_c128_kernel(const float2* __restrict__ x, double2* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = make_double2(x[i].x, x[i].y);
+}
+
+__global__ void fill_kernel(double2* __restrict__ x, double2 v, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = v;
+}
+
+__global__ void conj_kernel(double2* __restrict__ x, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i].y = -x[i].y;
+}
+
+__global__ void transpose_kernel(const double2* __restrict__ in, int64_t rows, int64_t cols,
+                                 double2* __restrict__ out) {
+  __shared__ double2 tile[32][33];
+  const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int64_t rr = r0 + r, cc = c0 + threadIdx.x;
+    if (rr < rows && cc < cols) tile[r][threadIdx.x] = in[rr * cols + cc];
+  }
+  __syncthreads();
+  for (int c = threadIdx.y; c < 32; c += 8) {
+    const int64_t cc = c0 + c, rr = r0 + threadIdx.x;
+    if (rr < rows && cc < cols) out[cc * rows + rr] = tile[threadIdx.x][c];
+  }
+}
+
+__global__ void zero_lower_kernel(double2* __restrict__ R, int64_t rows, int64_t cols) {
+  const int64_t total = rows * cols;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / cols, c = i - r * cols;
+    if (c < r) R[i] = make_double2(0.0, 0.0);
+  }
+}
+
+__global__ void diag_scale_kernel(double2* __restrict__ A, int64_t rows, int64_t cols,
+                                  const double* __restrict__ d, int side) {
+  const int64_t total = rows * cols;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / cols;
+    const double f = side == 0 ? d[i - r * cols] : d[r];
+    A[i].x *= f;
+    A[i].y *= f;
+  }
+}
+
+inline unsigned grid_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 8) b = 152 * 8;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+int multidot_blocks(gtn_ctx ctx) { return (ctx->sm_count > 0 ? ctx->sm_count : 152) * 2; }
+
+cudaError_t launch_multidot(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
+                            double2* out, double2* scratch, int nblk, cudaStream_t s) {
+  if (J <= 0) return cudaSuccess;
+  if (J > kMaxJ) return cudaErrorInvalidValue;
+  for (int j0 = 0; j0 < J; j0 += 8) {
+    multidot_partial_kernel<8><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+  }
+  multidot_final_kernel<<<J, 256, 0, s>>>(scratch, nblk, J, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lincomb(double2* w, double2 beta, const double2* V, int64_t ldv, int J,
+                           const double2* coef, double2 cscale, int64_t n, cudaStream_t s) {
+  if (J > kMaxJ) return cudaErrorInvalidValue;
+  lincomb_kernel<<<grid_for(n), 256, 0, s>>>(w, beta, V, ldv, J, coef, cscale, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_axpby(int64_t n, double2 a, const double2* x, double2 b, double2* y, cudaStream_t s) {
+  axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, a, x, b, y);
+  return cudaGetLastError();
+}
+cudaError_t launch_c64_to_c128(const float2* x, double2* y, int64_t n, cudaStream_t s) {
+  c64_to_c128_kernel<<<grid_for(n), 256, 0, s>>>(x, y, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_fill_c128(double2* x, double2 v, int64_t n, cudaStream_t s) {
+  fill_kernel<<<grid_for(n), 256, 0, s>>>(x, v, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_conj_inplace(double2* x, int64_t n, cudaStream_t s) {
+  conj_kernel<<<grid_for(n), 256, 0, s>>>(x, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_transpose_c128(const double2* in, int64_t rows, int64_t cols, double2* out,
+                                  cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return cudaSuccess;
+  const int64_t gy = (rows + 31) / 32;
+  if (gy > 65535) return cudaErrorInvalidConfiguration;
+  transpose_kernel<<<dim3((unsigned)((cols + 31) / 32), (unsigned)gy), dim3(32, 8), 0, s>>>(in, rows, cols, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_zero_lower(double2* R, int64_t rows, int64_t cols, cudaStream_t s) {
+  zero_lower_kernel<<<grid_for(rows * cols), 256, 0, s>>>(R, rows, cols);
+  return cudaGetLastError();
+}
+cudaError_t launch_diag_scale(double2* A, int64_t rows, int64_t cols, const double* d, int side,
+                              cudaStream_t s) {
+  diag_scale_kernel<<<grid_for(rows * cols), 256, 0, s>>>(A, rows, cols, d, side);
+  return cudaGetLastError();
+}

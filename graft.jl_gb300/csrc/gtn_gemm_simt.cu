@@ -1,0 +1,109 @@
+// Complex SIMT GEMMs for the FP64 path (DFMA) and the FP32 diagnostic path (FFMA).
+//   C[n][m] = sum_k A[m][k] * B[n][k]      A: [M][K], B: [N][K], C: [N][M] (row-major)
+// The output is written m-fastest so that each warp's stores are contiguous.
+#include "gtn_internal.h"
+
+namespace {
+
+template <typename T> struct CT;
+template <> struct CT<double2> {
+  using R = double;
+  __device__ static double2 zero() { return make_double2(0.0, 0.0); }
+};
+template <> struct CT<float2> {
+  using R = float;
+  __device__ static float2 zero() { return make_float2(0.f, 0.f); }
+};
+
+constexpr int BM = 64, BN = 64, BK = 16;
+
+// 256 threads; thread (tx = tid % 16, ty = tid / 16) owns m = tx + 16*i, n = ty + 16*j.
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_simt_kernel(const T* __restrict__ A, const T* __restrict__ B,
+                                                        T* __restrict__ C, int64_t M, int64_t N,
+                                                        int64_t K) {
+  using R = typename CT<T>::R;
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int64_t m0 = (int64_t)blockIdx.x * BM;
+  const int64_t n0 = (int64_t)blockIdx.y * BN;
+  R acc_r[4][4], acc_i[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { acc_r[i][j] = 0; acc_i[i][j] = 0; }
+
+  for (int64_t k0 = 0; k0 < K; k0 += BK) {
+    // load A tile: BM rows x BK cols = 1024 elements, 4 per thread; lanes walk k.
+#pragma unroll
+    for (int l = 0; l < (BM * BK) / 256; ++l) {
+      const int e = tid + l * 256;
+      const int r = e / BK, c = e % BK;
+      const int64_t m = m0 + r, k = k0 + c;
+      As[c][r] = (m < M && k < K) ? A[m * K + k] : CT<T>::zero();
+    }
+#pragma unroll
+    for (int l = 0; l < (BN * BK) / 256; ++l) {
+      const int e = tid + l * 256;
+      const int r = e / BK, c = e % BK;
+      const int64_t n = n0 + r, k = k0 + c;
+      Bs[c][r] = (n < N && k < K) ? B[n * K + k] : CT<T>::zero();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < BK; ++kk) {
+      T a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          acc_r[i][j] = fma(a[i].x, b[j].x, acc_r[i][j]);
+          acc_r[i][j] = fma(-a[i].y, b[j].y, acc_r[i][j]);
+          acc_i[i][j] = fma(a[i].x, b[j].y, acc_i[i][j]);
+          acc_i[i][j] = fma(a[i].y, b[j].x, acc_i[i][j]);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int64_t n = n0 + ty + 16 * j;
+    if (n >= N) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t m = m0 + tx + 16 * i;
+      if (m < M) {
+        T v;
+        v.x = acc_r[i][j];
+        v.y = acc_i[i][j];
+        C[n * M + m] = v;
+      }
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, cudaStream_t s) {
+  if (M <= 0 || N <= 0) return cudaSuccess;
+  const int64_t gx = (M + BM - 1) / BM, gy = (N + BN - 1) / BN;
+  if (gy > 65535) return cudaErrorInvalidConfiguration;
+  gemm_simt_kernel<T><<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(A, B, C, M, N, K);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_zgemm_simt(const double2* A, const double2* B, double2* C, int64_t M, int64_t N,
+                              int64_t K, cudaStream_t s) {
+  return launch(A, B, C, M, N, K, s);
+}
+cudaError_t launch_cgemm_simt(const float2* A, const float2* B, float2* C, int64_t M, int64_t N,
+                              int64_t K, cudaStream_t s) {
+  return launch(A, B, C, M, N, K, s);
+}

@@ -1,0 +1,363 @@
+// tcgen05 split-precision GEMM for sm_103a.
+//
+// Real GEMM  C_real[M x 2N] = A_real[M x 2K] * B'_real[2N x 2K]^T  on bf16 slice planes,
+// FP32 accumulation in TMEM.  A_real is the complex operand with (re, im) interleaved
+// along K; B' is the expanded static operand [[Br, -Bi], [Bi, Br]] so that column pair
+// (2n, 2n+1) of C_real is the complex output n.  Split precision: A ~ sum_p A_p,
+// B' ~ sum_q B_q (bf16 slices); the product list (p, q) is accumulated into one TMEM
+// accumulator as a longer K loop.
+//
+// One CTA (128 threads) per 128 x BN output tile:
+//   warp 0 lane 0 : TMA producer (cp.async.bulk.tensor.3d, SWIZZLE_128B, no multicast)
+//   warp 1 lane 0 : tcgen05.mma issuer (kind::f16, bf16 x bf16 -> f32)
+//   warp 2        : TMEM allocator
+//   warps 0-3     : epilogue (tcgen05.ld 32x32b -> complex FP32 stores, m-fastest)
+// Every mbarrier wait is bounded (globaltimer, 4 s); on timeout the CTA records an error
+// code in the context's device flag, drains its own copies and MMAs, frees TMEM, returns.
+#include "gtn_internal.h"
+#include <cuda.h>
+
+namespace {
+
+constexpr int BM = 128;
+constexpr int BKE = 64;  // bf16 elements per k-block = 128 bytes = one SW128 row
+constexpr int A_BYTES = BM * BKE * 2;
+constexpr uint64_t kTimeoutNs = 4000000000ull;
+
+struct ProdList {
+  int n;
+  int a[9];
+  int b[9];
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait on a phase parity.  Returns false on timeout or when another role of the
+// CTA has already aborted.
+__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255u) == 255u) {
+      if (*abort_flag) return false;
+      const uint64_t now = globaltimer();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kTimeoutNs) return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* tm, uint64_t* bar, int x,
+                                            int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;            // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024u >> 4) << 32;  // stride byte offset
+  d |= (uint64_t)1u << 46;            // descriptor version
+  d |= (uint64_t)2u << 61;            // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D=f32, A=B=bf16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <int BN> struct Cfg {
+  static constexpr int B_BYTES = BN * BKE * 2;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int STAGES = (196608 / STAGE_BYTES) > 8 ? 8 : (196608 / STAGE_BYTES);
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024;
+  static constexpr uint32_t TMEM_COLS = BN < 32 ? 32 : BN;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   float2* __restrict__ C, int64_t M, int64_t N, int nkb, ProdList prods,
+                   int* __restrict__ errflag) {
+  using CF = Cfg<BN>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~static_cast<uintptr_t>(1023));
+  __shared__ __align__(8) uint64_t full_bar[CF::STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[CF::STAGES];
+  __shared__ __align__(8) uint64_t accum_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  __shared__ int n_issued, n_consumed;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < CF::STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(&accum_bar, 1);
+    abort_flag = 0;
+    n_issued = 0;
+    n_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(CF::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem_d = tmem_slot;
+
+  const int total = prods.n * nkb;
+  const int m0 = blockIdx.x * BM;
+  const int r0 = blockIdx.y * BN;  // first real output column (row of B')
+
+  if (warp == 0 && lane == 0) {
+    int it = 0;
+    for (; it < total; ++it) {
+      const int s = it % CF::STAGES;
+      const uint32_t ph = (uint32_t)(it / CF::STAGES) & 1u;
+      if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_flag)) {
+        abort_flag = 1;
+        atomicCAS(errflag, 0, DEVERR_TMA_TIMEOUT);
+        break;
+      }
+      const int p = it / nkb, kb = it - p * nkb;
+      const uint32_t sa = smem_u32(smem + s * CF::STAGE_BYTES);
+      const uint32_t sb = sa + A_BYTES;
+      mbar_expect_tx(&full_bar[s], CF::STAGE_BYTES);
+      tma_load_3d(sa, &tmA, &full_bar[s], kb * BKE, m0, prods.a[p]);
+      tma_load_3d(sb, &tmB, &full_bar[s], kb * BKE, r0, prods.b[p]);
+    }
+    n_issued = it;
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = idesc_bf16(BM, BN);
+    int it = 0;
+    for (; it < total; ++it) {
+      const int s = it % CF::STAGES;
+      const uint32_t ph = (uint32_t)(it / CF::STAGES) & 1u;
+      if (!mbar_wait(&full_bar[s], ph, &abort_flag)) {
+        abort_flag = 1;
+        atomicCAS(errflag, 0, DEVERR_MMA_TIMEOUT);
+        break;
+      }
+      fence_after();
+      const uint32_t sa = smem_u32(smem + s * CF::STAGE_BYTES);
+      const uint32_t sb = sa + A_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < BKE / 16; ++kk) {
+        umma_bf16(tmem_d, sdesc(sa + kk * 32), sdesc(sb + kk * 32), idesc,
+                  (it > 0 || kk > 0) ? 1u : 0u);
+      }
+      umma_commit(&empty_bar[s]);
+    }
+    n_consumed = it;
+    umma_commit(&accum_bar);  // arrives once every MMA issued above has completed
+  }
+  __syncwarp();
+
+  // ---- epilogue: TMEM -> registers -> complex FP32 stores (C[n][m], m fastest) ----------
+  const bool ok = mbar_wait(&accum_bar, 0u, &abort_flag);
+  if (!ok && lane == 0) {
+    abort_flag = 1;
+    atomicCAS(errflag, 0, DEVERR_EPI_TIMEOUT);
+  }
+  __syncwarp();
+  fence_after();
+  if (ok) {
+    const int row = warp * 32 + lane;
+    const int64_t m = (int64_t)m0 + row;
+    const uint32_t taddr = tmem_d + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c = 0; c < BN; c += 16) {
+      uint32_t v[16];
+      tmem_ld16(taddr + (uint32_t)c, v);
+      if (m < M) {
+        const int64_t nb = (int64_t)(r0 + c) >> 1;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int64_t n = nb + j;
+          if (n < N) C[n * M + m] = make_float2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  // Drain: copies issued but never consumed (abort path only) must land before exit.
+  if (threadIdx.x == 0) {
+    for (int it = n_consumed; it < n_issued; ++it) {
+      volatile int no_abort = 0;
+      mbar_wait(&full_bar[it % CF::STAGES], (uint32_t)(it / CF::STAGES) & 1u, &no_abort);
+    }
+  }
+  __syncthreads();
+  if (warp == 2) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d),
+                 "r"(CF::TMEM_COLS)
+                 : "memory");
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// 3-D map over bf16 planes: (2Kp elements, rows, planes), box (64, box_rows, 1).
+bool make_map(CUtensorMap* tm, const void* base, int64_t Kp, int64_t rows, int planes, int box_rows,
+              std::string* why) {
+  EncodeTiledFn enc = get_encode();
+  if (!enc) {
+    if (why) *why = "cuTensorMapEncodeTiled unavailable";
+    return false;
+  }
+  cuuint64_t gdim[3] = {(cuuint64_t)(2 * Kp), (cuuint64_t)rows, (cuuint64_t)planes};
+  cuuint64_t gstr[2] = {(cuuint64_t)(2 * Kp * 2), (cuuint64_t)(rows * 2 * Kp * 2)};
+  cuuint32_t box[3] = {(cuuint32_t)BKE, (cuuint32_t)box_rows, 1u};
+  cuuint32_t estr[3] = {1u, 1u, 1u};
+  CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), gdim, gstr, box,
+                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    if (why) *why = "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")";
+    return false;
+  }
+  return true;
+}
+
+template <int BN>
+cudaError_t launch_bn(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why) {
+  using CF = Cfg<BN>;
+  CUtensorMap tmA, tmB;
+  if (!make_map(&tmA, a.A, a.Kp, a.M, a.a_planes, BM, why)) return cudaErrorInvalidValue;
+  if (!make_map(&tmB, a.B, a.Kp, 2 * a.N, a.b_planes, BN, why)) return cudaErrorInvalidValue;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         CF::SMEM);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  ProdList pl;
+  pl.n = a.nprod;
+  for (int i = 0; i < 9; ++i) {
+    pl.a[i] = i < a.nprod ? a.prod_a[i] : 0;
+    pl.b[i] = i < a.nprod ? a.prod_b[i] : 0;
+  }
+  const int nkb = (int)((2 * a.Kp + BKE - 1) / BKE);
+  const int64_t gx = (a.M + BM - 1) / BM;
+  const int64_t gy = (2 * a.N + BN - 1) / BN;
+  if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
+  tc_gemm_kernel<BN><<<dim3((unsigned)gx, (unsigned)gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb,
+                                                                              pl, errflag);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool tc_gemm_supported(int cc_major, int cc_minor) {
+  (void)cc_minor;
+  return cc_major == 10 && get_encode() != nullptr;
+}
+
+cudaError_t launch_tc_gemm(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why) {
+  if (a.M <= 0 || a.N <= 0) return cudaSuccess;
+  if (a.Kp % 32 != 0 || a.nprod < 1 || a.nprod > 9) {
+    if (why) *why = "tc_gemm: Kp must be a multiple of 32 and 1..9 products";
+    return cudaErrorInvalidValue;
+  }
+  if (reinterpret_cast<uintptr_t>(a.A) % 16 || reinterpret_cast<uintptr_t>(a.B) % 16) {
+    if (why) *why = "tc_gemm: operand planes must be 16-byte aligned";
+    return cudaErrorInvalidValue;
+  }
+  const int64_t n2 = 2 * a.N;
+  if (n2 <= 32) return launch_bn<32>(a, errflag, s, why);
+  if (n2 <= 64) return launch_bn<64>(a, errflag, s, why);
+  if (n2 <= 128) return launch_bn<128>(a, errflag, s, why);
+  return launch_bn<256>(a, errflag, s, why);
+}

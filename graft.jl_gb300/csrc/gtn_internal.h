@@ -1,0 +1,175 @@
+// Internal declarations shared by the libgrafttn translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <memory>
+
+#include "../../include/grafttn.h"
+
+#define GTN_MAXG 8
+
+// A multi-index group: index i in [0, prod(dim)) decomposes into digits (outer..inner)
+// whose strides (in elements) give the offset into a row-major tensor.
+struct GroupSpec {
+  int n;
+  int64_t dim[GTN_MAXG];
+  int64_t str[GTN_MAXG];
+};
+
+// Device error codes written to the context's error flag by bounded waits.
+enum : int { DEVERR_NONE = 0, DEVERR_TMA_TIMEOUT = 1, DEVERR_MMA_TIMEOUT = 2, DEVERR_EPI_TIMEOUT = 3 };
+
+struct gtn_ctx_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  int64_t launches = 0;
+  int* d_errflag = nullptr;
+  int sm_count = 0;
+  int cc_major = 0, cc_minor = 0;
+  // reduction scratch (device + pinned host)
+  double2* d_red = nullptr;
+  size_t red_cap = 0;
+  double2* h_red = nullptr;
+  size_t hred_cap = 0;
+  // transient workspace for one-shot contractions / factorisations
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  void* cusolver = nullptr;
+};
+
+// ---- status helpers -------------------------------------------------------------
+int set_err(gtn_ctx ctx, int code, const std::string& msg);
+#define GTN_CUDA_TRY(ctx, expr)                                                       \
+  do {                                                                                \
+    cudaError_t e__ = (expr);                                                         \
+    if (e__ != cudaSuccess)                                                           \
+      return set_err((ctx), GTN_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e__)); \
+  } while (0)
+
+cudaError_t ctx_workspace(gtn_ctx ctx, size_t bytes, void** out);
+cudaError_t ctx_red(gtn_ctx ctx, size_t n2);   // ensure d_red/h_red hold n2 double2
+void linalg_release(gtn_ctx ctx);               // drop the cuSOLVER handle (gtn_linalg.cu)
+
+// ---- layout kernels (gtn_layout.cu) ----------------------------------------------
+// out[m, k] = T[offM(m) + offK(k)] for m < M, k < Kw (zero where k >= K).
+cudaError_t launch_gather_c128_to_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                       int64_t M, int64_t K, int64_t ldo, double2* out, cudaStream_t s);
+cudaError_t launch_gather_c128_to_c64(const double2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                      int64_t M, int64_t K, int64_t ldo, float2* out, cudaStream_t s);
+cudaError_t launch_gather_c64_to_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                     int64_t M, int64_t K, int64_t ldo, float2* out, cudaStream_t s);
+cudaError_t launch_gather_c64_to_c128(const float2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                      int64_t M, int64_t K, int64_t ldo, double2* out, cudaStream_t s);
+// Split into bf16 planes: plane p at out + p*pstride, row m at m*ld2, complex k at 2k.
+// Columns K <= k < Kp are written as zero (TMA reads the padded extent).
+cudaError_t launch_split_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M,
+                              int64_t K, int64_t Kp, int nplanes, int64_t pstride,
+                              __nv_bfloat16* out, cudaStream_t s);
+cudaError_t launch_split_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M,
+                             int64_t K, int64_t Kp, int nplanes, int64_t pstride,
+                             __nv_bfloat16* out, cudaStream_t s);
+// Expanded real operand of a static B [N][K] (complex, row-major) for the tcgen05 path:
+// rows (n, c_out), columns (k, c_in): [[Br, -Bi], [Bi, Br]], split into bf16 planes.
+cudaError_t launch_pack_b_planes(const double2* B, int64_t N, int64_t K, int64_t Kp, int nplanes,
+                                 int64_t pstride, __nv_bfloat16* out, cudaStream_t s);
+
+// C[n][m] = sum_k T[offM(m) + offK(k)] * B[n][k]   (small K; B in shared memory)
+cudaError_t launch_small_contract_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                       int64_t M, int K, int N, const double2* B, double2* C,
+                                       cudaStream_t s);
+cudaError_t launch_small_contract_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                      int64_t M, int K, int N, const float2* B, float2* C,
+                                      cudaStream_t s);
+bool small_contract_fits(int K, int N, size_t elem_bytes);
+
+// ---- SIMT GEMMs (gtn_gemm_simt.cu): C[n][m] = sum_k A[m][k] B[n][k] -----------------
+cudaError_t launch_zgemm_simt(const double2* A, const double2* B, double2* C, int64_t M, int64_t N,
+                              int64_t K, cudaStream_t s);
+cudaError_t launch_cgemm_simt(const float2* A, const float2* B, float2* C, int64_t M, int64_t N,
+                              int64_t K, cudaStream_t s);
+
+// ---- tcgen05 GEMM (gtn_gemm_tc.cu) ---------------------------------------------------
+// Real GEMM on bf16 slice planes: C (complex fp32, [N][M]) from A planes [P][M][2Kp] and
+// B planes [P][2N][2Kp].  prods lists (a_plane, b_plane) pairs accumulated in order.
+struct TcGemmArgs {
+  const __nv_bfloat16* A;  // planes, pitch 2Kp elements per row
+  const __nv_bfloat16* B;
+  float2* C;
+  int64_t M, N, Kp;        // complex dims; Kp = padded K (multiple of 32)
+  int a_planes, b_planes;  // number of planes stored (for the tensor-map extents)
+  int nprod;
+  int prod_a[9], prod_b[9];
+};
+cudaError_t launch_tc_gemm(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why);
+bool tc_gemm_supported(int cc_major, int cc_minor);
+
+// ---- vector kernels (gtn_blas.cu) --------------------------------------------------
+cudaError_t launch_multidot(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
+                            double2* out /*[J]*/, double2* scratch, int nblk, cudaStream_t s);
+cudaError_t launch_lincomb(double2* w, double2 beta, const double2* V, int64_t ldv, int J,
+                           const double2* coef /*device [J]*/, double2 cscale, int64_t n,
+                           cudaStream_t s);
+cudaError_t launch_axpby(int64_t n, double2 a, const double2* x, double2 b, double2* y,
+                         cudaStream_t s);
+cudaError_t launch_c64_to_c128(const float2* x, double2* y, int64_t n, cudaStream_t s);
+cudaError_t launch_fill_c128(double2* x, double2 v, int64_t n, cudaStream_t s);
+cudaError_t launch_conj_inplace(double2* x, int64_t n, cudaStream_t s);
+cudaError_t launch_transpose_c128(const double2* in, int64_t rows, int64_t cols, double2* out,
+                                  cudaStream_t s);  // out[c][r] = in[r][c]
+cudaError_t launch_zero_lower(double2* R, int64_t rows, int64_t cols, cudaStream_t s);
+cudaError_t launch_diag_scale(double2* A, int64_t rows, int64_t cols, const double* d, int side,
+                              cudaStream_t s);
+int multidot_blocks(gtn_ctx ctx);
+
+// ---- plans (gtn_plan.cpp) ----------------------------------------------------------
+struct PlanStep {
+  int operand;             // static operand absorbed
+  bool small;              // strided SIMT path (no permute)
+  bool tc;                 // tcgen05 path (mixed precisions only)
+  int64_t M, K, N, Kp;
+  GroupSpec mg, kg;        // access of the running tensor as [M, K]
+  std::vector<int> out_labels;       // labels of C = [N legs..., M legs...]
+  std::vector<int64_t> out_dims;
+  int64_t out_elems;
+  // packed static operand (owned by the map)
+  double2* b64 = nullptr;          // [N][K] c128 (conj applied)
+  float2* b32 = nullptr;           // [N][K] c64
+  __nv_bfloat16* bpl = nullptr;    // [P][2N][2Kp] slice planes
+  int bplanes = 0;
+  double macs = 0;
+};
+
+struct gtn_map_s {
+  gtn_ctx ctx = nullptr;
+  int precision = 0;
+  std::vector<int64_t> x_dims, y_dims;
+  int64_t x_elems = 0, y_elems = 0;
+  std::vector<PlanStep> steps;
+  GroupSpec fin_mg, fin_kg;  // final permute of the last C into y order
+  int64_t fin_M = 0, fin_K = 0;
+  bool fin_identity = false;
+  double flops = 0;
+  int64_t max_t = 0;       // largest running tensor (elements)
+  int64_t max_a = 0;       // largest A operand (elements, for permuted / split staging)
+  int64_t max_apl = 0;     // largest split-plane staging (bf16 elements per plane * planes)
+  // device workspace owned by the map
+  void* buf0 = nullptr; void* buf1 = nullptr; void* abuf = nullptr;
+  void* dx = nullptr; void* dy = nullptr;     // staging for the host-buffer entry point
+  int64_t bytes = 0;
+  std::vector<void*> owned;
+  // Krylov scratch
+  double2* kv = nullptr; int kv_cap = 0;     // (krylovdim+1) vectors
+  double2* kcoef = nullptr; double2* kscratch = nullptr; int kscratch_cap = 0;
+};
+
+int plan_build(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dims,
+               const int* labels, const int* conj, const int* order, const void* const* statics,
+               int precision, gtn_map map);
+int map_run(gtn_map map, int precision, const double2* x, double2* y);
+void map_free(gtn_map map);

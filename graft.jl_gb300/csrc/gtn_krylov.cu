@@ -1,0 +1,343 @@
+// Device-resident Krylov solvers: the eigsolve / exponentiate hooks of the reference
+// (lib/GraftGroundState/src/GroundState/GroundState.jl:25-39,
+//  lib/GraftEvolution/src/Evolution/Evolution.jl:54-68).
+//
+// Krylov vectors live in HBM as complex FP64.  Each Lanczos step applies the map (in its
+// precision mode), then runs two passes of classical Gram-Schmidt against the whole basis
+// in FP64 (batched projections h = V^H w and one linear combination per pass), then
+// normalises.  Only the tridiagonal coefficients cross to the host; the small symmetric
+// eigenproblem is solved there by cyclic Jacobi rotations.
+#include "gtn_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+
+namespace {
+
+constexpr int kMaxKrylov = 63;
+
+// Cyclic Jacobi eigen-decomposition of a symmetric n x n matrix (row-major A, destroyed).
+// On return w holds eigenvalues ascending and V's columns the matching eigenvectors.
+void jacobi_eig(int n, std::vector<double>& A, std::vector<double>& w, std::vector<double>& V) {
+  V.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
+  auto a = [&](int i, int j) -> double& { return A[(size_t)i * n + j]; };
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0, diag = 0;
+    for (int p = 0; p < n; ++p) {
+      diag += a(p, p) * a(p, p);
+      for (int q = p + 1; q < n; ++q) off += a(p, q) * a(p, q);
+    }
+    if (off <= 1e-32 * (diag + 1e-300)) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = a(p, q);
+        if (std::fabs(apq) < 1e-300) continue;
+        const double theta = (a(q, q) - a(p, p)) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {  // columns p, q
+          const double akp = a(k, p), akq = a(k, q);
+          a(k, p) = c * akp - s * akq;
+          a(k, q) = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // rows p, q
+          const double apk = a(p, k), aqk = a(q, k);
+          a(p, k) = c * apk - s * aqk;
+          a(q, k) = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double vkp = V[(size_t)k * n + p], vkq = V[(size_t)k * n + q];
+          V[(size_t)k * n + p] = c * vkp - s * vkq;
+          V[(size_t)k * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](int x, int y) { return a(x, x) < a(y, y); });
+  std::vector<double> V2((size_t)n * n);
+  w.resize(n);
+  for (int j = 0; j < n; ++j) {
+    w[j] = a(idx[j], idx[j]);
+    for (int k = 0; k < n; ++k) V2[(size_t)k * n + j] = V[(size_t)k * n + idx[j]];
+  }
+  V.swap(V2);
+}
+
+struct Krylov {
+  gtn_map map;
+  gtn_ctx ctx;
+  int64_t n;
+  double2* V;       // (kd+1) x n
+  double2* coef;    // device coefficient area: [0,64) h1, [64,128) h2, [128] norm^2, [192,256) lincomb
+  double2* part;    // multidot partials
+  int nblk;
+};
+
+int krylov_setup(gtn_map map, int kd, Krylov* K) {
+  gtn_ctx ctx = map->ctx;
+  if (kd < 1 || kd > kMaxKrylov) return set_err(ctx, GTN_ERR_INVALID, "krylovdim must be in 1..63");
+  if (map->x_elems != map->y_elems) return set_err(ctx, GTN_ERR_SHAPE, "Krylov solvers need a square map");
+  K->map = map;
+  K->ctx = ctx;
+  K->n = map->x_elems;
+  K->nblk = multidot_blocks(ctx);
+  if (map->kv_cap < kd + 1) {
+    if (map->kv) cudaFree(map->kv);
+    map->kv = nullptr;
+    map->kv_cap = 0;
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    const size_t need = (size_t)(kd + 1) * K->n * sizeof(double2);
+    if (need + (size_t(1) << 30) > freeb)
+      return set_err(ctx, GTN_ERR_MEMORY, "memory admission refused: Krylov basis needs " +
+                                              std::to_string(need >> 20) + " MiB");
+    if (cudaMalloc(&map->kv, need) != cudaSuccess) return set_err(ctx, GTN_ERR_MEMORY, "Krylov basis allocation failed");
+    map->kv_cap = kd + 1;
+  }
+  if (!map->kcoef) {
+    if (cudaMalloc(&map->kcoef, 256 * sizeof(double2)) != cudaSuccess)
+      return set_err(ctx, GTN_ERR_MEMORY, "Krylov coefficient allocation failed");
+    map->owned.push_back(map->kcoef);
+  }
+  if (map->kscratch_cap < K->nblk * 64) {
+    if (map->kscratch) cudaFree(map->kscratch);
+    if (cudaMalloc(&map->kscratch, (size_t)K->nblk * 64 * sizeof(double2)) != cudaSuccess)
+      return set_err(ctx, GTN_ERR_MEMORY, "Krylov scratch allocation failed");
+    map->kscratch_cap = K->nblk * 64;
+  }
+  K->V = map->kv;
+  K->coef = map->kcoef;
+  K->part = map->kscratch;
+  GTN_CUDA_TRY(ctx, ctx_red(ctx, 64));
+  return GTN_OK;
+}
+
+// ||x||^2 into coef[slot] (device)
+cudaError_t norm2_dev(Krylov& K, const double2* x, double2* dst) {
+  K.ctx->launches += 2;
+  return launch_multidot(x, 0, 1, x, K.n, dst, K.part, K.nblk, K.ctx->stream);
+}
+
+// Copy `cnt` double2 from device to host and wait; reports device-side wait timeouts.
+int fetch(Krylov& K, const double2* dsrc, int cnt, double2* out) {
+  gtn_ctx ctx = K.ctx;
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_red, dsrc, cnt * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+  int st = gtn_ctx_sync(ctx);
+  if (st != GTN_OK) return st;
+  for (int i = 0; i < cnt; ++i) out[i] = ctx->h_red[i];
+  return GTN_OK;
+}
+
+int push(Krylov& K, const std::vector<double2>& c, double2* ddst) {
+  gtn_ctx ctx = K.ctx;
+  for (size_t i = 0; i < c.size(); ++i) ctx->h_red[64 + i] = c[i];
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(ddst, ctx->h_red + 64, c.size() * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+  // the pinned staging area is reused on the next call: wait for the copy
+  GTN_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return GTN_OK;
+}
+
+// x <- x / ||x||, returns the norm.
+int normalize(Krylov& K, double2* x, double* nrm) {
+  GTN_CUDA_TRY(K.ctx, norm2_dev(K, x, K.coef + 128));
+  double2 h;
+  int st = fetch(K, K.coef + 128, 1, &h);
+  if (st != GTN_OK) return st;
+  *nrm = std::sqrt(std::max(h.x, 0.0));
+  if (*nrm > 0) {
+    GTN_CUDA_TRY(K.ctx, launch_axpby(K.n, make_double2(1.0 / *nrm, 0.0), x, make_double2(0.0, 0.0), x, K.ctx->stream));
+    K.ctx->launches++;
+  }
+  return GTN_OK;
+}
+
+// One Lanczos expansion from V[0] (unit norm).  Fills a[0..m), b[0..m) and returns m (the
+// number of basis vectors).  Stops early at an invariant subspace, or when `stop` says so.
+template <class Stop>
+int lanczos_expand(Krylov& K, int kd, int precision, std::vector<double>& a, std::vector<double>& b,
+                   int* m_out, int* matvecs, bool* breakdown, Stop stop) {
+  gtn_ctx ctx = K.ctx;
+  cudaStream_t s = ctx->stream;
+  a.assign(kd, 0.0);
+  b.assign(kd, 0.0);
+  *breakdown = false;
+  int m = kd;
+  for (int j = 0; j < kd; ++j) {
+    double2* vj = K.V + (int64_t)j * K.n;
+    double2* w = K.V + (int64_t)(j + 1) * K.n;
+    int st = map_run(K.map, precision, vj, w);
+    if (st != GTN_OK) return st;
+    (*matvecs)++;
+    // two classical Gram-Schmidt passes against V[0..j]
+    GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef, K.part, K.nblk, s));
+    GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef, make_double2(-1.0, 0.0), K.n, s));
+    GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
+    GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
+    GTN_CUDA_TRY(ctx, norm2_dev(K, w, K.coef + 128));
+    ctx->launches += 2 * ((j + 8) / 8 + 1) + 2;
+    double2 hbuf[130];
+    st = fetch(K, K.coef, 130, hbuf);  // h (0..63), h2 (64..127), |w|^2 (128)
+    if (st != GTN_OK) return st;
+    const double2 nn = hbuf[128];
+    a[j] = hbuf[j].x + hbuf[64 + j].x;
+    const double beta = std::sqrt(std::max(nn.x, 0.0));
+    b[j] = beta;
+    if (beta <= 1e-13 * std::max(1.0, std::fabs(a[j]))) {
+      m = j + 1;
+      *breakdown = true;
+      break;
+    }
+    GTN_CUDA_TRY(ctx, launch_axpby(K.n, make_double2(1.0 / beta, 0.0), w, make_double2(0.0, 0.0), w, s));
+    ctx->launches++;
+    if (stop(j + 1, a, b)) {
+      m = j + 1;
+      break;
+    }
+  }
+  *m_out = m;
+  return GTN_OK;
+}
+
+void tridiag_eig(int m, const std::vector<double>& a, const std::vector<double>& b, std::vector<double>& w,
+                 std::vector<double>& Q) {
+  std::vector<double> T((size_t)m * m, 0.0);
+  for (int i = 0; i < m; ++i) {
+    T[(size_t)i * m + i] = a[i];
+    if (i + 1 < m) {
+      T[(size_t)i * m + i + 1] = b[i];
+      T[(size_t)(i + 1) * m + i] = b[i];
+    }
+  }
+  jacobi_eig(m, T, w, Q);
+}
+
+}  // namespace
+
+extern "C" int gtn_lanczos_min(gtn_map map, void* xv, int krylovdim, double tol, int maxiter, int rq_fp64,
+                               double* energy, int* info, double* resid) {
+  if (!map || !xv || !energy) return GTN_ERR_INVALID;
+  Krylov K;
+  int st = krylov_setup(map, std::min<int64_t>(krylovdim, std::max<int64_t>(map->x_elems, 1)), &K);
+  if (st != GTN_OK) return st;
+  gtn_ctx ctx = K.ctx;
+  double2* x = static_cast<double2*>(xv);
+  const int kd = (int)std::min<int64_t>(krylovdim, K.n);
+  int matvecs = 0, restarts = 0;
+  bool converged = false;
+  double theta = 0, res = 0;
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(K.V, x, K.n * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
+  double nrm;
+  st = normalize(K, K.V, &nrm);
+  if (st != GTN_OK) return st;
+  if (nrm == 0) return set_err(ctx, GTN_ERR_INVALID, "zero start vector");
+  std::vector<double> a, b, w, Q;
+  for (int it = 0; it < std::max(1, maxiter); ++it) {
+    restarts = it + 1;
+    int m = 0;
+    bool brk = false;
+    auto stop = [&](int mm, const std::vector<double>& aa, const std::vector<double>& bb) {
+      if (mm < 2 && kd > 1) return false;
+      std::vector<double> ww, QQ;
+      tridiag_eig(mm, aa, bb, ww, QQ);
+      const double r = std::fabs(bb[mm - 1] * QQ[(size_t)(mm - 1) * mm + 0]);
+      return r <= tol * std::max(1.0, std::fabs(ww[0]));
+    };
+    st = lanczos_expand(K, kd, map->precision, a, b, &m, &matvecs, &brk, stop);
+    if (st != GTN_OK) return st;
+    tridiag_eig(m, a, b, w, Q);
+    theta = w[0];
+    res = brk ? 0.0 : std::fabs(b[m - 1] * Q[(size_t)(m - 1) * m + 0]);
+    // Ritz vector x = sum_i Q[i,0] V_i
+    std::vector<double2> c(m);
+    for (int i = 0; i < m; ++i) c[i] = make_double2(Q[(size_t)i * m + 0], 0.0);
+    st = push(K, c, K.coef + 192);
+    if (st != GTN_OK) return st;
+    GTN_CUDA_TRY(ctx, launch_lincomb(x, make_double2(0.0, 0.0), K.V, K.n, m, K.coef + 192, make_double2(1.0, 0.0), K.n, ctx->stream));
+    ctx->launches++;
+    st = normalize(K, x, &nrm);
+    if (st != GTN_OK) return st;
+    converged = brk || res <= tol * std::max(1.0, std::fabs(theta)) || m == K.n;
+    if (converged) break;
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(K.V, x, K.n * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  double E = theta;
+  if (rq_fp64) {
+    double2* y = K.V + K.n;  // scratch slot
+    st = map_run(map, GTN_PREC_FP64, x, y);
+    if (st != GTN_OK) return st;
+    matvecs++;
+    GTN_CUDA_TRY(ctx, launch_multidot(x, 0, 1, y, K.n, K.coef + 130, K.part, K.nblk, ctx->stream));
+    ctx->launches += 2;
+    double2 h;
+    st = fetch(K, K.coef + 130, 1, &h);
+    if (st != GTN_OK) return st;
+    E = h.x;
+  }
+  *energy = E;
+  if (info) {
+    info[0] = restarts;
+    info[1] = matvecs;
+    info[2] = converged ? 1 : 0;
+  }
+  if (resid) *resid = res;
+  return converged ? GTN_OK : set_err(ctx, GTN_ERR_NOT_CONVERGED, "Lanczos reached maxiter");
+}
+
+extern "C" int gtn_expm_apply(gtn_map map, double dz_re, double dz_im, void* xv, int krylovdim, double tol,
+                              int* info) {
+  if (!map || !xv) return GTN_ERR_INVALID;
+  Krylov K;
+  int st = krylov_setup(map, std::min<int64_t>(krylovdim, std::max<int64_t>(map->x_elems, 1)), &K);
+  if (st != GTN_OK) return st;
+  gtn_ctx ctx = K.ctx;
+  double2* x = static_cast<double2*>(xv);
+  const int kd = (int)std::min<int64_t>(krylovdim, K.n);
+  const std::complex<double> dz(dz_re, dz_im);
+  double remaining = 1.0, frac = 1.0;
+  int matvecs = 0, substeps = 0;
+  std::vector<double> a, b, w, Q;
+  while (remaining > 1e-14) {
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(K.V, x, K.n * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
+    double beta0;
+    st = normalize(K, K.V, &beta0);
+    if (st != GTN_OK) return st;
+    if (beta0 == 0) break;
+    int m = 0;
+    bool brk = false;
+    st = lanczos_expand(K, kd, map->precision, a, b, &m, &matvecs, &brk,
+                        [](int, const std::vector<double>&, const std::vector<double>&) { return false; });
+    if (st != GTN_OK) return st;
+    tridiag_eig(m, a, b, w, Q);
+    double step = std::min(frac, remaining);
+    std::vector<std::complex<double>> c(m);
+    for (int tries = 0; tries < 60; ++tries) {
+      for (int i = 0; i < m; ++i) {
+        std::complex<double> acc = 0;
+        for (int k = 0; k < m; ++k)
+          acc += Q[(size_t)i * m + k] * std::exp(dz * (step * w[k])) * Q[(size_t)0 * m + k];
+        c[i] = acc;
+      }
+      const double err = (brk || m < kd) ? 0.0 : beta0 * std::fabs(b[m - 1]) * std::abs(c[m - 1]);
+      if (err <= tol || step < 1e-12) break;
+      step *= 0.5;
+    }
+    std::vector<double2> cd(m);
+    for (int i = 0; i < m; ++i) cd[i] = make_double2(beta0 * c[i].real(), beta0 * c[i].imag());
+    st = push(K, cd, K.coef + 192);
+    if (st != GTN_OK) return st;
+    GTN_CUDA_TRY(ctx, launch_lincomb(x, make_double2(0.0, 0.0), K.V, K.n, m, K.coef + 192, make_double2(1.0, 0.0), K.n, ctx->stream));
+    ctx->launches++;
+    remaining -= step;
+    frac = step;
+    substeps++;
+    if (substeps > 4096) return set_err(ctx, GTN_ERR_NOT_CONVERGED, "expm: too many substeps");
+  }
+  if (info) {
+    info[0] = substeps;
+    info[1] = matvecs;
+  }
+  return gtn_ctx_sync(ctx);
+}

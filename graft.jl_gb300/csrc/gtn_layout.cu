@@ -1,0 +1,263 @@
+// Layout kernels: strided gathers (permutations), bf16 slice splitting for the tcgen05
+// operands, and the strided small-K contraction used for TTNO (W) steps.  All are
+// HBM-bound; tiles are 32x32 through shared memory so that both the read and the write
+// side are coalesced.
+#include "gtn_internal.h"
+
+namespace {
+
+__device__ __forceinline__ int64_t decompose(int64_t i, const GroupSpec& g) {
+  int64_t off = 0;
+#pragma unroll 1
+  for (int j = g.n - 1; j >= 0; --j) {
+    const int64_t d = g.dim[j];
+    const int64_t q = i / d;
+    off += (i - q * d) * g.str[j];
+    i = q;
+  }
+  return off;
+}
+
+template <typename T> struct Zero;
+template <> struct Zero<double2> { __device__ static double2 v() { return make_double2(0.0, 0.0); } };
+template <> struct Zero<float2> { __device__ static float2 v() { return make_float2(0.f, 0.f); } };
+
+__device__ __forceinline__ double2 cvt(double2 a, double2*) { return a; }
+__device__ __forceinline__ float2 cvt(double2 a, float2*) { return make_float2((float)a.x, (float)a.y); }
+__device__ __forceinline__ float2 cvt(float2 a, float2*) { return a; }
+__device__ __forceinline__ double2 cvt(float2 a, double2*) { return make_double2(a.x, a.y); }
+
+// Writer for complex outputs: out[m*ldo + k].
+template <typename Tout> struct ComplexWriter {
+  Tout* out;
+  int64_t ldo;
+  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v) const {
+    out[m * ldo + k] = cvt(v, (Tout*)nullptr);
+  }
+};
+
+// Splits x into up to 3 bf16 slices x ~ s0 + s1 + s2 (round-to-nearest each step).
+__device__ __forceinline__ void split3(double x, __nv_bfloat16* s) {
+  __nv_bfloat16 a = __double2bfloat16(x);
+  double r = x - (double)__bfloat162float(a);
+  __nv_bfloat16 b = __double2bfloat16(r);
+  r -= (double)__bfloat162float(b);
+  s[0] = a; s[1] = b; s[2] = __double2bfloat16(r);
+}
+__device__ __forceinline__ void split3(float x, __nv_bfloat16* s) {
+  __nv_bfloat16 a = __float2bfloat16_rn(x);
+  float r = x - __bfloat162float(a);
+  __nv_bfloat16 b = __float2bfloat16_rn(r);
+  r -= __bfloat162float(b);
+  s[0] = a; s[1] = b; s[2] = __float2bfloat16_rn(r);
+}
+
+// Writer for bf16 slice planes.
+struct SplitWriter {
+  __nv_bfloat16* out;
+  int64_t ld2;      // row pitch in bf16 elements (= 2*Kp)
+  int64_t pstride;  // plane pitch in bf16 elements
+  int nplanes;
+  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v) const {
+    __nv_bfloat16 sr[3], si[3];
+    split3(v.x, sr);
+    split3(v.y, si);
+    __nv_bfloat162* row = reinterpret_cast<__nv_bfloat162*>(out + m * ld2 + 2 * k);
+    for (int p = 0; p < nplanes; ++p) {
+      __nv_bfloat162 pr;
+      pr.x = sr[p];
+      pr.y = si[p];
+      *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<__nv_bfloat16*>(row) + p * pstride) = pr;
+    }
+  }
+};
+
+// Tile gather: rows m (M), columns k (K valid, Kw written).  m_fast selects whether the
+// load phase maps lanes to m (the running tensor's unit-stride leg is in M) or to k.
+template <typename Tin, class Writer>
+__global__ void __launch_bounds__(256) gather_tile_kernel(const Tin* __restrict__ T, GroupSpec mg,
+                                                          GroupSpec kg, int64_t M, int64_t K,
+                                                          int64_t Kw, int m_fast, Writer w) {
+  __shared__ int64_t offM[32];
+  __shared__ int64_t offK[32];
+  __shared__ Tin tile[32][33];
+  const int64_t m0 = (int64_t)blockIdx.x * 32;
+  const int64_t k0 = (int64_t)blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  if (ty == 0) {
+    const int64_t m = m0 + tx;
+    offM[tx] = m < M ? decompose(m, mg) : 0;
+  } else if (ty == 1) {
+    const int64_t k = k0 + tx;
+    offK[tx] = k < K ? decompose(k, kg) : 0;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int im = m_fast ? tx : r;
+    const int ik = m_fast ? r : tx;
+    const int64_t m = m0 + im, k = k0 + ik;
+    tile[im][ik] = (m < M && k < K) ? T[offM[im] + offK[ik]] : Zero<Tin>::v();
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int64_t m = m0 + r, k = k0 + tx;
+    if (m < M && k < Kw) w(m, k, tile[r][tx]);
+  }
+}
+
+inline bool choose_m_fast(const GroupSpec& mg, const GroupSpec& kg) {
+  const int64_t sm = mg.n > 0 ? mg.str[mg.n - 1] : INT64_MAX;
+  const int64_t sk = kg.n > 0 ? kg.str[kg.n - 1] : INT64_MAX;
+  return sm < sk;
+}
+
+template <typename Tin, class Writer>
+cudaError_t launch_gather(const Tin* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M,
+                          int64_t K, int64_t Kw, const Writer& w, cudaStream_t s) {
+  if (M <= 0 || Kw <= 0) return cudaSuccess;
+  const int64_t gy = (Kw + 31) / 32;
+  const int64_t gx = (M + 31) / 32;
+  if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
+  dim3 grid((unsigned)gx, (unsigned)gy), block(32, 8);
+  gather_tile_kernel<Tin, Writer><<<grid, block, 0, s>>>(T, mg, kg, M, K, Kw,
+                                                         choose_m_fast(mg, kg) ? 1 : 0, w);
+  return cudaGetLastError();
+}
+
+// Expanded static operand for the tcgen05 path.
+__global__ void pack_b_planes_kernel(const double2* __restrict__ B, int64_t N, int64_t K, int64_t Kp,
+                                     int nplanes, int64_t pstride, __nv_bfloat16* __restrict__ out) {
+  const int64_t total = 2 * N * Kp;  // (row = (n, c_out)) x (complex column k)
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = idx / Kp;
+    const int64_t k = idx - row * Kp;
+    const int64_t n = row >> 1;
+    const int c_out = (int)(row & 1);
+    double v0 = 0.0, v1 = 0.0;  // columns (k, re) and (k, im)
+    if (k < K) {
+      const double2 b = B[n * K + k];
+      if (c_out == 0) { v0 = b.x; v1 = -b.y; } else { v0 = b.y; v1 = b.x; }
+    }
+    __nv_bfloat16 s0[3], s1[3];
+    split3(v0, s0);
+    split3(v1, s1);
+    for (int p = 0; p < nplanes; ++p) {
+      __nv_bfloat162 pr;
+      pr.x = s0[p];
+      pr.y = s1[p];
+      *reinterpret_cast<__nv_bfloat162*>(out + p * pstride + row * (2 * Kp) + 2 * k) = pr;
+    }
+  }
+}
+
+__device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+__device__ __forceinline__ void cfma(float2& acc, float2 a, float2 b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(-a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(a.y, b.x, acc.y);
+}
+
+constexpr int kSmallSmemBytes = 48 * 1024;
+
+// C[n][m] = sum_k T[offM(m) + offK(k)] * B[n][k]; B and the K offsets live in shared memory.
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) small_contract_kernel(const T* __restrict__ A, GroupSpec mg,
+                                                             GroupSpec kg, int64_t M, int K, int N,
+                                                             const T* __restrict__ B,
+                                                             T* __restrict__ C) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int64_t* offK = reinterpret_cast<int64_t*>(smem_raw);
+  T* Bs = reinterpret_cast<T*>(smem_raw + ((K * sizeof(int64_t) + 15) / 16) * 16);
+  for (int i = threadIdx.x; i < K; i += blockDim.x) offK[i] = decompose(i, kg);
+  for (int i = threadIdx.x; i < N * K; i += blockDim.x) Bs[i] = B[i];
+  __syncthreads();
+  for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < M;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t om = decompose(m, mg);
+    for (int n0 = 0; n0 < N; n0 += NB) {
+      T acc[NB];
+#pragma unroll
+      for (int j = 0; j < NB; ++j) acc[j] = Zero<T>::v();
+      for (int k = 0; k < K; ++k) {
+        const T t = A[om + offK[k]];
+#pragma unroll
+        for (int j = 0; j < NB; ++j)
+          if (n0 + j < N) cfma(acc[j], t, Bs[(n0 + j) * K + k]);
+      }
+#pragma unroll
+      for (int j = 0; j < NB; ++j)
+        if (n0 + j < N) C[(int64_t)(n0 + j) * M + m] = acc[j];
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_small(const T* A, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int K,
+                         int N, const T* B, T* C, cudaStream_t s) {
+  if (M <= 0) return cudaSuccess;
+  const size_t smem = ((K * sizeof(int64_t) + 15) / 16) * 16 + (size_t)N * K * sizeof(T);
+  if (smem > (size_t)kSmallSmemBytes) return cudaErrorInvalidValue;
+  int64_t blocks = (M + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  small_contract_kernel<T, 8><<<(unsigned)blocks, 256, smem, s>>>(A, mg, kg, M, K, N, B, C);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool small_contract_fits(int K, int N, size_t elem_bytes) {
+  return ((K * sizeof(int64_t) + 15) / 16) * 16 + (size_t)N * K * elem_bytes <= (size_t)kSmallSmemBytes;
+}
+
+cudaError_t launch_gather_c128_to_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                       int64_t M, int64_t K, int64_t ldo, double2* out, cudaStream_t s) {
+  return launch_gather(T, mg, kg, M, K, K, ComplexWriter<double2>{out, ldo}, s);
+}
+cudaError_t launch_gather_c128_to_c64(const double2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                      int64_t M, int64_t K, int64_t ldo, float2* out, cudaStream_t s) {
+  return launch_gather(T, mg, kg, M, K, K, ComplexWriter<float2>{out, ldo}, s);
+}
+cudaError_t launch_gather_c64_to_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                     int64_t M, int64_t K, int64_t ldo, float2* out, cudaStream_t s) {
+  return launch_gather(T, mg, kg, M, K, K, ComplexWriter<float2>{out, ldo}, s);
+}
+cudaError_t launch_gather_c64_to_c128(const float2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                      int64_t M, int64_t K, int64_t ldo, double2* out, cudaStream_t s) {
+  return launch_gather(T, mg, kg, M, K, K, ComplexWriter<double2>{out, ldo}, s);
+}
+cudaError_t launch_split_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M,
+                              int64_t K, int64_t Kp, int nplanes, int64_t pstride,
+                              __nv_bfloat16* out, cudaStream_t s) {
+  return launch_gather(T, mg, kg, M, K, Kp, SplitWriter{out, 2 * Kp, pstride, nplanes}, s);
+}
+cudaError_t launch_split_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M,
+                             int64_t K, int64_t Kp, int nplanes, int64_t pstride,
+                             __nv_bfloat16* out, cudaStream_t s) {
+  return launch_gather(T, mg, kg, M, K, Kp, SplitWriter{out, 2 * Kp, pstride, nplanes}, s);
+}
+cudaError_t launch_pack_b_planes(const double2* B, int64_t N, int64_t K, int64_t Kp, int nplanes,
+                                 int64_t pstride, __nv_bfloat16* out, cudaStream_t s) {
+  const int64_t total = 2 * N * Kp;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (blocks < 1) blocks = 1;
+  pack_b_planes_kernel<<<(unsigned)blocks, 256, 0, s>>>(B, N, K, Kp, nplanes, pstride, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_small_contract_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                       int64_t M, int K, int N, const double2* B, double2* C,
+                                       cudaStream_t s) {
+  return launch_small(T, mg, kg, M, K, N, B, C, s);
+}
+cudaError_t launch_small_contract_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg,
+                                      int64_t M, int K, int N, const float2* B, float2* C,
+                                      cudaStream_t s) {
+  return launch_small(T, mg, kg, M, K, N, B, C, s);
+}

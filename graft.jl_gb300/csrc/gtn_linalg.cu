@@ -1,0 +1,240 @@
+// FP64 factorisations on device through cuSOLVER runtime calls: truncated SVD for the
+// two-site split (lib/GraftFoundation/src/Backend/Backend.jl:466-505,
+// lib/GraftContractions/src/Contractions/effective.jl:852-876) and thin QR for the gauge
+// moves (Backend.jl:602-630, lib/GraftNetworks/src/Networks/ttns.jl:181-203).
+// cuSOLVER is loaded on first use with dlopen so that the rest of the library does not
+// depend on it being installed.
+#include "gtn_internal.h"
+
+#include <cusolverDn.h>
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <cmath>
+
+namespace {
+
+struct Solver {
+  void* lib = nullptr;
+  decltype(&cusolverDnCreate) create = nullptr;
+  decltype(&cusolverDnDestroy) destroy = nullptr;
+  decltype(&cusolverDnSetStream) set_stream = nullptr;
+  decltype(&cusolverDnZgesvd_bufferSize) gesvd_bs = nullptr;
+  decltype(&cusolverDnZgesvd) gesvd = nullptr;
+  decltype(&cusolverDnZgeqrf_bufferSize) geqrf_bs = nullptr;
+  decltype(&cusolverDnZgeqrf) geqrf = nullptr;
+  decltype(&cusolverDnZungqr_bufferSize) ungqr_bs = nullptr;
+  decltype(&cusolverDnZungqr) ungqr = nullptr;
+  bool ok = false;
+};
+
+Solver& solver() {
+  static Solver s;
+  static bool tried = false;
+  if (tried) return s;
+  tried = true;
+  const char* names[] = {"libcusolver.so.12", "libcusolver.so.11", "libcusolver.so.13", "libcusolver.so"};
+  for (const char* nm : names) {
+    s.lib = dlopen(nm, RTLD_NOW | RTLD_LOCAL);
+    if (s.lib) break;
+  }
+  if (!s.lib) return s;
+#define LOAD(field, sym) s.field = reinterpret_cast<decltype(s.field)>(dlsym(s.lib, #sym))
+  LOAD(create, cusolverDnCreate);
+  LOAD(destroy, cusolverDnDestroy);
+  LOAD(set_stream, cusolverDnSetStream);
+  LOAD(gesvd_bs, cusolverDnZgesvd_bufferSize);
+  LOAD(gesvd, cusolverDnZgesvd);
+  LOAD(geqrf_bs, cusolverDnZgeqrf_bufferSize);
+  LOAD(geqrf, cusolverDnZgeqrf);
+  LOAD(ungqr_bs, cusolverDnZungqr_bufferSize);
+  LOAD(ungqr, cusolverDnZungqr);
+#undef LOAD
+  s.ok = s.create && s.destroy && s.set_stream && s.gesvd_bs && s.gesvd && s.geqrf_bs && s.geqrf &&
+         s.ungqr_bs && s.ungqr;
+  return s;
+}
+
+int handle(gtn_ctx ctx, cusolverDnHandle_t* h) {
+  Solver& s = solver();
+  if (!s.ok) return set_err(ctx, GTN_ERR_UNSUPPORTED, "cuSOLVER could not be loaded");
+  if (!ctx->cusolver) {
+    cusolverDnHandle_t hh;
+    if (s.create(&hh) != CUSOLVER_STATUS_SUCCESS) return set_err(ctx, GTN_ERR_CUDA, "cusolverDnCreate failed");
+    ctx->cusolver = hh;
+  }
+  *h = static_cast<cusolverDnHandle_t>(ctx->cusolver);
+  if (s.set_stream(*h, ctx->stream) != CUSOLVER_STATUS_SUCCESS) return set_err(ctx, GTN_ERR_CUDA, "cusolverDnSetStream failed");
+  return GTN_OK;
+}
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+void linalg_release(gtn_ctx ctx) {
+  if (ctx->cusolver) {
+    Solver& s = solver();
+    if (s.ok) s.destroy(static_cast<cusolverDnHandle_t>(ctx->cusolver));
+    ctx->cusolver = nullptr;
+  }
+}
+
+extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, int64_t maxdim, double atol,
+                             double rtol, double discarded_weight, void* U, double* S, void* Vh,
+                             int64_t* rank, double* discarded) {
+  if (!ctx || !A || !U || !S || !Vh || !rank || m <= 0 || n <= 0)
+    return set_err(ctx, GTN_ERR_INVALID, "gtn_svd_trunc: bad argument");
+  if (m > INT32_MAX || n > INT32_MAX) return set_err(ctx, GTN_ERR_UNSUPPORTED, "gtn_svd_trunc: matrix too large");
+  cusolverDnHandle_t h;
+  int st = handle(ctx, &h);
+  if (st != GTN_OK) return st;
+  Solver& sv = solver();
+  cudaStream_t s = ctx->stream;
+  const int64_t k = std::min(m, n);
+  // Column-major problem B (rows >= cols): for n >= m, B = A^T (the same buffer); else B =
+  // column-major copy of A (a transpose).
+  const bool wide = n >= m;
+  const int64_t br = wide ? n : m, bc = wide ? m : n;  // B is br x bc, br >= bc
+  int lwork = 0;
+  if (sv.gesvd_bs(h, (int)br, (int)bc, &lwork) != CUSOLVER_STATUS_SUCCESS)
+    return set_err(ctx, GTN_ERR_CUDA, "gesvd_bufferSize failed");
+  const size_t bB = align256(br * bc * sizeof(double2)), bU = align256(br * k * sizeof(double2)),
+               bVT = align256(k * bc * sizeof(double2)), bS = align256(k * sizeof(double)),
+               bW = align256((size_t)lwork * sizeof(double2)), bR = align256(k * sizeof(double)),
+               bT = align256(std::max(m * k, k * n) * sizeof(double2));
+  void* ws = nullptr;
+  GTN_CUDA_TRY(ctx, ctx_workspace(ctx, bB + bU + bVT + bS + bW + bR + bT + 256, &ws));
+  char* p = static_cast<char*>(ws);
+  double2* dB = reinterpret_cast<double2*>(p); p += bB;
+  double2* dU = reinterpret_cast<double2*>(p); p += bU;
+  double2* dVT = reinterpret_cast<double2*>(p); p += bVT;
+  double* dS = reinterpret_cast<double*>(p); p += bS;
+  double2* dW = reinterpret_cast<double2*>(p); p += bW;
+  double* dR = reinterpret_cast<double*>(p); p += bR;
+  double2* dT = reinterpret_cast<double2*>(p); p += bT;
+  int* dinfo = reinterpret_cast<int*>(p);
+  if (wide) {
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(dB, A, m * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  } else {
+    GTN_CUDA_TRY(ctx, launch_transpose_c128(static_cast<const double2*>(A), m, n, dB, s));  // row-major n x m
+    ctx->launches++;
+  }
+  if (sv.gesvd(h, 'S', 'S', (int)br, (int)bc, reinterpret_cast<cuDoubleComplex*>(dB), (int)br, dS,
+               reinterpret_cast<cuDoubleComplex*>(dU), (int)br, reinterpret_cast<cuDoubleComplex*>(dVT), (int)k,
+               reinterpret_cast<cuDoubleComplex*>(dW), lwork, dR, dinfo) != CUSOLVER_STATUS_SUCCESS)
+    return set_err(ctx, GTN_ERR_CUDA, "cusolverDnZgesvd failed");
+  int hinfo = 0;
+  std::vector<double> hs(k);
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(hs.data(), dS, k * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  if (hinfo != 0) return set_err(ctx, GTN_ERR_CUDA, "gesvd info = " + std::to_string(hinfo));
+  // truncation rank (truncrank & trunctol & truncerror)
+  int64_t r = k;
+  if (maxdim > 0) r = std::min(r, maxdim);
+  if (atol > 0 || rtol > 0) {
+    const double thr = std::max(atol, rtol * hs[0]);
+    int64_t c = 0;
+    for (int64_t i = 0; i < k; ++i) c += hs[i] > thr ? 1 : 0;
+    r = std::min(r, c);
+  }
+  double tot = 0;
+  for (double v : hs) tot += v * v;
+  if (discarded_weight > 0) {
+    double tail = 0;
+    int64_t rr = k;
+    for (int64_t i = k - 1; i >= 0; --i) {
+      tail += hs[i] * hs[i];
+      if (std::sqrt(tail) <= discarded_weight * std::sqrt(tot)) rr = i;
+      else break;
+    }
+    r = std::min(r, rr);
+  }
+  r = std::max<int64_t>(r, 1);
+  double disc = 0;
+  for (int64_t i = r; i < k; ++i) disc += hs[i] * hs[i];
+  for (int64_t i = 0; i < r; ++i) S[i] = hs[i];
+  *rank = r;
+  if (discarded) *discarded = std::sqrt(disc);
+  double2* Uo = static_cast<double2*>(U);
+  double2* Vo = static_cast<double2*>(Vh);
+  if (wide) {
+    // U_A (m x k row-major) = VT buffer; Vh_A (k x n row-major) = U buffer.
+    GTN_CUDA_TRY(ctx, cudaMemcpy2DAsync(Uo, r * sizeof(double2), dVT, k * sizeof(double2), r * sizeof(double2), m,
+                                        cudaMemcpyDeviceToDevice, s));
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(Vo, dU, r * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  } else {
+    // A = U S VT column-major: U (m x k, ld m) -> row-major via transpose of the k x m
+    // row-major view; VT (k x n, ld k) -> row-major via transpose of the n x k view.
+    GTN_CUDA_TRY(ctx, launch_transpose_c128(dU, k, m, dT, s));  // dT: m x k row-major
+    GTN_CUDA_TRY(ctx, cudaMemcpy2DAsync(Uo, r * sizeof(double2), dT, k * sizeof(double2), r * sizeof(double2), m,
+                                        cudaMemcpyDeviceToDevice, s));
+    GTN_CUDA_TRY(ctx, launch_transpose_c128(dVT, n, k, dT, s));  // dT: k x n row-major
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(Vo, dT, r * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    ctx->launches += 2;
+  }
+  return gtn_ctx_sync(ctx);
+}
+
+extern "C" int gtn_qr(gtn_ctx ctx, int64_t m, int64_t n, const void* A, void* Q, void* R) {
+  if (!ctx || !A || !Q || !R || m <= 0 || n <= 0) return set_err(ctx, GTN_ERR_INVALID, "gtn_qr: bad argument");
+  if (m > INT32_MAX || n > INT32_MAX) return set_err(ctx, GTN_ERR_UNSUPPORTED, "gtn_qr: matrix too large");
+  cusolverDnHandle_t h;
+  int st = handle(ctx, &h);
+  if (st != GTN_OK) return st;
+  Solver& sv = solver();
+  cudaStream_t s = ctx->stream;
+  const int64_t k = std::min(m, n);
+  int l1 = 0, l2 = 0;
+  const size_t bA = align256(m * n * sizeof(double2)), btau = align256(k * sizeof(double2)),
+               bT = align256(std::max(m * n, m * k) * sizeof(double2));
+  void* ws = nullptr;
+  GTN_CUDA_TRY(ctx, ctx_workspace(ctx, bA + btau + bT + 256, &ws));  // sized again below with lwork
+  char* p = static_cast<char*>(ws);
+  double2* dA = reinterpret_cast<double2*>(p);
+  GTN_CUDA_TRY(ctx, launch_transpose_c128(static_cast<const double2*>(A), m, n, dA, s));  // column-major m x n
+  ctx->launches++;
+  if (sv.geqrf_bs(h, (int)m, (int)n, reinterpret_cast<cuDoubleComplex*>(dA), (int)m, &l1) != CUSOLVER_STATUS_SUCCESS ||
+      sv.ungqr_bs(h, (int)m, (int)k, (int)k, reinterpret_cast<cuDoubleComplex*>(dA), (int)m, nullptr, &l2) !=
+          CUSOLVER_STATUS_SUCCESS)
+    return set_err(ctx, GTN_ERR_CUDA, "QR bufferSize failed");
+  const size_t bW = align256((size_t)std::max(l1, l2) * sizeof(double2));
+  const size_t need = bA + btau + bT + bW + 256;
+  if (need > ctx->ws_bytes) {
+    // grow while preserving the transposed copy
+    void* tmp = nullptr;
+    GTN_CUDA_TRY(ctx, cudaMalloc(&tmp, bA));
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(tmp, dA, m * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    GTN_CUDA_TRY(ctx, ctx_workspace(ctx, need, &ws));
+    p = static_cast<char*>(ws);
+    dA = reinterpret_cast<double2*>(p);
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(dA, tmp, m * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    cudaFree(tmp);
+  }
+  p = static_cast<char*>(ws) + bA;
+  double2* dtau = reinterpret_cast<double2*>(p); p += btau;
+  double2* dT = reinterpret_cast<double2*>(p); p += bT;
+  double2* dW = reinterpret_cast<double2*>(p); p += bW;
+  int* dinfo = reinterpret_cast<int*>(p);
+  if (sv.geqrf(h, (int)m, (int)n, reinterpret_cast<cuDoubleComplex*>(dA), (int)m, reinterpret_cast<cuDoubleComplex*>(dtau),
+               reinterpret_cast<cuDoubleComplex*>(dW), std::max(l1, l2), dinfo) != CUSOLVER_STATUS_SUCCESS)
+    return set_err(ctx, GTN_ERR_CUDA, "cusolverDnZgeqrf failed");
+  // R: rows 0..k-1 of the row-major form of the factored matrix, lower part zeroed
+  GTN_CUDA_TRY(ctx, launch_transpose_c128(dA, n, m, dT, s));  // dT: m x n row-major
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(R, dT, k * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  GTN_CUDA_TRY(ctx, launch_zero_lower(static_cast<double2*>(R), k, n, s));
+  if (sv.ungqr(h, (int)m, (int)k, (int)k, reinterpret_cast<cuDoubleComplex*>(dA), (int)m,
+               reinterpret_cast<cuDoubleComplex*>(dtau), reinterpret_cast<cuDoubleComplex*>(dW), std::max(l1, l2),
+               dinfo) != CUSOLVER_STATUS_SUCCESS)
+    return set_err(ctx, GTN_ERR_CUDA, "cusolverDnZungqr failed");
+  GTN_CUDA_TRY(ctx, launch_transpose_c128(dA, k, m, static_cast<double2*>(Q), s));  // Q: m x k row-major
+  ctx->launches += 3;
+  int hinfo = 0;
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
+  st = gtn_ctx_sync(ctx);
+  if (st != GTN_OK) return st;
+  if (hinfo != 0) return set_err(ctx, GTN_ERR_CUDA, "QR info = " + std::to_string(hinfo));
+  return GTN_OK;
+}

@@ -1,0 +1,372 @@
+// Plan compiler and executor for effective maps: an ncon label graph is lowered once
+// into a chain of pair steps (the reference's ContractionPlan of PairSteps,
+// lib/GraftPlanning/src/Planning/types.jl:54-115, executed like executor.jl:99-144).
+//
+// Each step absorbs one static S into the running tensor T:
+//     C[n][m] = sum_k T[m, k] * S[n, k]
+// m runs over T's free legs (in T's order), k over the shared legs (in T's order), n over
+// S's free legs (in S's order).  C's legs are (S free..., T free...), row-major.  T is read
+// in place through strided index groups, so no permutation kernel runs for small-K steps;
+// large-K steps gather T into a K-major operand (c128 for FP64, bf16 slice planes for the
+// tcgen05 path).  Statics are permuted/conjugated/packed once when the map is created.
+#include "gtn_internal.h"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <set>
+
+namespace {
+
+constexpr int kSmallK = 64;
+
+// Build an index group over `legs` (positions into a row-major tensor with `dims`),
+// merging neighbours that are contiguous in memory.
+bool make_group(const std::vector<int64_t>& dims, const std::vector<int>& legs, GroupSpec* g) {
+  std::vector<int64_t> strides(dims.size(), 1);
+  for (int i = (int)dims.size() - 2; i >= 0; --i) strides[i] = strides[i + 1] * dims[i + 1];
+  std::vector<int64_t> gd, gs;
+  for (int l : legs) {
+    const int64_t d = dims[l], st = strides[l];
+    if (d == 1) continue;
+    if (!gd.empty() && gs.back() == st * d) {
+      gd.back() *= d;
+      gs.back() = st;
+    } else {
+      gd.push_back(d);
+      gs.push_back(st);
+    }
+  }
+  if ((int)gd.size() > GTN_MAXG) return false;
+  std::memset(g, 0, sizeof(*g));
+  g->n = (int)gd.size();
+  for (int i = 0; i < g->n; ++i) {
+    g->dim[i] = gd[i];
+    g->str[i] = gs[i];
+  }
+  return true;
+}
+
+int64_t prod(const std::vector<int64_t>& d, const std::vector<int>& legs) {
+  int64_t p = 1;
+  for (int l : legs) p *= d[l];
+  return p;
+}
+
+template <typename T> cudaError_t dalloc(gtn_map map, T** p, size_t bytes) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, bytes < 256 ? 256 : bytes);
+  if (e == cudaSuccess) {
+    map->owned.push_back(q);
+    map->bytes += (int64_t)bytes;
+  }
+  *p = static_cast<T*>(q);
+  return e;
+}
+
+bool is_tc(int precision) { return precision == GTN_PREC_BF16X6 || precision == GTN_PREC_BF16X3; }
+int nplanes_of(int precision) { return precision == GTN_PREC_BF16X6 ? 3 : 2; }
+
+}  // namespace
+
+__global__ void c128_to_c64_kernel(const double2* __restrict__ x, float2* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = make_float2((float)x[i].x, (float)x[i].y);
+}
+
+int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const int* labels,
+               const int* conj, const int* order, const void* const* statics, int precision,
+               gtn_map map) {
+  if (n < 2) return set_err(ctx, GTN_ERR_INVALID, "map needs the input and at least one static");
+  if (precision < 0 || precision > 3) return set_err(ctx, GTN_ERR_INVALID, "unknown precision");
+  if (is_tc(precision) && !tc_gemm_supported(ctx->cc_major, ctx->cc_minor))
+    return set_err(ctx, GTN_ERR_UNSUPPORTED, "tcgen05 precision modes need an sm_10x device");
+  std::vector<std::vector<int64_t>> D(n);
+  std::vector<std::vector<int>> L(n);
+  int64_t off = 0;
+  std::map<int, int> count;
+  std::map<int, int64_t> ldim;
+  for (int i = 0; i < n; ++i) {
+    if (ranks[i] < 0 || ranks[i] > 16) return set_err(ctx, GTN_ERR_INVALID, "bad operand rank");
+    for (int r = 0; r < ranks[i]; ++r) {
+      D[i].push_back(dims[off + r]);
+      L[i].push_back(labels[off + r]);
+      if (dims[off + r] <= 0) return set_err(ctx, GTN_ERR_SHAPE, "non-positive leg dimension");
+      const int l = labels[off + r];
+      if (l == 0) return set_err(ctx, GTN_ERR_INVALID, "label 0 is not allowed");
+      count[l]++;
+      auto it = ldim.find(l);
+      if (it != ldim.end() && it->second != dims[off + r])
+        return set_err(ctx, GTN_ERR_SHAPE, "label " + std::to_string(l) + " joins legs of different dimension");
+      ldim[l] = dims[off + r];
+    }
+    off += ranks[i];
+  }
+  int nout = 0;
+  for (auto& kv : count) {
+    if (kv.first > 0 && kv.second != 2)
+      return set_err(ctx, GTN_ERR_INVALID, "positive label " + std::to_string(kv.first) + " must appear twice");
+    if (kv.first < 0) {
+      if (kv.second != 1) return set_err(ctx, GTN_ERR_INVALID, "output label repeated");
+      nout++;
+    }
+  }
+  for (int k = 1; k <= nout; ++k)
+    if (!count.count(-k)) return set_err(ctx, GTN_ERR_INVALID, "output labels must be -1..-R");
+  if (conj && conj[0]) return set_err(ctx, GTN_ERR_INVALID, "the input operand cannot be conjugated");
+  {
+    std::set<int> seen;
+    if (order[0] != 0) return set_err(ctx, GTN_ERR_INVALID, "order must start with operand 0");
+    for (int i = 0; i < n; ++i) {
+      if (order[i] < 0 || order[i] >= n || seen.count(order[i]))
+        return set_err(ctx, GTN_ERR_INVALID, "order must be a permutation of the operands");
+      seen.insert(order[i]);
+    }
+  }
+
+  map->ctx = ctx;
+  map->precision = precision;
+  map->x_dims = D[0];
+  map->x_elems = 1;
+  for (auto d : D[0]) map->x_elems *= d;
+  std::vector<int> LT = L[0];
+  std::vector<int64_t> DT = D[0];
+  map->max_t = map->x_elems;
+  map->max_a = 0;
+  map->max_apl = 0;
+  const bool tc = is_tc(precision);
+  const int P = tc ? nplanes_of(precision) : 0;
+
+  for (int s = 1; s < n; ++s) {
+    const int j = order[s];
+    const std::vector<int>& LS = L[j];
+    const std::vector<int64_t>& DS = D[j];
+    std::vector<int> sh, freeT, freeS;  // positions
+    std::vector<int> shS;               // positions in S of the shared labels (T order)
+    for (int a = 0; a < (int)LT.size(); ++a) {
+      const int l = LT[a];
+      auto it = std::find(LS.begin(), LS.end(), l);
+      if (l > 0 && it != LS.end()) {
+        sh.push_back(a);
+        shS.push_back((int)(it - LS.begin()));
+      } else {
+        freeT.push_back(a);
+      }
+    }
+    for (int b = 0; b < (int)LS.size(); ++b)
+      if (std::find(shS.begin(), shS.end(), b) == shS.end()) freeS.push_back(b);
+    for (int a : freeT)
+      if (LT[a] > 0 && std::count(LT.begin(), LT.end(), LT[a]) > 1)
+        return set_err(ctx, GTN_ERR_UNSUPPORTED, "self-contraction inside one operand");
+
+    PlanStep st;
+    st.operand = j;
+    st.M = prod(DT, freeT);
+    st.K = prod(DT, sh);
+    st.N = prod(DS, freeS);
+    st.macs = (double)st.M * (double)st.N * (double)st.K;
+    if (!make_group(DT, freeT, &st.mg) || !make_group(DT, sh, &st.kg))
+      return set_err(ctx, GTN_ERR_UNSUPPORTED, "too many non-contiguous leg groups");
+    st.small = st.K <= kSmallK && small_contract_fits((int)st.K, (int)std::min<int64_t>(st.N, 1 << 20), sizeof(double2));
+    st.tc = tc && !st.small;
+    st.Kp = ((st.K + 31) / 32) * 32;
+    // C legs: S free (S order), then T free (T order)
+    for (int b : freeS) { st.out_labels.push_back(LS[b]); st.out_dims.push_back(DS[b]); }
+    for (int a : freeT) { st.out_labels.push_back(LT[a]); st.out_dims.push_back(DT[a]); }
+    st.out_elems = st.M * st.N;
+    map->max_t = std::max(map->max_t, st.out_elems);
+    if (!st.small) {
+      map->max_a = std::max(map->max_a, st.M * st.K);
+      if (st.tc) map->max_apl = std::max(map->max_apl, (int64_t)P * st.M * 2 * st.Kp);
+    }
+
+    // ---- pack the static: B[n][k] = S[freeS(n), shared(k)] (conj applied) -------------
+    if (statics && statics[j]) {
+      cudaError_t e = dalloc(map, &st.b64, (size_t)st.N * st.K * sizeof(double2));
+      if (e != cudaSuccess) return set_err(ctx, GTN_ERR_MEMORY, "static packing allocation failed");
+      GroupSpec gn, gk;
+      if (!make_group(DS, freeS, &gn) || !make_group(DS, shS, &gk))
+        return set_err(ctx, GTN_ERR_UNSUPPORTED, "too many non-contiguous static leg groups");
+      e = launch_gather_c128_to_c128(static_cast<const double2*>(statics[j]), gn, gk, st.N, st.K, st.K,
+                                     st.b64, ctx->stream);
+      ctx->launches++;
+      if (e == cudaSuccess && conj && conj[j]) {
+        e = launch_conj_inplace(st.b64, st.N * st.K, ctx->stream);
+        ctx->launches++;
+      }
+      if (e == cudaSuccess) {
+        e = dalloc(map, &st.b32, (size_t)st.N * st.K * sizeof(float2));
+        if (e == cudaSuccess) {
+          const int64_t ne = st.N * st.K;
+          int64_t blocks = std::min<int64_t>((ne + 255) / 256, 152 * 8);
+          c128_to_c64_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(st.b64, st.b32, ne);
+          ctx->launches++;
+          e = cudaGetLastError();
+        }
+      }
+      if (e == cudaSuccess && st.tc) {
+        st.bplanes = P;
+        const int64_t pstride = 2 * st.N * 2 * st.Kp;
+        e = dalloc(map, &st.bpl, (size_t)P * pstride * sizeof(__nv_bfloat16));
+        if (e == cudaSuccess) {
+          e = launch_pack_b_planes(st.b64, st.N, st.K, st.Kp, P, pstride, st.bpl, ctx->stream);
+          ctx->launches++;
+        }
+      }
+      if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("static packing: ") + cudaGetErrorString(e));
+    }
+    map->flops += 8.0 * st.macs;
+    map->steps.push_back(st);
+    LT = map->steps.back().out_labels;
+    DT = map->steps.back().out_dims;
+  }
+  for (int l : LT)
+    if (l > 0) return set_err(ctx, GTN_ERR_INVALID, "unresolved positive label after the last step");
+  // final permutation to y order (-1, -2, ...)
+  const int R = (int)LT.size();
+  std::vector<int> ypos(R);
+  map->y_dims.assign(R, 1);
+  for (int a = 0; a < R; ++a) {
+    const int k = -LT[a] - 1;
+    ypos[k] = a;
+    map->y_dims[k] = DT[a];
+  }
+  map->y_elems = 1;
+  for (auto d : map->y_dims) map->y_elems *= d;
+  std::vector<int> mlegs(ypos.begin(), ypos.end() - (R > 0 ? 1 : 0));
+  std::vector<int> klegs;
+  if (R > 0) klegs.push_back(ypos[R - 1]);
+  if (!make_group(DT, mlegs, &map->fin_mg) || !make_group(DT, klegs, &map->fin_kg))
+    return set_err(ctx, GTN_ERR_UNSUPPORTED, "too many non-contiguous output leg groups");
+  map->fin_K = R > 0 ? map->y_dims[R - 1] : 1;
+  map->fin_M = map->y_elems / map->fin_K;
+  bool ident = true;
+  for (int a = 0; a < R; ++a) ident = ident && ypos[a] == a;
+  map->fin_identity = ident;
+
+  // ---- workspace admission, then allocation ------------------------------------------
+  const size_t tbytes = (size_t)map->max_t * sizeof(double2);
+  const size_t abytes = std::max<size_t>((size_t)map->max_a * sizeof(double2),
+                                         (size_t)map->max_apl * sizeof(__nv_bfloat16));
+  size_t freeb = 0, totalb = 0;
+  cudaMemGetInfo(&freeb, &totalb);
+  const size_t need = 2 * tbytes + abytes + (size_t)(1u << 30);
+  if (need > freeb)
+    return set_err(ctx, GTN_ERR_MEMORY, "memory admission refused: map workspace " +
+                                            std::to_string(need >> 20) + " MiB > free " +
+                                            std::to_string(freeb >> 20) + " MiB");
+  if (dalloc(map, &map->buf0, tbytes) != cudaSuccess || dalloc(map, &map->buf1, tbytes) != cudaSuccess ||
+      dalloc(map, &map->abuf, std::max<size_t>(abytes, 256)) != cudaSuccess)
+    return set_err(ctx, GTN_ERR_MEMORY, "map workspace allocation failed");
+  return GTN_OK;
+}
+
+void map_free(gtn_map map) {
+  for (void* p : map->owned) cudaFree(p);
+  map->owned.clear();
+}
+
+int map_run(gtn_map map, int precision, const double2* x, double2* y) {
+  gtn_ctx ctx = map->ctx;
+  cudaStream_t s = ctx->stream;
+  const bool tc = is_tc(precision);
+  if (tc) {
+    for (auto& st : map->steps)
+      if (!st.small && (!st.bpl || st.bplanes != nplanes_of(precision)))
+        return set_err(ctx, GTN_ERR_INVALID, "map was not created for this tcgen05 precision");
+  }
+  const bool fp64 = precision == GTN_PREC_FP64;
+  const int P = tc ? nplanes_of(precision) : 0;
+  void* bufs[2] = {map->buf0, map->buf1};
+  const void* cur = x;
+  bool cur64 = true;
+  cudaError_t e = cudaSuccess;
+  const int nst = (int)map->steps.size();
+  for (int i = 0; i < nst && e == cudaSuccess; ++i) {
+    const PlanStep& st = map->steps[i];
+    void* out = bufs[i & 1];
+    if (fp64) {
+      if (st.small) {
+        e = launch_small_contract_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, (int)st.K,
+                                       (int)st.N, st.b64, static_cast<double2*>(out), s);
+        ctx->launches++;
+      } else {
+        double2* A = static_cast<double2*>(map->abuf);
+        e = launch_gather_c128_to_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.K, A, s);
+        if (e == cudaSuccess) e = launch_zgemm_simt(A, st.b64, static_cast<double2*>(out), st.M, st.N, st.K, s);
+        ctx->launches += 2;
+      }
+    } else {
+      if (cur64 && (st.small || !tc)) {
+        // the FP32 kernels read complex FP32: convert the FP64 input once
+        void* conv = bufs[(i + 1) & 1];
+        int64_t blocks = std::min<int64_t>((map->x_elems + 255) / 256, 152 * 8);
+        c128_to_c64_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(
+            static_cast<const double2*>(cur), static_cast<float2*>(conv), map->x_elems);
+        ctx->launches++;
+        e = cudaGetLastError();
+        cur = conv;
+        cur64 = false;
+        if (e != cudaSuccess) break;
+      }
+      if (st.small) {
+        e = launch_small_contract_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, (int)st.K,
+                                      (int)st.N, st.b32, static_cast<float2*>(out), s);
+        ctx->launches++;
+      } else if (!tc) {
+        float2* A = static_cast<float2*>(map->abuf);
+        e = launch_gather_c64_to_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.K, A, s);
+        if (e == cudaSuccess) e = launch_cgemm_simt(A, st.b32, static_cast<float2*>(out), st.M, st.N, st.K, s);
+        ctx->launches += 2;
+      } else {
+        __nv_bfloat16* Apl = static_cast<__nv_bfloat16*>(map->abuf);
+        const int64_t pstride = st.M * 2 * st.Kp;
+        if (cur64)
+          e = launch_split_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
+                                pstride, Apl, s);
+        else
+          e = launch_split_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
+                               pstride, Apl, s);
+        ctx->launches++;
+        if (e == cudaSuccess) {
+          TcGemmArgs a;
+          a.A = Apl;
+          a.B = st.bpl;
+          a.C = static_cast<float2*>(out);
+          a.M = st.M;
+          a.N = st.N;
+          a.Kp = st.Kp;
+          a.a_planes = P;
+          a.b_planes = P;
+          // products accumulated small terms first
+          if (P == 3) {
+            const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+            a.nprod = 6;
+            for (int q = 0; q < 6; ++q) { a.prod_a[q] = pa[q]; a.prod_b[q] = pb[q]; }
+          } else {
+            const int pa[3] = {1, 0, 0}, pb[3] = {0, 1, 0};
+            a.nprod = 3;
+            for (int q = 0; q < 3; ++q) { a.prod_a[q] = pa[q]; a.prod_b[q] = pb[q]; }
+          }
+          std::string why;
+          e = launch_tc_gemm(a, ctx->d_errflag, s, &why);
+          ctx->launches++;
+          if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, "tc_gemm: " + why + " " + cudaGetErrorString(e));
+        }
+      }
+      cur64 = false;
+    }
+    cur = out;
+  }
+  if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("map step: ") + cudaGetErrorString(e));
+  if (cur64)
+    e = launch_gather_c128_to_c128(static_cast<const double2*>(cur), map->fin_mg, map->fin_kg, map->fin_M,
+                                   map->fin_K, map->fin_K, y, s);
+  else
+    e = launch_gather_c64_to_c128(static_cast<const float2*>(cur), map->fin_mg, map->fin_kg, map->fin_M,
+                                  map->fin_K, map->fin_K, y, s);
+  ctx->launches++;
+  if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("map output: ") + cudaGetErrorString(e));
+  return GTN_OK;
+}

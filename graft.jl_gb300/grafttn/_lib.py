@@ -1,0 +1,140 @@
+"""ctypes binding of libgrafttn.so (the C ABI declared in include/grafttn.h).
+
+The shared library is built in-tree next to this package (``graft.jl_gb300/libgrafttn.so``).
+There is no fallback: importing the device layer without the library raises ImportError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "libgrafttn.so")
+
+GTN_OK = 0
+GTN_ERR_INVALID = 1
+GTN_ERR_SHAPE = 2
+GTN_ERR_MEMORY = 3
+GTN_ERR_CUDA = 4
+GTN_ERR_TIMEOUT = 5
+GTN_ERR_UNSUPPORTED = 6
+GTN_ERR_NOT_CONVERGED = 7
+
+PREC_FP64 = 0
+PREC_BF16X6 = 1
+PREC_BF16X3 = 2
+PREC_FP32 = 3
+PRECISIONS = {"fp64": PREC_FP64, "bf16x6": PREC_BF16X6, "bf16x3": PREC_BF16X3, "fp32": PREC_FP32}
+
+# Every symbol declared in include/grafttn.h, with (restype, argtypes).
+_p = C.c_void_p
+_i = C.c_int
+_i64 = C.c_int64
+_d = C.c_double
+_pi = C.POINTER(C.c_int)
+_pi64 = C.POINTER(C.c_int64)
+_pd = C.POINTER(C.c_double)
+SIGNATURES = {
+    "gtn_ctx_create": (_i, [_i, C.POINTER(_p)]),
+    "gtn_ctx_destroy": (_i, [_p]),
+    "gtn_ctx_set_stream": (_i, [_p, _p]),
+    "gtn_ctx_stream": (_p, [_p]),
+    "gtn_last_error": (C.c_char_p, [_p]),
+    "gtn_ctx_launch_count": (_i64, [_p]),
+    "gtn_ctx_sync": (_i, [_p]),
+    "gtn_map_create": (_i, [_p, _i, _pi, _pi64, _pi, _pi, _pi, C.POINTER(_p), _i, C.POINTER(_p)]),
+    "gtn_map_destroy": (_i, [_p]),
+    "gtn_map_apply": (_i, [_p, _p, _p]),
+    "gtn_map_apply_prec": (_i, [_p, _i, _p, _p]),
+    "gtn_map_apply_host": (_i, [_p, _p, _p]),
+    "gtn_map_info": (_i, [_p, _pi64, _pi64, _pd, _pi, _pi64]),
+    "gtn_map_out_shape": (_i, [_p, _pi, _pi64]),
+    "gtn_contract": (_i, [_p, _i, _pi, _pi64, _pi, _pi, _pi, C.POINTER(_p), _p, _i]),
+    "gtn_permute": (_i, [_p, _i, _pi64, _pi, _p, _p]),
+    "gtn_lanczos_min": (_i, [_p, _p, _i, _d, _i, _i, _pd, _pi, _pd]),
+    "gtn_expm_apply": (_i, [_p, _d, _d, _p, _i, _d, _pi]),
+    "gtn_svd_trunc": (_i, [_p, _i64, _i64, _p, _i64, _d, _d, _d, _p, _pd, _p, _pi64, _pd]),
+    "gtn_qr": (_i, [_p, _i64, _i64, _p, _p, _p]),
+    "gtn_dot": (_i, [_p, _i64, _p, _p, _pd]),
+    "gtn_axpby": (_i, [_p, _i64, _d, _d, _p, _d, _d, _p]),
+    "gtn_diag_scale": (_i, [_p, _i64, _i64, _pd, _i, _p]),
+}
+
+
+class GraftError(RuntimeError):
+    """Base class of library errors."""
+
+
+class SpaceMismatch(ValueError):
+    """Leg dimensions do not match (the reference's TensorKit.SpaceMismatch)."""
+
+
+class MemoryAdmissionError(MemoryError):
+    """The library refused an allocation before launching anything."""
+
+
+class DeviceTimeoutError(GraftError):
+    """A bounded device-side wait gave up."""
+
+
+class NotConvergedError(GraftError):
+    pass
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libgrafttn.so not built at {LIB_PATH}: run __graft_entry__.build()")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = _load()
+    return _LIB
+
+
+def check(status, ctx=None, what=""):
+    if status == GTN_OK:
+        return
+    msg = ""
+    if ctx is not None:
+        raw = lib().gtn_last_error(ctx)
+        msg = raw.decode() if raw else ""
+    text = f"{what}: {msg}" if what else msg
+    if status == GTN_ERR_INVALID:
+        raise ValueError(text)
+    if status == GTN_ERR_SHAPE:
+        raise SpaceMismatch(text)
+    if status == GTN_ERR_MEMORY:
+        raise MemoryAdmissionError(text)
+    if status == GTN_ERR_TIMEOUT:
+        raise DeviceTimeoutError(text)
+    if status == GTN_ERR_UNSUPPORTED:
+        raise NotImplementedError(text)
+    if status == GTN_ERR_NOT_CONVERGED:
+        raise NotConvergedError(text)
+    raise GraftError(f"status {status}: {text}")
+
+
+def int_array(vals):
+    vals = list(vals)
+    return (C.c_int * max(len(vals), 1))(*vals)
+
+
+def i64_array(vals):
+    vals = list(vals)
+    return (C.c_int64 * max(len(vals), 1))(*vals)
+
+
+def ptr_array(vals):
+    vals = list(vals)
+    return (C.c_void_p * max(len(vals), 1))(*[C.c_void_p(v) if v else None for v in vals])

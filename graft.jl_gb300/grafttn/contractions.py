@@ -1,0 +1,328 @@
+"""Environment cache and effective-Hamiltonian maps on the device.
+
+Mirrors lib/GraftContractions/src/Contractions/envcache.jl (EnvCache, env!, build_env,
+invalidation) and effective.jl (eff_h1 / eff_h2 / eff_h0): the label graphs are the
+reference's, operand by operand and leg by leg, and the contraction order is its env-first
+``preferred_slots`` order.  A map compiles once into a libgrafttn plan (statics packed on
+the device) and is then applied many times by the Krylov solvers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, i64_array, int_array, ptr_array
+from .device import Context
+from .networks import TTNO, TTNS
+
+
+def _stateleg(t, u, w):
+    """(envcache.jl:852-853)"""
+    return t.nchildren(u) + 1 if t.parent[u] == w else t.childslot(u, w)
+
+
+def _opleg(t, u, w):
+    """(envcache.jl:856-857)"""
+    return t.nchildren(u) + 2 if t.parent[u] == w else t.childslot(u, w)
+
+
+class _Fresh:
+    def __init__(self):
+        self.n = 0
+
+    def __call__(self):
+        self.n += 1
+        return self.n
+
+
+def env_spec(t, u, v, a_rank, w_rank):
+    """Sandwich at u with the legs towards v open (envcache.jl:919-999).  Operands:
+    (ket, env(w->u) for neighbours w != v..., root cap?, W, conj(bra)).  Output (ket, op, bra)."""
+    K = t.nchildren(u)
+    fresh = _Fresh()
+    aidx, bidx, widx = [0] * a_rank, [0] * a_rank, [0] * w_rank
+    pin, pout = fresh(), fresh()
+    aidx[K] = pin
+    widx[K + 1] = pin
+    widx[K] = pout
+    bidx[K] = pout
+    envs, envlabels = [], []
+    for w in t.neighbors(u):
+        la = _stateleg(t, u, w)
+        if w == v:
+            aidx[la], widx[_opleg(t, u, w)], bidx[la] = -1, -2, -3
+        else:
+            e = [fresh(), fresh(), fresh()]
+            aidx[la], widx[_opleg(t, u, w)], bidx[la] = e
+            envs.append(w)
+            envlabels.append(e)
+    cap = None
+    if t.parent[u] < 0:
+        ka, ko, kb = fresh(), fresh(), fresh()
+        aidx[-1], widx[-1], bidx[-1] = ka, ko, kb
+        cap = [kb, ko, ka]
+    labels = [aidx] + envlabels + ([cap] if cap else []) + [widx, bidx]
+    conj = [False] * (len(labels) - 1) + [True]
+    return labels, conj, envs, cap is not None
+
+
+def h1_spec(t, n, x_rank, w_rank):
+    """(effective.jl:627-686) operands (x, W, env(w->n) for neighbours..., cap?), env-first order."""
+    K = t.nchildren(n)
+    fresh = _Fresh()
+    xidx, widx = [0] * x_rank, [0] * w_rank
+    labels = [xidx, widx]
+    pin = fresh()
+    xidx[K] = pin
+    widx[K + 1] = pin
+    widx[K] = -(K + 1)
+    children, parents, caps, envs = [], [], [], []
+    for w in t.neighbors(n):
+        lx = _stateleg(t, n, w)
+        kk, oo = fresh(), fresh()
+        xidx[lx] = kk
+        widx[_opleg(t, n, w)] = oo
+        labels.append([kk, oo, -(lx + 1)])
+        envs.append((w, n))
+        (parents if t.parent[n] == w else children).append(len(labels) - 1)
+    if t.parent[n] < 0:
+        ka, ko = fresh(), fresh()
+        xidx[-1] = ka
+        widx[-1] = ko
+        labels.append([ka, ko, -x_rank])
+        caps.append(len(labels) - 1)
+    return labels, [0] + children + [1] + parents + caps, envs
+
+
+def h2_spec(t, n, m, x_rank, wn_rank, wm_rank, pn):
+    """(effective.jl:878-976) operands (Θ, Wn, Wm, env(w->n)..., env(w->m)..., cap?)."""
+    k = t.childslot(m, n)
+    Kn, Km = t.nchildren(n), t.nchildren(m)
+    fresh = _Fresh()
+    xidx, wnidx, wmidx = [0] * x_rank, [0] * wn_rank, [0] * wm_rank
+    labels = [xidx, wnidx, wmidx]
+
+    def mpos(j):
+        return pn + (j if j < k else j - 1)
+    ob = fresh()
+    wnidx[-1] = ob
+    wmidx[k] = ob
+    pin = fresh()
+    xidx[Kn] = pin
+    wnidx[Kn + 1] = pin
+    wnidx[Kn] = -(Kn + 1)
+    pin = fresh()
+    xidx[mpos(Km)] = pin
+    wmidx[Km + 1] = pin
+    wmidx[Km] = -(mpos(Km) + 1)
+    envn, envmc, envmp, caps, envs = [], [], [], [], []
+    for w in t.neighbors(n):
+        if w == m:
+            continue
+        lx = t.childslot(n, w)
+        kk, oo = fresh(), fresh()
+        xidx[lx] = kk
+        wnidx[lx] = oo
+        labels.append([kk, oo, -(lx + 1)])
+        envs.append((w, n))
+        envn.append(len(labels) - 1)
+    for w in t.neighbors(m):
+        if w == n:
+            continue
+        if t.parent[m] == w:
+            lw, lx = wm_rank - 1, x_rank - 1
+        else:
+            lw = t.childslot(m, w)
+            lx = mpos(lw)
+        kk, oo = fresh(), fresh()
+        xidx[lx] = kk
+        wmidx[lw] = oo
+        labels.append([kk, oo, -(lx + 1)])
+        envs.append((w, m))
+        (envmp if t.parent[m] == w else envmc).append(len(labels) - 1)
+    if t.parent[m] < 0:
+        ka, ko = fresh(), fresh()
+        xidx[-1] = ka
+        wmidx[-1] = ko
+        labels.append([ka, ko, -x_rank])
+        caps.append(len(labels) - 1)
+    order = [0] + envn + [1] + envmc + [2] + envmp + caps
+    return labels, order, envs
+
+
+class EffectiveMap:
+    """Callable y = H_eff x backed by a compiled libgrafttn plan (types.jl:410-445)."""
+
+    def __init__(self, ctx: Context, x_shape, labels, order, statics, precision=_lib.PREC_FP64):
+        self.ctx = ctx
+        self.x_shape = tuple(int(s) for s in x_shape)
+        self.precision = _lib.PRECISIONS.get(precision, precision) if isinstance(precision, str) else precision
+        ranks = [len(self.x_shape)] + [s.dim() for s in statics]
+        dims = list(self.x_shape) + [int(d) for s in statics for d in s.shape]
+        labs = [int(l) for lab in labels for l in lab]
+        h = C.c_void_p()
+        self._statics = statics  # keep alive until the packing kernels ran
+        st = ctx.lib.gtn_map_create(ctx.h, len(ranks), int_array(ranks), i64_array(dims), int_array(labs),
+                                    int_array([0] * len(ranks)), int_array(order),
+                                    ptr_array([0] + [s.data_ptr() for s in statics]), self.precision,
+                                    C.byref(h))
+        check(st, ctx.h, "map_create")
+        self.h = h
+        rank = C.c_int()
+        odims = (C.c_int64 * 32)()
+        check(ctx.lib.gtn_map_out_shape(self.h, C.byref(rank), odims), ctx.h, "map_out_shape")
+        self.y_shape = tuple(odims[i] for i in range(rank.value))
+        xe, ye, fl, ns, by = C.c_int64(), C.c_int64(), C.c_double(), C.c_int(), C.c_int64()
+        check(ctx.lib.gtn_map_info(self.h, C.byref(xe), C.byref(ye), C.byref(fl), C.byref(ns), C.byref(by)),
+              ctx.h, "map_info")
+        self.flops = fl.value
+        self.n_steps = ns.value
+        self.bytes = by.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gtn_map_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def apply_into(self, x, y, precision=None):
+        prec = self.precision if precision is None else precision
+        check(self.ctx.lib.gtn_map_apply_prec(self.h, prec, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr())),
+              self.ctx.h, "map_apply")
+        return y
+
+    def __call__(self, x, precision=None):
+        """Fresh output, as the reference's executor allocates the root output (executor.jl:122-127)."""
+        if tuple(x.shape) != self.x_shape:
+            raise _lib.SpaceMismatch(f"map input shape {tuple(x.shape)} != {self.x_shape}")
+        return self.apply_into(x.contiguous(), self.ctx.empty(self.y_shape), precision)
+
+    def apply_host(self, x_host):
+        """Host buffers in and out (host->device copy, apply, device->host copy in one call)."""
+        xh = np.ascontiguousarray(x_host, dtype=np.complex128)
+        yh = np.empty(self.y_shape, dtype=np.complex128)
+        check(self.ctx.lib.gtn_map_apply_host(self.h, xh.ctypes.data_as(C.c_void_p), yh.ctypes.data_as(C.c_void_p)),
+              self.ctx.h, "map_apply_host")
+        return yh
+
+    def lanczos_min(self, x0, krylovdim=20, tol=1e-12, maxiter=100, rq_fp64=False):
+        """Lowest eigenpair (groundstate_eigsolve_backend, GroundState.jl:25-39); x0 untouched."""
+        x = x0.contiguous().clone()
+        E = C.c_double()
+        info = (C.c_int * 3)()
+        res = C.c_double()
+        st = self.ctx.lib.gtn_lanczos_min(self.h, C.c_void_p(x.data_ptr()), krylovdim, tol, maxiter,
+                                          1 if rq_fp64 else 0, C.byref(E), info, C.byref(res))
+        if st not in (_lib.GTN_OK, _lib.GTN_ERR_NOT_CONVERGED):
+            check(st, self.ctx.h, "lanczos")
+        return E.value, x, dict(restarts=info[0], matvecs=info[1], converged=bool(info[2]), resid=res.value)
+
+    def exponentiate(self, dz, x0, krylovdim=30, tol=1e-12):
+        """exp(dz H) x0 (evolution_exponentiate_backend, Evolution.jl:54-68)."""
+        x = x0.contiguous().clone()
+        info = (C.c_int * 2)()
+        dz = complex(dz)
+        check(self.ctx.lib.gtn_expm_apply(self.h, dz.real, dz.imag, C.c_void_p(x.data_ptr()), krylovdim, tol, info),
+              self.ctx.h, "expm")
+        return x, dict(substeps=info[0], matvecs=info[1])
+
+
+class EnvCache:
+    """Directed-edge environments on the device (envcache.jl:61-109) with the reference's
+    invalidation rule: an env is dropped when its contracted side contains a touched node
+    (envcache.jl:812-844)."""
+
+    def __init__(self, topo):
+        self.topo = topo
+        self.envs = {}
+        self.builds = 0
+
+    def invalidate_node(self, n):
+        t = self.topo
+        for key in [k for k in self.envs if n in t.subtree_nodes(k[0], k[1])]:
+            del self.envs[key]
+
+    def invalidate_edge(self, n, m):
+        self.invalidate_node(n)
+        self.invalidate_node(m)
+
+    def env(self, psi: TTNS, H: TTNO, u, v):
+        """E(u->v)[ket, op, bra], built lazily after its prerequisites (envcache.jl:1440-1476)."""
+        key = (u, v)
+        if key in self.envs:
+            return self.envs[key]
+        t = self.topo
+        for w in t.neighbors(u):
+            if w != v:
+                self.env(psi, H, w, u)
+        A, W = psi.tensors[u], H.tensors[u]
+        labels, conj, envs, has_cap = env_spec(t, u, v, A.dim(), W.dim())
+        ops = [A] + [self.envs[(w, u)] for w in envs]
+        if has_cap:
+            ops.append(psi.ctx.upload(np.ones((1, 1, 1))))
+        ops += [W, A]
+        E = psi.ctx.contract(ops, labels, conj)
+        self.envs[key] = E
+        self.builds += 1
+        return E
+
+
+def _cap(ctx):
+    return ctx.upload(np.ones((1, 1, 1)))
+
+
+def eff_h1(cache: EnvCache, psi: TTNS, H: TTNO, n, precision=_lib.PREC_FP64):
+    """(effective.jl:709-730)"""
+    t = psi.topo
+    x = psi.tensors[n]
+    labels, order, envs = h1_spec(t, n, x.dim(), H.tensors[n].dim())
+    statics = [H.tensors[n]] + [cache.env(psi, H, w, u) for (w, u) in envs]
+    if t.parent[n] < 0:
+        statics.append(_cap(psi.ctx))
+    return EffectiveMap(psi.ctx, x.shape, labels, order, statics, precision)
+
+
+def two_site_shape(psi: TTNS, n, m):
+    k = psi.topo.childslot(m, n)
+    return tuple(psi.tensors[n].shape[:-1]) + tuple(s for j, s in enumerate(psi.tensors[m].shape) if j != k)
+
+
+def eff_h2(cache: EnvCache, psi: TTNS, H: TTNO, n, m, precision=_lib.PREC_FP64):
+    """(effective.jl:986-1034)"""
+    t = psi.topo
+    if t.parent[n] != m:
+        raise ValueError("eff_h2: m must be the parent of n")
+    pn = psi.tensors[n].dim() - 1
+    xs = two_site_shape(psi, n, m)
+    labels, order, envs = h2_spec(t, n, m, len(xs), H.tensors[n].dim(), H.tensors[m].dim(), pn)
+    statics = [H.tensors[n], H.tensors[m]] + [cache.env(psi, H, w, u) for (w, u) in envs]
+    if t.parent[m] < 0:
+        statics.append(_cap(psi.ctx))
+    return EffectiveMap(psi.ctx, xs, labels, order, statics, precision)
+
+
+def eff_h0(cache: EnvCache, psi: TTNS, H: TTNO, n, m, precision=_lib.PREC_FP64):
+    """Link map y = E(n->m) C E(m->n) (effective.jl:739-797)."""
+    if psi.topo.parent[n] != m:
+        raise ValueError("eff_h0: m must be the parent of n")
+    En = cache.env(psi, H, n, m)
+    Em = cache.env(psi, H, m, n)
+    labels = [[1, 2], [1, 3, -1], [2, 3, -2]]
+    return EffectiveMap(psi.ctx, (En.shape[0], Em.shape[0]), labels, [0, 1, 2], [En, Em], precision)
+
+
+def expect(psi: TTNS, H: TTNO):
+    """<psi|H|psi> / <psi|psi> closed at the centre (expectation.jl:32-40)."""
+    cache = EnvCache(psi.topo)
+    c = psi.center
+    x = psi.tensors[c]
+    h1 = eff_h1(cache, psi, H, c)
+    y = h1(x)
+    return psi.ctx.dot(x, y) / psi.ctx.dot(x, x)

@@ -1,0 +1,139 @@
+"""Sweep drivers: dmrg2! (lib/GraftGroundState/src/GroundState/GroundState.jl:102-143) and
+TDVP1 (lib/GraftEvolution/src/Evolution/tdvp.jl:171-301) on the device-resident network.
+
+The host keeps only the sweep order and the gauge bookkeeping; every tensor operation
+(QR, SVD, environment builds, the effective maps and their Krylov solves) runs through
+libgrafttn on the GPU.
+"""
+from __future__ import annotations
+
+import time
+
+from . import _lib
+from .contractions import EnvCache, eff_h0, eff_h1, eff_h2
+from .networks import (TTNO, TTNS, TruncationScheme, absorb_on_leg, left_orth, move_center,
+                       orth_factor_leg, split_two_site, two_site_tensor)
+
+
+def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10, tol=1e-10,
+          krylovdim=20, precision="fp64", rq_fp64=None, lanczos_tol=1e-12, maxiter=100,
+          verbose=False, stats=None):
+    """Two-site DMRG; returns (psi, energies per sweep).  ``precision`` selects the map
+    arithmetic; with a mixed mode the energy of every local solve is the FP64 Rayleigh
+    quotient of its eigenvector (``rq_fp64`` defaults to True for mixed modes)."""
+    if not H.ishermitian:
+        raise ValueError("dmrg2: DMRG requires ishermitian(H) == true")
+    prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
+    if rq_fp64 is None:
+        rq_fp64 = prec != _lib.PREC_FP64
+    trunc = trunc or TruncationScheme()
+    t = psi.topo
+    cache = EnvCache(t)
+    energies = []
+    bonds = [n for n in t.postorder() if t.parent[n] >= 0]
+    sched = [(n, "m") for n in bonds] + [(n, "n") for n in reversed(bonds)]
+    for sweep in range(nsweeps):
+        E = float("nan")
+        t0 = time.perf_counter()
+        for n, center_on in sched:
+            m = t.parent[n]
+            move_center(psi, n, cache)
+            theta = two_site_tensor(psi, n, m)
+            h2 = eff_h2(cache, psi, H, n, m, prec)
+            E, v, info = h2.lanczos_min(theta, krylovdim=krylovdim, tol=lanczos_tol, maxiter=maxiter,
+                                        rq_fp64=rq_fp64)
+            if stats is not None:
+                stats.setdefault("matvecs", 0)
+                stats["matvecs"] += info["matvecs"]
+            h2.close()
+            cache.invalidate_edge(n, m)
+            split_two_site(psi, v, n, m, trunc, center_on)
+        energies.append(float(E))
+        if verbose:
+            print(f"dmrg2 sweep {sweep + 1}: E = {E:.15f}  ({time.perf_counter() - t0:.3f} s)")
+        if len(energies) >= 2 and abs(energies[-1] - energies[-2]) < tol:
+            break
+    return psi, energies
+
+
+class TDVP1:
+    """One-site TDVP with order-2 splitting (tdvp.jl:31-44, 171-301)."""
+
+    def __init__(self, order=2, krylovdim=30, tol=1e-12, precision="fp64"):
+        if order not in (1, 2):
+            raise ValueError("order must be 1 or 2")
+        self.order = order
+        self.krylovdim = krylovdim
+        self.tol = tol
+        self.precision = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
+        self.cache = None
+
+    def step(self, psi: TTNS, H: TTNO, dz):
+        if self.cache is None or self.cache.topo != psi.topo:
+            self.cache = EnvCache(psi.topo)
+        if self.order == 1:
+            self._sweep(psi, H, dz, rev=False)
+        else:
+            self._sweep(psi, H, dz / 2, rev=False, terminal_dz=dz)
+            self._sweep(psi, H, dz / 2, rev=True, skip_initial=True)
+        return psi
+
+    def _sweep(self, psi, H, dz, rev, terminal_dz=None, skip_initial=False):
+        t = psi.topo
+        cache = self.cache
+        order = t.postorder()
+        if rev:
+            order = order[::-1]
+        move_center(psi, order[0], cache)
+        for i, n in enumerate(order):
+            assert psi.center == n
+            if not (skip_initial and i == 0):
+                sdz = terminal_dz if (terminal_dz is not None and i == len(order) - 1) else dz
+                h1 = eff_h1(cache, psi, H, n, self.precision)
+                A, _ = h1.exponentiate(sdz, psi.tensors[n], self.krylovdim, self.tol)
+                h1.close()
+                psi.tensors[n] = A
+                cache.invalidate_node(n)
+            if i == len(order) - 1:
+                break
+            seg = t.path_between(n, order[i + 1])
+            for j in range(1, len(seg)):
+                u, v = seg[j - 1], seg[j]
+                if (t.parent[u] == v) != rev:
+                    self._evolve_link_and_move(psi, H, u, v, dz)
+                else:
+                    move_center(psi, v, cache)
+
+    def _evolve_link_and_move(self, psi, H, u, v, dz):
+        """(tdvp.jl:257-288)"""
+        ctx, t, cache = psi.ctx, psi.topo, self.cache
+        if t.parent[u] == v:
+            Q, Cl = left_orth(ctx, psi.tensors[u])
+            psi.tensors[u] = Q
+            cache.invalidate_node(u)
+            k0 = eff_h0(cache, psi, H, u, v, self.precision)
+            Cl, _ = k0.exponentiate(-dz, Cl, self.krylovdim, self.tol)
+            k0.close()
+            psi.tensors[v] = absorb_on_leg(ctx, psi.tensors[v], Cl, t.childslot(v, u))
+        else:
+            k = t.childslot(u, v)
+            Q, Cd = orth_factor_leg(ctx, psi.tensors[u], k)
+            psi.tensors[u] = Q
+            Cl = ctx.permute(Cd, [1, 0])
+            cache.invalidate_node(u)
+            k0 = eff_h0(cache, psi, H, v, u, self.precision)
+            Cl, _ = k0.exponentiate(-dz, Cl, self.krylovdim, self.tol)
+            k0.close()
+            Av = psi.tensors[v]
+            r = Av.dim()
+            lab = [-(j + 1) for j in range(r - 1)] + [1]
+            psi.tensors[v] = ctx.contract([Av, Cl], [lab, [1, -r]])
+        psi.center = v
+        cache.invalidate_node(v)
+
+
+def evolve(ev: TDVP1, psi: TTNS, H: TTNO, dz, nsteps):
+    """(Evolution.jl:86-93)"""
+    for _ in range(nsteps):
+        ev.step(psi, H, dz)
+    return psi

@@ -1,0 +1,147 @@
+/*
+ * grafttn.h - C ABI of the GB300 (sm_103a) tree-tensor-network effective-Hamiltonian
+ * library (libgrafttn.so).
+ *
+ * Conventions
+ *  - Complex data is interleaved (re, im) double precision (ComplexF64 / complex128).
+ *  - A tensor of rank r with leg dims (d0, ..., d{r-1}) is stored row-major: the LAST leg
+ *    varies fastest.  A Julia/TensorKit column-major array with legs (l1..lr) is the same
+ *    buffer described with its legs (and labels) reversed.
+ *  - Leg order inside a tensor follows the reference: TTNS node (children..., phys,
+ *    parent), TTNO node (children..., P_out, P_in, parent), environment (ket, op, bra).
+ *  - Device buffers are plain CUDA device pointers owned by the caller, unless an entry
+ *    point says "host".  All work is ordered on the context's stream.
+ *  - Every call returns a gtn_status; gtn_last_error() returns the message of the last
+ *    failure on that context.  No exceptions cross the ABI.  Device waits inside kernels
+ *    are bounded and surface as GTN_ERR_TIMEOUT.
+ *  - A context is used by one host thread at a time (the reference's task-local
+ *    WorkspaceMap rule, lib/GraftPlanning/src/Planning/types.jl:503-552).
+ */
+#ifndef GRAFTTN_H
+#define GRAFTTN_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GTN_OK = 0,
+  GTN_ERR_INVALID = 1,        /* bad argument (the reference's ArgumentError) */
+  GTN_ERR_SHAPE = 2,          /* leg dimension mismatch (the reference's SpaceMismatch) */
+  GTN_ERR_MEMORY = 3,         /* memory admission refused before any launch */
+  GTN_ERR_CUDA = 4,           /* CUDA runtime / library error */
+  GTN_ERR_TIMEOUT = 5,        /* a bounded device wait gave up */
+  GTN_ERR_UNSUPPORTED = 6,    /* feature not available (library missing, arch) */
+  GTN_ERR_NOT_CONVERGED = 7   /* Krylov solver hit maxiter (result still returned) */
+} gtn_status;
+
+/* Arithmetic of a map application.  The Krylov vectors and all orthogonalisation are
+ * FP64 in every mode; the mode selects how the contraction chain is computed. */
+typedef enum {
+  GTN_PREC_FP64 = 0,       /* complex FP64 throughout (DFMA SIMT kernels) */
+  GTN_PREC_BF16X6 = 1,     /* tcgen05: 3 bf16 slices per operand, 6 products, FP32 accum */
+  GTN_PREC_BF16X3 = 2,     /* tcgen05: 2 bf16 slices per operand, 3 products, FP32 accum */
+  GTN_PREC_FP32 = 3        /* complex FP32 SIMT kernels (diagnostic mode) */
+} gtn_precision;
+
+typedef struct gtn_ctx_s* gtn_ctx;
+typedef struct gtn_map_s* gtn_map;
+
+/* ---- context --------------------------------------------------------------------- */
+
+/* Create a context on CUDA device `device` with its own non-blocking stream. */
+int gtn_ctx_create(int device, gtn_ctx* out);
+int gtn_ctx_destroy(gtn_ctx ctx);
+/* Use an external cudaStream_t (e.g. the caller's current stream) for all later work. */
+int gtn_ctx_set_stream(gtn_ctx ctx, void* stream);
+void* gtn_ctx_stream(gtn_ctx ctx);
+const char* gtn_last_error(gtn_ctx ctx);
+/* Number of library kernels launched on this context so far (launch accounting). */
+int64_t gtn_ctx_launch_count(gtn_ctx ctx);
+/* Wait for the stream and report (then clear) any device-side error flag. */
+int gtn_ctx_sync(gtn_ctx ctx);
+
+/* ---- effective maps: replaces Planning.EffectiveMap / execute / contract_pair ------
+ * lib/GraftPlanning/src/Planning/types.jl:410-445 (EffectiveMap callable),
+ * lib/GraftPlanning/src/Planning/executor.jl:16-45,99-144 (execute / _execute_workspace),
+ * lib/GraftFoundation/src/Backend/Backend.jl:166-222 (contract_pair[!]).
+ *
+ * A map is an ncon-style label graph over `n_operands` tensors.  Operand 0 is the
+ * varying input x; operands 1.. are statics (environments, TTNO tensors, root cap) that
+ * are copied / packed into the map at creation, so their buffers may be freed afterwards.
+ * labels: positive = contracted pair, -k = output leg k (1-based).  order[] is the
+ * pairwise absorption order starting with operand 0 (the reference's env-first
+ * preferred_slots order, lib/GraftContractions/src/Contractions/effective.jl:683,971).
+ * conj[i] != 0 conjugates operand i (only statics may be conjugated).
+ */
+int gtn_map_create(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dims,
+                   const int* labels, const int* conj, const int* order,
+                   const void* const* statics, int precision, gtn_map* out);
+int gtn_map_destroy(gtn_map map);
+/* y = H_eff x on device buffers (c128), in the map's default precision. */
+int gtn_map_apply(gtn_map map, const void* x, void* y);
+int gtn_map_apply_prec(gtn_map map, int precision, const void* x, void* y);
+/* Same with HOST buffers: host->device copy, apply, device->host copy (one call). */
+int gtn_map_apply_host(gtn_map map, const void* x_host, void* y_host);
+/* Shape/cost facts: elements of x and y, algorithmic FLOPs per apply (complex MAC = 8),
+ * number of pair steps, and device workspace bytes held by the map. */
+int gtn_map_info(gtn_map map, int64_t* x_elems, int64_t* y_elems, double* flops,
+                 int* n_steps, int64_t* bytes);
+/* Output leg dims of the map (rank written to *rank, dims to dims[0..rank-1]). */
+int gtn_map_out_shape(gtn_map map, int* rank, int64_t* dims);
+
+/* One-shot contraction of a label graph where every operand is given (environment
+ * builds, envcache.jl:1010-1101; two-site merge, effective.jl:827-843).  Operand 0 starts
+ * the chain; out receives the tensor with legs ordered -1, -2, ... (c128). */
+int gtn_contract(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dims,
+                 const int* labels, const int* conj, const int* order,
+                 const void* const* operands, void* out, int precision);
+
+/* Row-major permutation of a c128 tensor: out has legs (perm[0], perm[1], ...). */
+int gtn_permute(gtn_ctx ctx, int rank, const int64_t* dims, const int* perm,
+                const void* in, void* out);
+
+/* ---- Krylov solvers: replace the solver hooks ------------------------------------
+ * groundstate_eigsolve_backend, lib/GraftGroundState/src/GroundState/GroundState.jl:25-39
+ * evolution_exponentiate_backend, lib/GraftEvolution/src/Evolution/Evolution.jl:54-68
+ */
+/* Lowest eigenpair of the (Hermitian) map by restarted Lanczos with FP64 full
+ * re-orthogonalisation on device.  x (device, c128) holds the start vector on entry and
+ * the normalised eigenvector on exit.  With rq_fp64 != 0 the returned energy is the
+ * FP64 Rayleigh quotient <x|H x> of the final vector (one FP64 apply).
+ * info[0] = restarts, info[1] = matvecs, info[2] = converged flag; resid[0] = residual. */
+int gtn_lanczos_min(gtn_map map, void* x, int krylovdim, double tol, int maxiter,
+                    int rq_fp64, double* energy, int* info, double* resid);
+/* x <- exp((dz_re + i dz_im) H) x by a Lanczos Krylov exponential with FP64
+ * orthogonalisation and sub-stepping to meet tol.  info[0] = substeps, info[1] = matvecs. */
+int gtn_expm_apply(gtn_map map, double dz_re, double dz_im, void* x, int krylovdim,
+                   double tol, int* info);
+
+/* ---- factorisations (FP64, cuSOLVER runtime calls) --------------------------------
+ * split_svd / TruncationScheme, lib/GraftFoundation/src/Backend/Backend.jl:466-505;
+ * left_orth / orth_factor_leg, Backend.jl:602-630.
+ */
+/* Truncated SVD of the row-major m x n matrix A (device c128).  Keeps
+ * r = min(maxdim, #{s > max(atol, rtol*s0)}, discarded-weight rank) >= 1 values.
+ * U (m x r, row-major), S (r doubles, HOST), Vh (r x n, row-major) must hold
+ * min(m,n) columns/rows of capacity.  *rank = r, *discarded = 2-norm of dropped s. */
+int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, int64_t maxdim,
+                  double atol, double rtol, double discarded_weight, void* U, double* S,
+                  void* Vh, int64_t* rank, double* discarded);
+/* Thin QR of the row-major m x n matrix A: Q (m x k), R (k x n), k = min(m, n). */
+int gtn_qr(gtn_ctx ctx, int64_t m, int64_t n, const void* A, void* Q, void* R);
+
+/* ---- vector helpers on device c128 buffers (used by the host drivers) ------------- */
+int gtn_dot(gtn_ctx ctx, int64_t n, const void* x, const void* y, double* out2);  /* <x,y> */
+int gtn_axpby(gtn_ctx ctx, int64_t n, double a_re, double a_im, const void* x,
+              double b_re, double b_im, void* y);                                  /* y = a x + b y */
+/* In-place diagonal scaling of a row-major rows x cols c128 matrix by real HOST factors:
+ * side 0 scales column j by d[j] (U * diag(S)), side 1 scales row i by d[i] (diag(S) * Vh). */
+int gtn_diag_scale(gtn_ctx ctx, int64_t rows, int64_t cols, const double* d_host, int side, void* A);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRAFTTN_H */

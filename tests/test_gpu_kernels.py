@@ -1,0 +1,135 @@
+"""Kernel-level parity of libgrafttn against numpy (called through the C ABI)."""
+import numpy as np
+import pytest
+
+from oracle import ttn_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 2e-6, "bf16x3": 1e-3}
+
+
+def crandn(rng, shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("shape,perm", [((3, 4, 5), (2, 0, 1)), ((7, 1, 33, 2), (3, 2, 1, 0)),
+                                        ((64, 65), (1, 0)), ((2, 3, 4, 5, 6), (4, 1, 3, 0, 2))])
+def test_permute(ctx, shape, perm):
+    rng = np.random.default_rng(0)
+    a = crandn(rng, shape)
+    out = ctx.download(ctx.permute(ctx.upload(a), list(perm)))
+    assert np.array_equal(out, a.transpose(perm))
+
+
+def _contract_case(ctx, rng, shapes, labels, order, prec):
+    ts = [crandn(rng, s) for s in shapes]
+    ref = O.ncon(ts, labels, None, order)
+    from grafttn import _lib
+    out = ctx.download(ctx.contract([ctx.upload(t) for t in ts], labels, None, order, _lib.PRECISIONS[prec]))
+    return rel(out, ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "bf16x6", "bf16x3"])
+def test_contract_small_k(ctx, prec):
+    # W-like step: K = 10 (strided SIMT path), legs interleaved
+    rng = np.random.default_rng(1)
+    shapes = [(5, 6, 2, 7), (5, 2, 2, 3)]
+    labels = [[1, -1, 2, -2], [1, -3, 2, -4]]
+    assert _contract_case(ctx, rng, shapes, labels, [0, 1], prec) < RTOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "bf16x6", "bf16x3"])
+@pytest.mark.parametrize("mkn", [(130, 200, 70), (257, 1000, 129), (64, 96, 300), (1, 128, 1)])
+def test_contract_gemm(ctx, prec, mkn):
+    # GEMM path (K > 64): tcgen05 for the bf16 modes, SIMT for fp64 / fp32
+    M, K, N = mkn
+    rng = np.random.default_rng(2)
+    shapes = [(M, K), (K, N)]
+    labels = [[-1, 1], [1, -2]]
+    assert _contract_case(ctx, rng, shapes, labels, [0, 1], prec) < RTOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "bf16x6"])
+def test_contract_gemm_permuted(ctx, prec):
+    # contracted legs not innermost in the running tensor, statics with conj
+    rng = np.random.default_rng(3)
+    a, b = crandn(rng, (9, 40, 3, 8)), crandn(rng, (8, 11, 40))
+    labels = [[-1, 1, -2, 2], [2, -3, 1]]
+    ref = O.ncon([a, b], labels, [False, True])
+    from grafttn import _lib
+    out = ctx.download(ctx.contract([ctx.upload(a), ctx.upload(b)], labels, [False, True], None,
+                                    _lib.PRECISIONS[prec]))
+    assert rel(out, ref) < RTOL[prec]
+
+
+def test_tc_gemm_large(ctx):
+    # multi-tile, multi-stage pipeline: M, 2N and 2K well above one tile / stage ring
+    rng = np.random.default_rng(4)
+    M, K, N = 700, 2000, 300
+    from grafttn import _lib
+    for prec in ("bf16x6", "bf16x3"):
+        assert _contract_case(ctx, rng, [(M, K), (K, N)], [[-1, 1], [1, -2]], [0, 1], prec) < RTOL[prec]
+    ctx.sync()
+
+
+def test_chain_map_all_precisions(ctx):
+    # a chain of steps with mixed small-K / GEMM steps: an h2-like map on random statics
+    rng = np.random.default_rng(5)
+    D, w, d = 40, 5, 2
+    theta = crandn(rng, (D, d, d, D))
+    L, R = crandn(rng, (D, w, D)), crandn(rng, (D, w, D))
+    W1, W2 = crandn(rng, (w, d, d, w)), crandn(rng, (w, d, d, w))
+    # labels: theta [a, s1, s2, b]; L [a, wl, -1]; W1 [wl, -2, s1, wm]; W2 [wm, -3, s2, wr]; R [b, wr, -4]
+    labels = [[1, 2, 3, 4], [1, 5, -1], [5, -2, 2, 6], [6, -3, 3, 7], [4, 7, -4]]
+    ref = O.ncon([theta, L, W1, W2, R], labels)
+    from grafttn.contractions import EffectiveMap
+    for prec in ("fp64", "fp32", "bf16x6", "bf16x3"):
+        hm = EffectiveMap(ctx, theta.shape, labels, [0, 1, 2, 3, 4],
+                          [ctx.upload(x) for x in (L, W1, W2, R)], prec)
+        y = ctx.download(hm(ctx.upload(theta)))
+        assert rel(y, ref) < RTOL[prec], prec
+        hm.close()
+
+
+def test_qr_svd(ctx):
+    rng = np.random.default_rng(6)
+    for m, n in [(50, 20), (20, 50), (33, 33)]:
+        a = crandn(rng, (m, n))
+        Q, R = ctx.qr(ctx.upload(a))
+        Q, R = ctx.download(Q), ctx.download(R)
+        assert rel(Q @ R, a) < 1e-13
+        assert np.allclose(Q.conj().T @ Q, np.eye(min(m, n)), atol=1e-13)
+        assert np.allclose(np.tril(R, -1), 0)
+        U, S, Vh, disc = ctx.svd_trunc(ctx.upload(a))
+        U, Vh = ctx.download(U), ctx.download(Vh)
+        assert rel((U * S) @ Vh, a) < 1e-13
+        assert np.allclose(S, np.linalg.svd(a, compute_uv=False), rtol=1e-12)
+        U, S, Vh, disc = ctx.svd_trunc(ctx.upload(a), maxdim=5)
+        s_all = np.linalg.svd(a, compute_uv=False)
+        assert len(S) == 5 and abs(disc - np.sqrt(np.sum(s_all[5:] ** 2))) < 1e-12
+
+
+def test_lanczos_and_expm(ctx):
+    rng = np.random.default_rng(7)
+    n = 60
+    A = crandn(rng, (n, n))
+    Hm = (A + A.conj().T) / 2
+    # a map y = H x as a one-step contraction of x[n] with the static H[n, n] -> y[n]
+    from grafttn.contractions import EffectiveMap
+    hm = EffectiveMap(ctx, (n,), [[1], [-1, 1]], [0, 1], [ctx.upload(Hm)], "fp64")
+    x0 = crandn(rng, (n,))
+    E, v, info = hm.lanczos_min(ctx.upload(x0), krylovdim=30, tol=1e-13, maxiter=50)
+    w = np.linalg.eigvalsh(Hm)
+    assert abs(E - w[0]) < 1e-10, (E, w[0], info)
+    vv = ctx.download(v)
+    assert np.linalg.norm(Hm @ vv - E * vv) < 1e-6
+    y, info = hm.exponentiate(-0.3j, ctx.upload(x0), krylovdim=30, tol=1e-12)
+    import scipy.linalg as sla
+    ref = sla.expm(-0.3j * Hm) @ x0
+    assert rel(ctx.download(y), ref) < 1e-10
+    hm.close()

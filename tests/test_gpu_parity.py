@@ -1,0 +1,139 @@
+"""The reference's own known-answer gates, run on the GPU path through the C ABI:
+DMRG vs exact diagonalisation (test/runtests.jl:687-700), eff_h1 Rayleigh closure
+(:654-672), merge/split round trip (:674-685), planned map == unplanned ncon and Hermitian
+(test/contraction_planning.jl:111-160), TDVP1 vs exact propagation (:895-959)."""
+import numpy as np
+import pytest
+
+import grafttn as G
+from oracle import ttn_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def oracle_state(psi_dev):
+    o = O.TTNS(O.TreeTopology(psi_dev.topo.ids[0], [(psi_dev.topo.ids[psi_dev.topo.parent[i]], psi_dev.topo.ids[i])
+                                                     for i in range(1, psi_dev.topo.nnodes)]),
+               psi_dev.host_tensors(), psi_dev.center)
+    return o
+
+
+def test_dmrg_vs_ed_star31(ctx):
+    topo = G.star_topology(3, 1)
+    H = G.tfi(topo, g=0.9)
+    Hd = O.dense_hamiltonian(O.tfi(O.star_topology(3, 1), g=0.9))
+    E0, _ = O.exact_groundstate(Hd)
+    psi = G.random_ttns(np.random.default_rng(11), topo, 2, 2, ctx=ctx)
+    W = G.TTNO.from_hamiltonian(H, ctx)
+    _, Es = G.dmrg2(psi, W, G.TruncationScheme(maxdim=16), nsweeps=8)
+    assert abs(Es[-1] - E0) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "bf16x6"])
+def test_dmrg_star32_tfi(ctx, precision):
+    # star_topology(3,2) TFI (-1.0 ZZ, -0.9 X), bond 2, maxdim 32, 10 sweeps (exactly ED-checkable)
+    topo = G.star_topology(3, 2)
+    H = G.tfi(topo, J=1.0, g=0.9)
+    E0, _ = O.exact_groundstate(O.dense_hamiltonian(O.tfi(O.star_topology(3, 2), J=1.0, g=0.9)))
+    psi = G.random_ttns(np.random.default_rng(1), topo, 2, 2, ctx=ctx)
+    W = G.TTNO.from_hamiltonian(H, ctx)
+    _, Es = G.dmrg2(psi, W, G.TruncationScheme(maxdim=32), nsweeps=10, precision=precision)
+    assert abs(Es[-1] - E0) / abs(E0) < 1e-10
+
+
+def test_h1_closure_and_hermitian(ctx):
+    topo = G.star_topology(3, 2)
+    H = G.tfi(topo)
+    W = G.TTNO.from_hamiltonian(H, ctx)
+    psi = G.random_ttns(np.random.default_rng(3), topo, 2, 4, ctx=ctx)
+    o = oracle_state(psi)
+    Ws = O.ttno_nn(O.tfi(o.topo))
+    v = O.to_dense(o)
+    Hd = O.dense_hamiltonian(O.tfi(o.topo))
+    e_dense = np.vdot(v, Hd @ v)
+    e_gpu = G.expect(psi, W)
+    assert abs(e_gpu - e_dense) < 1e-12
+    cache = G.EnvCache(topo)
+    c = psi.center
+    h1 = G.eff_h1(cache, psi, W, c)
+    x = psi.tensors[c]
+    assert abs(ctx.dot(x, h1(x)) - e_dense) < 1e-12
+    rng = np.random.default_rng(4)
+    a = ctx.upload(O.randn_c(rng, tuple(x.shape)))
+    b = ctx.upload(O.randn_c(rng, tuple(x.shape)))
+    assert abs(ctx.dot(a, h1(b)) - ctx.dot(h1(a), b)) < 1e-11 * ctx.norm(a) * ctx.norm(b)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 2e-5), ("bf16x6", 2e-6), ("bf16x3", 1e-3)])
+def test_h2_matches_oracle_binary_heisenberg(ctx, precision, tol):
+    # planned GPU map == oracle ncon on every bond of a binary tree (contraction_planning.jl:111-160)
+    topo = G.binary_topology(3)
+    H = G.heisenberg(topo)
+    W = G.TTNO.from_hamiltonian(H, ctx)
+    psi = G.random_ttns(np.random.default_rng(5), topo, 2, 6, ctx=ctx)
+    ot = O.binary_topology(3)
+    Ws = O.ttno_nn(O.heisenberg(ot))
+    rng = np.random.default_rng(6)
+    for n in [7, 3, 1]:
+        m = topo.parent[n]
+        G.move_center(psi, n)
+        o = oracle_state(psi)
+        cache, ocache = G.EnvCache(topo), O.EnvCache(ot)
+        h2 = G.eff_h2(cache, psi, W, n, m, precision)
+        oh2 = O.eff_h2(ocache, o, Ws, n, m)
+        x = O.randn_c(rng, oh2.shape)
+        y = ctx.download(h2(ctx.upload(x)))
+        assert rel(y, oh2(x)) < tol, (n, precision)
+        h2.close()
+
+
+def test_h0_and_env_match_oracle(ctx):
+    topo = G.binary_topology(2)
+    H = G.heisenberg(topo)
+    W = G.TTNO.from_hamiltonian(H, ctx)
+    psi = G.random_ttns(np.random.default_rng(8), topo, 2, 3, ctx=ctx)
+    ot = O.binary_topology(2)
+    Ws = O.ttno_nn(O.heisenberg(ot))
+    n, m = 3, 1
+    G.move_center(psi, n)
+    o = oracle_state(psi)
+    cache, ocache = G.EnvCache(topo), O.EnvCache(ot)
+    for (u, v) in [(3, 1), (1, 3), (0, 1), (1, 0)]:
+        e = ctx.download(cache.env(psi, W, u, v))
+        assert rel(e, ocache.env(o, Ws, u, v)) < 1e-12
+    k0 = G.eff_h0(cache, psi, W, n, m)
+    ok0 = O.eff_h0(ocache, o, Ws, n, m)
+    x = O.randn_c(np.random.default_rng(9), ok0.shape)
+    assert rel(ctx.download(k0(ctx.upload(x))), ok0(x)) < 1e-12
+
+
+def test_merge_split_roundtrip(ctx):
+    topo = G.star_topology(3, 2)
+    psi = G.random_ttns(np.random.default_rng(10), topo, 2, 3, ctx=ctx)
+    v0 = O.to_dense(oracle_state(psi))
+    n, m = topo.index["b2_2"], topo.index["b2_1"]
+    G.move_center(psi, n)
+    theta = G.two_site_tensor(psi, n, m)
+    G.split_two_site(psi, theta, n, m, center_on="m")
+    assert np.linalg.norm(O.to_dense(oracle_state(psi)) - v0) < 1e-12
+
+
+def test_tdvp1_full_rank_vs_exact(ctx):
+    topo = G.star_topology(3, 2)
+    H = G.tfi(topo, g=0.9)
+    W = G.TTNO.from_hamiltonian(H, ctx)
+    psi = G.random_ttns(np.random.default_rng(12), topo, 2, 8, ctx=ctx)
+    Hd = O.dense_hamiltonian(O.tfi(O.star_topology(3, 2), g=0.9))
+    v0 = O.to_dense(oracle_state(psi))
+    dt, nsteps = 0.02, 5
+    vex = O.exact_evolve(Hd, v0, -1j * dt * nsteps)
+    ev = G.TDVP1(order=2)
+    for _ in range(nsteps):
+        ev.step(psi, W, -1j * dt)
+    v1 = O.to_dense(oracle_state(psi))
+    assert abs(1 - abs(np.vdot(v1, vex))) < 1e-10
+    assert abs(np.linalg.norm(v1) - 1) < 1e-10

@@ -1,0 +1,114 @@
+"""CPU gates: the oracle against the reference's known-answer tests (exact diagonalisation
+and identities), and the host-side metadata of the package against the oracle."""
+import numpy as np
+import pytest
+
+import grafttn as G
+from grafttn import contractions as GC
+from oracle import ttn_oracle as O
+
+
+def test_ttno_equals_dense_hamiltonian():
+    # test/runtests.jl:362-393: TTNO builder == dense H within 1e-12
+    for topo in (O.star_topology(3, 2), O.binary_topology(2), O.mps_topology(5)):
+        for H in (O.tfi(topo, g=0.7), O.heisenberg(topo)):
+            assert np.abs(O.ttno_to_dense(topo, O.ttno_nn(H)) - O.dense_hamiltonian(H)).max() < 1e-12
+
+
+def test_package_ttno_matches_oracle():
+    for name in ("star", "binary", "mps", "kary"):
+        gt = {"star": G.star_topology(3, 2), "binary": G.binary_topology(3), "mps": G.mps_topology(6),
+              "kary": G.kary_topology(4, 2)}[name]
+        ot = {"star": O.star_topology(3, 2), "binary": O.binary_topology(3), "mps": O.mps_topology(6),
+              "kary": O.kary_topology(4, 2)}[name]
+        assert gt.parent == ot.parent and gt.children == ot.children and gt.postorder() == ot.postorder()
+        for gh, oh in ((G.tfi(gt, J=1.0, g=0.9), O.tfi(ot, J=1.0, g=0.9)), (G.heisenberg(gt), O.heisenberg(ot))):
+            for a, b in zip(G.ttno_tensors(gh), O.ttno_nn(oh)):
+                assert a.shape == b.shape and np.array_equal(a, b)
+
+
+def test_dmrg_vs_ed():
+    # test/runtests.jl:687-700: TFI g=0.9 on star_topology(3,1), maxdim 16, 8 sweeps, 1e-10
+    topo = O.star_topology(3, 1)
+    H = O.tfi(topo, g=0.9)
+    E0, _ = O.exact_groundstate(O.dense_hamiltonian(H))
+    psi = O.random_ttns(np.random.default_rng(1), topo, 2, 2)
+    _, Es = O.dmrg2(psi, O.ttno_nn(H), maxdim=16, nsweeps=8)
+    assert abs(Es[-1] - E0) < 1e-10
+
+
+def test_dmrg_star32_matches_golden():
+    # the CPU-runnable workload: star_topology(3,2), -1.0 ZZ, -0.9 X, bond 2, maxdim 32
+    golden = np.load(__file__.replace("test_oracle.py", "golden/star32_tfi.npz"))
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo, J=1.0, g=0.9)
+    psi = O.random_ttns(np.random.default_rng(1), topo, 2, 2)
+    _, Es = O.dmrg2(psi, O.ttno_nn(H), maxdim=32, nsweeps=10)
+    assert abs(Es[-1] - float(golden["E_ed"])) < 1e-10
+
+
+def test_closure_roundtrip_hermitian():
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo)
+    Ws = O.ttno_nn(H)
+    psi = O.random_ttns(np.random.default_rng(3), topo, 2, 4)
+    v = O.to_dense(psi)
+    Hd = O.dense_hamiltonian(H)
+    # eff_h1 closes to <psi|H|psi> (test/runtests.jl:654-672)
+    assert abs(O.expect(psi, Ws) - np.vdot(v, Hd @ v)) < 1e-12
+    # merge/split round trip (test/runtests.jl:674-685)
+    n, m = topo.index["b2_2"], topo.index["b2_1"]
+    O.move_center(psi, n)
+    th = O.two_site_tensor(psi, n, m)
+    O.split_two_site(psi, th, n, m, center_on="m")
+    assert np.linalg.norm(O.to_dense(psi) - v) < 1e-12
+    # planned (env-first) == unplanned single ncon, and Hermitian (contraction_planning.jl:111-160)
+    cache = O.EnvCache(topo)
+    h2 = O.eff_h2(cache, psi, Ws, n, m)
+    rng = np.random.default_rng(0)
+    a, b = O.randn_c(rng, h2.shape), O.randn_c(rng, h2.shape)
+    y_plan = h2(a)
+    y_ref = O.ncon([a] + h2.statics, h2.labels, None, list(range(len(h2.labels))))
+    assert np.linalg.norm(y_plan - y_ref) < 1e-11 * np.linalg.norm(y_ref)
+    assert abs(np.vdot(a, h2(b)) - np.vdot(h2(a), b)) < 1e-11 * np.linalg.norm(a) * np.linalg.norm(b)
+
+
+def test_tdvp1_full_rank_vs_exact():
+    # test/runtests.jl:895-930: full-rank TDVP1 == exact evolution (fidelity 1e-10)
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo, g=0.9)
+    Ws = O.ttno_nn(H)
+    psi = O.random_ttns(np.random.default_rng(2), topo, 2, 8)
+    Hd = O.dense_hamiltonian(H)
+    vex = O.exact_evolve(Hd, O.to_dense(psi), -1j * 0.02 * 5)
+    cache = None
+    for _ in range(5):
+        cache = O.tdvp1_step(psi, Ws, -1j * 0.02, cache)
+    v = O.to_dense(psi)
+    assert abs(1 - abs(np.vdot(v, vex))) < 1e-10
+    assert abs(O.expect(psi, Ws) - np.vdot(vex, Hd @ vex)) < 1e-8
+
+
+@pytest.mark.parametrize("which", ["h1", "h2", "env"])
+def test_package_specs_match_oracle(which):
+    gt, ot = G.binary_topology(3), O.binary_topology(3)
+    for n in range(gt.nnodes):
+        K = gt.nchildren(n)
+        if which == "h1":
+            gl, go, _ = GC.h1_spec(gt, n, K + 2, K + 3)
+            ol, oo = O.h1_spec(ot, n, K + 2, K + 3)
+            assert gl == ol and go == oo
+        elif which == "env":
+            for v in gt.neighbors(n):
+                gl, gc, _, _ = GC.env_spec(gt, n, v, K + 2, K + 3)
+                a = np.zeros((1,) * (K + 2))
+                w = np.zeros((1,) * (K + 3))
+                ol, oc, _, _ = O.env_spec(ot, n, v, a, w)
+                assert gl == ol and gc == oc
+        elif gt.parent[n] >= 0:
+            m = gt.parent[n]
+            pn = K + 1
+            xr = pn + gt.nchildren(m) + 1
+            gl, go, _ = GC.h2_spec(gt, n, m, xr, K + 3, gt.nchildren(m) + 3, pn)
+            ol, oo, _ = O.h2_spec(ot, n, m, xr, K + 3, gt.nchildren(m) + 3, pn)
+            assert gl == ol and go == oo
