@@ -6,7 +6,7 @@ from oracle import ttn_oracle as O
 
 pytestmark = pytest.mark.gpu
 
-RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 2e-6, "bf16x3": 1e-3}
+RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 1e-5, "bf16x3": 1e-3}  # bf16x6: FP32 TMEM accumulation error grows with K
 
 
 def crandn(rng, shape):
