@@ -1,0 +1,401 @@
+"""Benchmark: eff_h2 applies/s at bond dimension 1024 (dense ComplexF64 Heisenberg,
+63-site binary tree), mixed split-bf16 tcgen05 path vs the plain FP64 GPU path.
+
+One step = one application y = H_eff x of the two-site effective Hamiltonian of the
+depth-3 -> depth-2 edge of binary_topology(5) at D = 1024 (Θ legs [8, 8, 2, 128, 2, 1024],
+33.6 M complex entries; environments [8,5,8] x2, [128,5,128], [1024,5,1024]; Heisenberg
+TTNO, w = 5).  Inputs are seeded synthetic tensors of exactly those shapes.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the reference
+path (numpy/OpenBLAS on all host cores) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "graft.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "eff_h2 applies/s at D=1024 (bin63 Heisenberg, depth3->depth2 edge), mixed bf16x6 tcgen05"
+WORKLOAD = "heisenberg_bin63_d3d2_D1024_eff_h2"
+D, W_OP, d = 1024, 5, 2
+
+
+# ---------------------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------------------
+
+WORKLOADS = {
+    # name: (topology, node n, bond dim) -- n's parent is m
+    "heisenberg_bin63_d3d2_D1024_eff_h2": ("binary", "n3_1", 1024),
+    "heisenberg_bin63_d3d2_D256_eff_h2": ("binary", "n3_1", 256),
+    "heisenberg_chain63_mid_D1024_eff_h2": ("mps", "site32", 1024),
+}
+
+
+def workload_arrays(name=WORKLOAD, seed=7):
+    """Labels, order and seeded synthetic statics of one eff_h2 map of the workload table.
+    Bond dimensions follow the saturated tree: min(D, product of the legs below)."""
+    import grafttn as G
+    from grafttn import contractions as GC
+    kind, nid, Dm = WORKLOADS[name]
+    topo = G.binary_topology(5) if kind == "binary" else G.mps_topology(63)
+    n = topo.index[nid]
+    m = topo.parent[n]
+    rng = np.random.default_rng(seed)
+
+    def crandn(shape):
+        return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2)
+
+    def env(dim):
+        # Hermitian in (ket, bra) for every operator index, like a converged environment
+        e = crandn((dim, W_OP, dim)) / np.sqrt(dim)
+        return (e + e.conj().transpose(2, 1, 0)) / 2
+    below = {}
+    for v in topo.postorder():
+        below[v] = d * int(np.prod([below[c] for c in topo.children[v]] or [1]))
+    bond = {v: min(Dm, below[v]) for v in range(topo.nnodes)}
+    Ws = G.ttno_tensors(G.heisenberg(topo))
+    k = topo.childslot(m, n)
+    x_shape = tuple([bond[c] for c in topo.children[n]] + [d]
+                    + [bond[c] for c in topo.children[m] if c != n] + [d, bond[m]])
+    pn = topo.nchildren(n) + 1
+    labels, order, envs = GC.h2_spec(topo, n, m, len(x_shape), Ws[n].ndim, Ws[m].ndim, pn)
+    statics = [Ws[n], Ws[m]] + [env(bond[w] if w != topo.parent[u] else bond[u]) for (w, u) in envs]
+    theta = crandn(x_shape)
+    theta /= np.linalg.norm(theta)
+    assert k >= 0
+    return x_shape, labels, order, statics, theta
+
+
+def oracle_flops(x_shape, labels, order, statics):
+    from oracle import ttn_oracle as O
+    return 8 * O.plan_macs([x_shape] + [s.shape for s in statics], labels, order)
+
+
+# ---------------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------------
+
+REASON_BITS = {0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap", 0x8: "hw_slowdown",
+               0x10: "sync_boost", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown", 0x100: "display_clock_setting"}
+
+
+class ClockSampler:
+    def __init__(self, device=0):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 3:
+                try:
+                    self.samples.append((float(parts[0]), float(parts[1]), int(parts[2], 16)))
+                except ValueError:
+                    pass
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [s[0] for s in self.samples]
+        reasons = set()
+        for s in self.samples:
+            for bit, name in REASON_BITS.items():
+                if s[2] & bit and name != "gpu_idle":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(s[1] for s in self.samples),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------
+# CPU arm: the oracle restatement of the reference path on the host cores
+# ---------------------------------------------------------------------------------------
+
+def cpu_apply_rate(x_shape, labels, order, statics, theta, budget_s=20.0, max_applies=3, warm=False):
+    """Applications of the oracle's env-first map per second on the host cores; stops after
+    `max_applies` or once `budget_s` is spent (at least one application)."""
+    from oracle import ttn_oracle as O
+    hm = O.EffMap(labels, order, statics, x_shape)
+    if warm:
+        hm(theta)
+    n, t0 = 0, time.perf_counter()
+    while n < max_applies:
+        hm(theta)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return n / el, n, el
+
+
+def blas_threads():
+    try:
+        from threadpoolctl import threadpool_info
+        info = threadpool_info()
+        return max((i.get("num_threads", 1) for i in info), default=os.cpu_count())
+    except Exception:
+        return os.cpu_count()
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the CPU restatement of the reference path on all host cores.  A
+    step is one full application; the timed steps are capped by a 150 s budget (a bounded
+    sample of K steps), the count actually timed is reported in `steps`."""
+    if rank != 0:
+        return
+    from oracle import ttn_oracle as O
+    x_shape, labels, order, statics, theta = workload_arrays(args.workload)
+    flops = oracle_flops(x_shape, labels, order, statics)
+    hm = O.EffMap(labels, order, statics, x_shape)
+    t_w = time.perf_counter()
+    for _ in range(min(args.warmup, 1)):
+        hm(theta)
+    t_apply = time.perf_counter() - t_w if args.warmup > 0 else None
+    steps = args.steps
+    if t_apply:
+        steps = max(1, min(args.steps, int(150.0 // max(t_apply, 1e-9))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        hm(theta)
+    total = time.perf_counter() - t0
+    value = steps / total
+    args = argparse.Namespace(**{**vars(args), "steps": steps})
+    cores = blas_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
+        "data": "synthetic (seeded Gaussian tensors of the workload shapes)",
+        "config": {"workload": args.workload, "theta_shape": list(x_shape), "bond_dim": D, "ttno_bond": W_OP,
+                   "algorithmic_flops_per_apply": flops},
+        "cpu_baseline": {"value": value, "unit": "applies/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full eff_h2 applications (numpy tensordot chain, env-first order)"},
+        "e2e": {"value": value, "unit": "applies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "achieved_tflops": flops * value / 1e12,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------------
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return j.get("bf16_tflops"), j.get("hbm_gbs"), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+def profile_traffic(kernel, workload):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary (profiles/traffic.txt)."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == kernel and parts[1] == workload:
+                return float(parts[2])
+    return None
+
+
+def run_ours(args, rank, world):
+    import torch
+    import grafttn as G
+    from grafttn.contractions import EffectiveMap
+    if world > 1:
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+    dev = torch.cuda.current_device()
+    ctx = G.default_context(dev)
+    x_shape, labels, order, statics, theta = workload_arrays(args.workload)
+    flops = oracle_flops(x_shape, labels, order, statics)
+    dstat = [ctx.upload(s) for s in statics]
+    x = ctx.upload(theta)
+    hm = EffectiveMap(ctx, x_shape, labels, order, dstat, "bf16x6")
+    y = ctx.empty(hm.y_shape)
+    assert abs(hm.flops - flops) / flops < 1e-12, (hm.flops, flops)
+    stream = ctx.stream
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        hm.apply_into(x, y)
+    ctx.sync()
+    barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        time.sleep(0.3)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            hm.apply_into(x, y)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        time.sleep(0.2)
+    ctx.sync()
+    launches = ctx.launches - l0
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    barrier()
+    value = world * args.steps / (ms / 1000.0)
+    # accuracy of the mixed apply against the FP64 apply of the same map
+    y64 = ctx.empty(hm.y_shape)
+    hm.apply_into(x, y64, precision=0)
+    ctx.sync()
+    diff = ctx.empty(hm.y_shape)
+    ctx.axpby(1.0, y, 0.0, diff)
+    ctx.axpby(-1.0, y64, 1.0, diff)
+    mixed_rel_err = ctx.norm(diff) / ctx.norm(y64)
+
+    if rank != 0:
+        return
+    # FP64 GPU path on the same map (a bounded sample: each apply takes ~2 s on GB300)
+    fp64_steps = max(1, min(2, args.steps))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(fp64_steps):
+        hm.apply_into(x, y64, precision=0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_rate = fp64_steps / (e0.elapsed_time(e1) / 1000.0)
+
+    # per-launch timing of one application (CUDA events on the launching stream)
+    recs = hm.apply_profiled(x, y)
+    by = {}
+    for name, t, f in recs:
+        a = by.setdefault(name, [0, 0.0, 0.0])
+        a[0] += 1
+        a[1] += t
+        a[2] += f
+    tot = sum(v[1] for v in by.values())
+    kernels = {k: {"launches": v[0], "ms": round(v[1], 4), "share": round(v[1] / tot, 4)} for k, v in by.items()}
+    tc = by.get("tc_gemm", [1, 1e-9, 0.0])
+    bf16_peak, hbm_peak, peak_kind = measured_peaks()
+    achieved = tc[2] / (tc[1] / 1000.0) / 1e12          # algorithmic complex flops / time
+    executed = achieved * 6                               # 6 bf16 products per complex MAC
+    traffic = profile_traffic("tc_gemm", args.workload)
+
+    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    xh = torch.from_numpy(theta.copy()).pin_memory()
+    yh = torch.empty(hm.y_shape, dtype=torch.complex128).pin_memory()
+    import ctypes as C
+    from grafttn._lib import check
+    e2e_steps = max(2, min(5, args.steps))
+    hm.ctx.lib.gtn_map_apply_host(hm.h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        check(hm.ctx.lib.gtn_map_apply_host(hm.h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr())), ctx.h)
+    e2e_rate = e2e_steps / (time.perf_counter() - t0)
+
+    # CPU baseline: the oracle on the host cores, bounded sample of the same workload
+    cpu_rate, cpu_n, cpu_el = cpu_apply_rate(x_shape, labels, order, statics, theta, budget_s=20.0, max_applies=2)
+    del statics
+
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16x6 split products on tcgen05, f32 accumulate, c128 in/out",
+        "data": "synthetic (seeded Gaussian tensors of the workload shapes)",
+        "config": {"workload": args.workload, "theta_shape": list(x_shape), "bond_dim": D, "ttno_bond": W_OP,
+                   "algorithmic_flops_per_apply": flops, "l2": "inputs larger than L2 (Θ and intermediates exceed 129 MB)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64_gpu": {"value": fp64_rate, "unit": "applies/s", "speedup_mixed_vs_fp64": value / world / fp64_rate,
+                     "samples": fp64_steps},
+        "mixed_vs_fp64_rel_err": mixed_rel_err,
+        "algorithmic_tflops": flops * value / world / 1e12,
+        "kernels": kernels,
+        "roofline": {"bound": "tensor", "kernel": "tc_gemm", "achieved": achieved, "peak": bf16_peak,
+                     "unit": "TFLOP/s", "frac": achieved / bf16_peak, "peak_kind": f"bf16 dense burst ({peak_kind})",
+                     "executed_tensor_tflops": executed, "frac_executed": executed / bf16_peak,
+                     "achieved_definition": "8*M*N*K complex-MAC flops of the tc_gemm launches / their event time",
+                     "traffic": traffic},
+        "cpu_baseline": {"value": cpu_rate, "unit": "applies/s", "cores": blas_threads(), "kind": "port",
+                         "sample": f"{cpu_n} eff_h2 application(s) of the same workload, {cpu_el:.1f} s"},
+        "e2e": {"value": e2e_rate, "unit": "applies/s", "h2d_bytes_per_step": int(theta.size * 16),
+                "d2h_bytes_per_step": int(np.prod(hm.y_shape) * 16),
+                "path": "gtn_map_apply_host (C ABI, pinned host buffers)"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if args.impl != "reference":
+            import torch
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+        dist.init_process_group(backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_ours(args, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -157,6 +157,13 @@ int gtn_map_apply(gtn_map map, const void* x, void* y) {
   return gtn_map_apply_prec(map, map->precision, x, y);
 }
 
+int gtn_map_apply_profiled(gtn_map map, int precision, const void* x, void* y, int cap, double* ms,
+                           int* kind, double* flops, int* count) {
+  if (!map || !x || !y || !ms || !kind || !flops || !count) return GTN_ERR_INVALID;
+  return map_run_profiled(map, precision, static_cast<const double2*>(x), static_cast<double2*>(y), cap, ms,
+                          kind, flops, count);
+}
+
 int gtn_map_apply_host(gtn_map map, const void* x_host, void* y_host) {
   if (!map || !x_host || !y_host) return GTN_ERR_INVALID;
   gtn_ctx ctx = map->ctx;

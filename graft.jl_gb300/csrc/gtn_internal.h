@@ -172,4 +172,6 @@ int plan_build(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dim
                const int* labels, const int* conj, const int* order, const void* const* statics,
                int precision, gtn_map map);
 int map_run(gtn_map map, int precision, const double2* x, double2* y);
+int map_run_profiled(gtn_map map, int precision, const double2* x, double2* y, int cap, double* ms,
+                     int* kind, double* flops, int* count);
 void map_free(gtn_map map);

@@ -267,6 +267,32 @@ void map_free(gtn_map map) {
   map->owned.clear();
 }
 
+// Optional per-launch timing: CUDA events around every kernel of one application.
+struct ProfRec {
+  cudaEvent_t a, b;
+  int kind;
+  double flops;
+};
+static std::vector<ProfRec>* g_prof = nullptr;
+
+static void prof_begin(cudaStream_t s) {
+  if (!g_prof) return;
+  ProfRec r;
+  cudaEventCreate(&r.a);
+  cudaEventCreate(&r.b);
+  cudaEventRecord(r.a, s);
+  r.kind = -1;
+  r.flops = 0;
+  g_prof->push_back(r);
+}
+static void prof_end(cudaStream_t s, int kind, double flops) {
+  if (!g_prof || g_prof->empty()) return;
+  ProfRec& r = g_prof->back();
+  cudaEventRecord(r.b, s);
+  r.kind = kind;
+  r.flops = flops;
+}
+
 int map_run(gtn_map map, int precision, const double2* x, double2* y) {
   gtn_ctx ctx = map->ctx;
   cudaStream_t s = ctx->stream;
@@ -288,13 +314,19 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
     void* out = bufs[i & 1];
     if (fp64) {
       if (st.small) {
+        prof_begin(s);
         e = launch_small_contract_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, (int)st.K,
                                        (int)st.N, st.b64, static_cast<double2*>(out), s);
+        prof_end(s, GTN_KERNEL_SMALL, 8.0 * st.macs);
         ctx->launches++;
       } else {
         double2* A = static_cast<double2*>(map->abuf);
+        prof_begin(s);
         e = launch_gather_c128_to_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.K, A, s);
+        prof_end(s, GTN_KERNEL_GATHER, 0.0);
+        prof_begin(s);
         if (e == cudaSuccess) e = launch_zgemm_simt(A, st.b64, static_cast<double2*>(out), st.M, st.N, st.K, s);
+        prof_end(s, GTN_KERNEL_ZGEMM, 8.0 * st.macs);
         ctx->launches += 2;
       }
     } else {
@@ -302,8 +334,10 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
         // the FP32 kernels read complex FP32: convert the FP64 input once
         void* conv = bufs[(i + 1) & 1];
         int64_t blocks = std::min<int64_t>((map->x_elems + 255) / 256, 152 * 8);
+        prof_begin(s);
         c128_to_c64_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(
             static_cast<const double2*>(cur), static_cast<float2*>(conv), map->x_elems);
+        prof_end(s, GTN_KERNEL_CONVERT, 0.0);
         ctx->launches++;
         e = cudaGetLastError();
         cur = conv;
@@ -311,23 +345,31 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
         if (e != cudaSuccess) break;
       }
       if (st.small) {
+        prof_begin(s);
         e = launch_small_contract_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, (int)st.K,
                                       (int)st.N, st.b32, static_cast<float2*>(out), s);
+        prof_end(s, GTN_KERNEL_SMALL, 8.0 * st.macs);
         ctx->launches++;
       } else if (!tc) {
         float2* A = static_cast<float2*>(map->abuf);
+        prof_begin(s);
         e = launch_gather_c64_to_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.K, A, s);
+        prof_end(s, GTN_KERNEL_GATHER, 0.0);
+        prof_begin(s);
         if (e == cudaSuccess) e = launch_cgemm_simt(A, st.b32, static_cast<float2*>(out), st.M, st.N, st.K, s);
+        prof_end(s, GTN_KERNEL_CGEMM, 8.0 * st.macs);
         ctx->launches += 2;
       } else {
         __nv_bfloat16* Apl = static_cast<__nv_bfloat16*>(map->abuf);
         const int64_t pstride = st.M * 2 * st.Kp;
+        prof_begin(s);
         if (cur64)
           e = launch_split_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
                                 pstride, Apl, s);
         else
           e = launch_split_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
                                pstride, Apl, s);
+        prof_end(s, GTN_KERNEL_SPLIT, 0.0);
         ctx->launches++;
         if (e == cudaSuccess) {
           TcGemmArgs a;
@@ -350,7 +392,9 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
             for (int q = 0; q < 3; ++q) { a.prod_a[q] = pa[q]; a.prod_b[q] = pb[q]; }
           }
           std::string why;
+          prof_begin(s);
           e = launch_tc_gemm(a, ctx->d_errflag, s, &why);
+          prof_end(s, GTN_KERNEL_TC_GEMM, 8.0 * st.macs);
           ctx->launches++;
           if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, "tc_gemm: " + why + " " + cudaGetErrorString(e));
         }
@@ -360,13 +404,41 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
     cur = out;
   }
   if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("map step: ") + cudaGetErrorString(e));
+  prof_begin(s);
   if (cur64)
     e = launch_gather_c128_to_c128(static_cast<const double2*>(cur), map->fin_mg, map->fin_kg, map->fin_M,
                                    map->fin_K, map->fin_K, y, s);
   else
     e = launch_gather_c64_to_c128(static_cast<const float2*>(cur), map->fin_mg, map->fin_kg, map->fin_M,
                                   map->fin_K, map->fin_K, y, s);
+  prof_end(s, GTN_KERNEL_OUTPUT, 0.0);
   ctx->launches++;
   if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("map output: ") + cudaGetErrorString(e));
+  return GTN_OK;
+}
+
+int map_run_profiled(gtn_map map, int precision, const double2* x, double2* y, int cap, double* ms,
+                     int* kind, double* flops, int* count) {
+  std::vector<ProfRec> recs;
+  g_prof = &recs;
+  int st = map_run(map, precision, x, y);
+  g_prof = nullptr;
+  cudaError_t e = cudaStreamSynchronize(map->ctx->stream);
+  int n = 0;
+  for (auto& r : recs) {
+    float t = 0.f;
+    if (st == GTN_OK && e == cudaSuccess) cudaEventElapsedTime(&t, r.a, r.b);
+    if (n < cap) {
+      ms[n] = t;
+      kind[n] = r.kind;
+      flops[n] = r.flops;
+    }
+    ++n;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  *count = n;
+  if (st != GTN_OK) return st;
+  if (e != cudaSuccess) return set_err(map->ctx, GTN_ERR_CUDA, cudaGetErrorString(e));
   return GTN_OK;
 }

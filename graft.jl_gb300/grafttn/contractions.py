@@ -204,6 +204,17 @@ class EffectiveMap:
             raise _lib.SpaceMismatch(f"map input shape {tuple(x.shape)} != {self.x_shape}")
         return self.apply_into(x.contiguous(), self.ctx.empty(self.y_shape), precision)
 
+    def apply_profiled(self, x, y, precision=None, cap=256):
+        """One application with CUDA events around each launch: list of (kernel, ms, flops)."""
+        prec = self.precision if precision is None else precision
+        ms = (C.c_double * cap)()
+        kind = (C.c_int * cap)()
+        fl = (C.c_double * cap)()
+        cnt = C.c_int()
+        check(self.ctx.lib.gtn_map_apply_profiled(self.h, prec, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                                                  cap, ms, kind, fl, C.byref(cnt)), self.ctx.h, "map_apply_profiled")
+        return [(_lib.KERNEL_NAMES.get(kind[i], str(kind[i])), ms[i], fl[i]) for i in range(min(cnt.value, cap))]
+
     def apply_host(self, x_host):
         """Host buffers in and out (host->device copy, apply, device->host copy in one call)."""
         xh = np.ascontiguousarray(x_host, dtype=np.complex128)

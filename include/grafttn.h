@@ -89,6 +89,22 @@ int gtn_map_apply_host(gtn_map map, const void* x_host, void* y_host);
  * number of pair steps, and device workspace bytes held by the map. */
 int gtn_map_info(gtn_map map, int64_t* x_elems, int64_t* y_elems, double* flops,
                  int* n_steps, int64_t* bytes);
+/* Kernel kinds reported by gtn_map_apply_profiled. */
+enum {
+  GTN_KERNEL_SMALL = 0,     /* strided small-K contraction (SIMT) */
+  GTN_KERNEL_GATHER = 1,    /* permutation of the running tensor into a K-major operand */
+  GTN_KERNEL_SPLIT = 2,     /* permutation + bf16 slice split */
+  GTN_KERNEL_ZGEMM = 3,     /* complex FP64 SIMT GEMM */
+  GTN_KERNEL_CGEMM = 4,     /* complex FP32 SIMT GEMM */
+  GTN_KERNEL_TC_GEMM = 5,   /* tcgen05 split-bf16 GEMM */
+  GTN_KERNEL_CONVERT = 6,   /* c128 -> c64 input conversion */
+  GTN_KERNEL_OUTPUT = 7     /* final permutation into the output leg order */
+};
+/* One application with CUDA events around every kernel launch (synchronises).  Writes up
+ * to `cap` records: duration in ms, kernel kind and algorithmic FLOPs of that launch;
+ * *count = number of launches of the application. */
+int gtn_map_apply_profiled(gtn_map map, int precision, const void* x, void* y, int cap, double* ms,
+                           int* kind, double* flops, int* count);
 /* Output leg dims of the map (rank written to *rank, dims to dims[0..rank-1]). */
 int gtn_map_out_shape(gtn_map map, int* rank, int64_t* dims);
 
