@@ -153,6 +153,19 @@ int gtn_qr(gtn_ctx ctx, int64_t m, int64_t n, const void* A, void* Q, void* R);
 int gtn_dot(gtn_ctx ctx, int64_t n, const void* x, const void* y, double* out2);  /* <x,y> */
 int gtn_axpby(gtn_ctx ctx, int64_t n, double a_re, double a_im, const void* x,
               double b_re, double b_im, void* y);                                  /* y = a x + b y */
+/* Allocation-free batched projections out[j] = <V_j, w> (j < J), complex FP64, for callers
+ * that cannot allocate device memory (a host whose own pool owns all HBM, or a loop that
+ * cannot take cudaMalloc's device-wide synchronisation).  No counterpart in the reference.
+ * Needs no context: runs on `stream` (a cudaStream_t, NULL = legacy default) of the current
+ * device.  V holds J vectors of n elements, `ldv` elements apart (ldv >= n when J > 1);
+ * w has n elements; out (device) receives J values.  Limits: 1 <= J <= 64; partial sums
+ * live in a library-owned 512 KiB __device__ array shared by all calls on a device, so
+ * calls that overlap on the GPU race (order them on one stream).  The first call on each
+ * device resolves that array's address; make it before any stream capture.  Returns
+ * GTN_ERR_INVALID for J outside 1..64 or bad pointers / strides; never allocates. */
+int gtn_multidot_noalloc(void* stream, int64_t n, int J, const void* V, int64_t ldv, const void* w,
+                         void* out);
+
 /* In-place diagonal scaling of a row-major rows x cols c128 matrix by real HOST factors:
  * side 0 scales column j by d[j] (U * diag(S)), side 1 scales row i by d[i] (diag(S) * Vh). */
 int gtn_diag_scale(gtn_ctx ctx, int64_t rows, int64_t cols, const double* d_host, int side, void* A);
