@@ -154,7 +154,10 @@ struct gtn_map_s {
   GroupSpec fin_mg, fin_kg;  // final permute of the last C into y order
   int64_t fin_M = 0, fin_K = 0;
   bool fin_identity = false;
-  double flops = 0;
+  double flops = 0;        // algorithmic FLOPs of the reference's env-first chain
+  double exec_flops = 0;   // FLOPs of the executed (possibly grouped) chain
+  int n_groups = 0;
+  gtn_map fp64_alt = nullptr;  // FP64-optimal plan sharing this map's workspace
   int64_t max_t = 0;       // largest running tensor (elements)
   int64_t max_a = 0;       // largest A operand (elements, for permuted / split staging)
   int64_t max_apl = 0;     // largest split-plane staging (bf16 elements per plane * planes)
@@ -170,7 +173,7 @@ struct gtn_map_s {
 
 int plan_build(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dims,
                const int* labels, const int* conj, const int* order, const void* const* statics,
-               int precision, gtn_map map);
+               int precision, gtn_map map, bool allow_group = true, bool alloc_ws = true);
 int map_run(gtn_map map, int precision, const double2* x, double2* y);
 int map_run_profiled(gtn_map map, int precision, const double2* x, double2* y, int cap, double* ms,
                      int* kind, double* flops, int* count);

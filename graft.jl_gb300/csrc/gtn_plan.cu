@@ -12,8 +12,10 @@
 #include "gtn_internal.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
+#include <new>
 #include <set>
 
 namespace {
@@ -69,6 +71,89 @@ int nplanes_of(int precision) { return precision == GTN_PREC_BF16X6 ? 3 : 2; }
 
 }  // namespace
 
+namespace {
+
+// ---- static grouping: pre-contract consecutive statics when the cost model says so -----
+// The chain absorbs statics one at a time; small statics (the child environments of a node
+// whose children have small bonds, a TTNO tensor) can be contracted with each other once,
+// at map creation, so that the running tensor meets one larger operator in a tensor-core
+// GEMM instead of several memory-bound small-K passes.  The reported algorithmic FLOPs stay
+// those of the reference's env-first chain.
+
+constexpr int64_t kMaxCombined = int64_t(1) << 22;  // elements of a pre-contracted static
+
+double est_step_time(int prec, double M, double K, double N) {
+  const bool fp64 = prec == GTN_PREC_FP64;
+  const double e = fp64 ? 16.0 : 8.0;
+  const double flops = 8.0 * M * K * N;
+  const double hbm = 5e12;
+  const bool small = K <= kSmallK && small_contract_fits((int)K, (int)std::min(N, 1048576.0), sizeof(double2));
+  double t = 5e-6;  // launch and tail
+  if (small) return t + (M * K + M * N) * e / hbm + flops / (fp64 ? 1.1e12 : 15e12);
+  if (fp64) return t + flops / 1.1e12 + (2 * M * K + M * N) * e / hbm;
+  if (prec == GTN_PREC_FP32) return t + flops / 20e12 + (2 * M * K + M * N) * e / hbm;
+  const double rate = prec == GTN_PREC_BF16X6 ? 200e12 : 300e12;
+  const double P = prec == GTN_PREC_BF16X6 ? 3.0 : 2.0;
+  const double Kp = std::ceil(K / 32.0) * 32.0;
+  return t + flops / rate + (M * K * e + M * 2 * Kp * P * 2 + M * N * 8) / hbm;
+}
+
+struct ChainOp {
+  std::vector<int> L;
+  std::vector<int64_t> D;
+};
+
+// External legs of a group of operands: labels not paired inside the group, in order.
+ChainOp group_external(const std::vector<ChainOp>& ops) {
+  std::map<int, int> cnt;
+  for (auto& o : ops)
+    for (int l : o.L) cnt[l]++;
+  ChainOp out;
+  for (auto& o : ops)
+    for (size_t i = 0; i < o.L.size(); ++i)
+      if (!(o.L[i] > 0 && cnt[o.L[i]] == 2)) {
+        out.L.push_back(o.L[i]);
+        out.D.push_back(o.D[i]);
+      }
+  return out;
+}
+
+// (cost, env-first MACs) of absorbing `chain` into the running tensor `x`.
+std::pair<double, double> chain_cost(const ChainOp& x, const std::vector<ChainOp>& chain, int prec) {
+  std::vector<int> LT = x.L;
+  std::vector<int64_t> DT = x.D;
+  double t = 0, macs = 0;
+  for (auto& S : chain) {
+    double M = 1, K = 1, N = 1;
+    std::vector<int> nL;
+    std::vector<int64_t> nD;
+    std::vector<int> shared;
+    for (size_t a = 0; a < LT.size(); ++a) {
+      const bool sh = LT[a] > 0 && std::find(S.L.begin(), S.L.end(), LT[a]) != S.L.end();
+      if (sh) { K *= (double)DT[a]; shared.push_back(LT[a]); }
+      else M *= (double)DT[a];
+    }
+    for (size_t b = 0; b < S.L.size(); ++b)
+      if (std::find(shared.begin(), shared.end(), S.L[b]) == shared.end()) {
+        N *= (double)S.D[b];
+        nL.push_back(S.L[b]);
+        nD.push_back(S.D[b]);
+      }
+    for (size_t a = 0; a < LT.size(); ++a)
+      if (std::find(shared.begin(), shared.end(), LT[a]) == shared.end()) {
+        nL.push_back(LT[a]);
+        nD.push_back(DT[a]);
+      }
+    t += est_step_time(prec, M, K, N);
+    macs += M * K * N;
+    LT.swap(nL);
+    DT.swap(nD);
+  }
+  return {t, macs};
+}
+
+}  // namespace
+
 __global__ void c128_to_c64_kernel(const double2* __restrict__ x, float2* __restrict__ y, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -77,7 +162,7 @@ __global__ void c128_to_c64_kernel(const double2* __restrict__ x, float2* __rest
 
 int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const int* labels,
                const int* conj, const int* order, const void* const* statics, int precision,
-               gtn_map map) {
+               gtn_map map, bool allow_group, bool alloc_ws) {
   if (n < 2) return set_err(ctx, GTN_ERR_INVALID, "map needs the input and at least one static");
   if (precision < 0 || precision > 3) return set_err(ctx, GTN_ERR_INVALID, "unknown precision");
   if (is_tc(precision) && !tc_gemm_supported(ctx->cc_major, ctx->cc_minor))
@@ -138,10 +223,106 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   const bool tc = is_tc(precision);
   const int P = tc ? nplanes_of(precision) : 0;
 
-  for (int s = 1; s < n; ++s) {
-    const int j = order[s];
-    const std::vector<int>& LS = L[j];
-    const std::vector<int64_t>& DS = D[j];
+  // ---- the reference's env-first chain and the grouped chain we execute ------------------
+  ChainOp X{L[0], D[0]};
+  std::vector<ChainOp> base;
+  for (int s = 1; s < n; ++s) base.push_back(ChainOp{L[order[s]], D[order[s]]});
+  const auto ref_cost = chain_cost(X, base, precision);
+  map->flops = 8.0 * ref_cost.second;
+  const int ns = n - 1;
+  std::vector<int> best_cut(ns, 1);  // cut[i] = 1: a group ends after static i
+  double best_t = ref_cost.first;
+  if (allow_group && statics && ns >= 2 && ns <= 12) {
+    for (uint32_t mask = 0; mask < (1u << (ns - 1)); ++mask) {
+      std::vector<ChainOp> chain;
+      std::vector<ChainOp> cur;
+      bool ok = true;
+      for (int i = 0; i < ns && ok; ++i) {
+        cur.push_back(base[i]);
+        const bool cut = i == ns - 1 || ((mask >> i) & 1u);
+        if (cut) {
+          if (cur.size() > 1) {
+            if (conj && conj[order[1 + i - (int)cur.size() + 1]]) ok = false;
+            ChainOp g = group_external(cur);
+            double sz = 1;
+            for (auto d : g.D) sz *= (double)d;
+            if (sz > (double)kMaxCombined) ok = false;
+            chain.push_back(g);
+          } else {
+            chain.push_back(cur[0]);
+          }
+          cur.clear();
+        }
+      }
+      if (!ok) continue;
+      const double t = chain_cost(X, chain, precision).first;
+      if (t < 0.9 * best_t) {
+        best_t = t;
+        for (int i = 0; i < ns; ++i) best_cut[i] = (i == ns - 1 || ((mask >> i) & 1u)) ? 1 : 0;
+      }
+    }
+  }
+  // materialise the chain: single statics as given, groups pre-contracted in FP64 on device
+  struct Entry {
+    std::vector<int> L;
+    std::vector<int64_t> D;
+    const void* ptr;
+    bool conj;
+  };
+  std::vector<Entry> chain;
+  {
+    std::vector<int> members;
+    for (int i = 0; i < ns; ++i) {
+      members.push_back(order[1 + i]);
+      if (!best_cut[i]) continue;
+      if (members.size() == 1) {
+        const int j = members[0];
+        chain.push_back(Entry{L[j], D[j], statics ? statics[j] : nullptr, conj && conj[j]});
+      } else {
+        std::vector<ChainOp> ops;
+        for (int j : members) ops.push_back(ChainOp{L[j], D[j]});
+        ChainOp g = group_external(ops);
+        // sub-network: internal labels kept, external legs renumbered -1..-R
+        std::vector<int> sranks, slabels, sconj, sorder;
+        std::vector<int64_t> sdims;
+        std::vector<const void*> sptrs;
+        for (size_t q = 0; q < members.size(); ++q) {
+          const int j = members[q];
+          sranks.push_back((int)L[j].size());
+          for (size_t r = 0; r < L[j].size(); ++r) {
+            sdims.push_back(D[j][r]);
+            int l = L[j][r];
+            auto it = std::find(g.L.begin(), g.L.end(), l);
+            if (!(l > 0 && std::count(g.L.begin(), g.L.end(), l) == 0)) l = -(int)(it - g.L.begin()) - 1;
+            slabels.push_back(l);
+          }
+          sconj.push_back(conj && conj[j] ? 1 : 0);
+          sorder.push_back((int)q);
+          sptrs.push_back(statics[j]);
+        }
+        int64_t ne = 1;
+        for (auto d : g.D) ne *= d;
+        double2* buf = nullptr;
+        if (dalloc(map, &buf, (size_t)ne * sizeof(double2)) != cudaSuccess)
+          return set_err(ctx, GTN_ERR_MEMORY, "pre-contracted static allocation failed");
+        gtn_map_s sub;
+        int st = plan_build(ctx, (int)members.size(), sranks.data(), sdims.data(), slabels.data(), sconj.data(),
+                            sorder.data(), sptrs.data(), GTN_PREC_FP64, &sub, false, true);
+        if (st == GTN_OK) st = map_run(&sub, GTN_PREC_FP64, static_cast<const double2*>(sptrs[0]), buf);
+        cudaStreamSynchronize(ctx->stream);
+        map_free(&sub);
+        if (st != GTN_OK) return st;
+        chain.push_back(Entry{g.L, g.D, buf, false});
+      }
+      members.clear();
+    }
+  }
+  map->n_groups = (int)chain.size();
+
+  for (int s = 1; s <= (int)chain.size(); ++s) {
+    const int j = s - 1;
+    const std::vector<int>& LS = chain[j].L;
+    const std::vector<int64_t>& DS = chain[j].D;
     std::vector<int> sh, freeT, freeS;  // positions
     std::vector<int> shS;               // positions in S of the shared labels (T order)
     for (int a = 0; a < (int)LT.size(); ++a) {
@@ -182,16 +363,16 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
     }
 
     // ---- pack the static: B[n][k] = S[freeS(n), shared(k)] (conj applied) -------------
-    if (statics && statics[j]) {
+    if (chain[j].ptr) {
       cudaError_t e = dalloc(map, &st.b64, (size_t)st.N * st.K * sizeof(double2));
       if (e != cudaSuccess) return set_err(ctx, GTN_ERR_MEMORY, "static packing allocation failed");
       GroupSpec gn, gk;
       if (!make_group(DS, freeS, &gn) || !make_group(DS, shS, &gk))
         return set_err(ctx, GTN_ERR_UNSUPPORTED, "too many non-contiguous static leg groups");
-      e = launch_gather_c128_to_c128(static_cast<const double2*>(statics[j]), gn, gk, st.N, st.K, st.K,
+      e = launch_gather_c128_to_c128(static_cast<const double2*>(chain[j].ptr), gn, gk, st.N, st.K, st.K,
                                      st.b64, ctx->stream);
       ctx->launches++;
-      if (e == cudaSuccess && conj && conj[j]) {
+      if (e == cudaSuccess && chain[j].conj) {
         e = launch_conj_inplace(st.b64, st.N * st.K, ctx->stream);
         ctx->launches++;
       }
@@ -216,7 +397,7 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
       }
       if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("static packing: ") + cudaGetErrorString(e));
     }
-    map->flops += 8.0 * st.macs;
+    map->exec_flops += 8.0 * st.macs;
     map->steps.push_back(st);
     LT = map->steps.back().out_labels;
     DT = map->steps.back().out_dims;
@@ -245,9 +426,30 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   for (int a = 0; a < R; ++a) ident = ident && ypos[a] == a;
   map->fin_identity = ident;
 
+  // ---- an FP64 plan of its own when this plan's grouping was chosen for a mixed mode ------
+  // (the Rayleigh quotient and FP64 comparisons then run the FP64-optimal chain; both plans
+  // share the workspace below, they never run concurrently)
+  if (allow_group && precision != GTN_PREC_FP64 && statics && map->n_groups != n - 1) {
+    gtn_map alt = new (std::nothrow) gtn_map_s();
+    if (!alt) return set_err(ctx, GTN_ERR_MEMORY, "host allocation failed");
+    const int st = plan_build(ctx, n, ranks, dims, labels, conj, order, statics, GTN_PREC_FP64, alt, true, false);
+    if (st != GTN_OK) {
+      map_free(alt);
+      delete alt;
+      return st;
+    }
+    map->fp64_alt = alt;
+  }
+  if (!alloc_ws) return GTN_OK;
+
   // ---- workspace admission, then allocation ------------------------------------------
-  const size_t tbytes = (size_t)map->max_t * sizeof(double2);
-  const size_t abytes = std::max<size_t>((size_t)map->max_a * sizeof(double2),
+  int64_t max_t = map->max_t, max_a = map->max_a;
+  if (map->fp64_alt) {
+    max_t = std::max(max_t, map->fp64_alt->max_t);
+    max_a = std::max(max_a, map->fp64_alt->max_a);
+  }
+  const size_t tbytes = (size_t)max_t * sizeof(double2);
+  const size_t abytes = std::max<size_t>((size_t)max_a * sizeof(double2),
                                          (size_t)map->max_apl * sizeof(__nv_bfloat16));
   size_t freeb = 0, totalb = 0;
   cudaMemGetInfo(&freeb, &totalb);
@@ -259,12 +461,26 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   if (dalloc(map, &map->buf0, tbytes) != cudaSuccess || dalloc(map, &map->buf1, tbytes) != cudaSuccess ||
       dalloc(map, &map->abuf, std::max<size_t>(abytes, 256)) != cudaSuccess)
     return set_err(ctx, GTN_ERR_MEMORY, "map workspace allocation failed");
+  if (map->fp64_alt) {
+    map->fp64_alt->buf0 = map->buf0;
+    map->fp64_alt->buf1 = map->buf1;
+    map->fp64_alt->abuf = map->abuf;
+  }
   return GTN_OK;
 }
 
 void map_free(gtn_map map) {
+  if (map->fp64_alt) {
+    map_free(map->fp64_alt);
+    delete map->fp64_alt;
+    map->fp64_alt = nullptr;
+  }
   for (void* p : map->owned) cudaFree(p);
   map->owned.clear();
+  if (map->kv) cudaFree(map->kv);
+  map->kv = nullptr;
+  if (map->kscratch) cudaFree(map->kscratch);
+  map->kscratch = nullptr;
 }
 
 // Optional per-launch timing: CUDA events around every kernel of one application.
@@ -294,6 +510,7 @@ static void prof_end(cudaStream_t s, int kind, double flops) {
 }
 
 int map_run(gtn_map map, int precision, const double2* x, double2* y) {
+  if (precision == GTN_PREC_FP64 && map->fp64_alt) return map_run(map->fp64_alt, precision, x, y);
   gtn_ctx ctx = map->ctx;
   cudaStream_t s = ctx->stream;
   const bool tc = is_tc(precision);

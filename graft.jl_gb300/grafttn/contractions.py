@@ -248,17 +248,26 @@ class EffectiveMap:
 class EnvCache:
     """Directed-edge environments on the device (envcache.jl:61-109) with the reference's
     invalidation rule: an env is dropped when its contracted side contains a touched node
-    (envcache.jl:812-844)."""
+    (envcache.jl:812-844).  ``max_env_bytes`` bounds the cached bytes with least-recently-
+    used eviction (envcache.jl:571-594); evicted environments are recomputed on demand."""
 
-    def __init__(self, topo):
+    def __init__(self, topo, max_env_bytes=None):
+        from collections import OrderedDict
         self.topo = topo
-        self.envs = {}
+        self.envs = OrderedDict()
+        self.max_env_bytes = max_env_bytes
+        self.bytes = 0
         self.builds = 0
+        self.evictions = 0
+
+    def _drop(self, key):
+        E = self.envs.pop(key)
+        self.bytes -= E.numel() * E.element_size()
 
     def invalidate_node(self, n):
         t = self.topo
         for key in [k for k in self.envs if n in t.subtree_nodes(k[0], k[1])]:
-            del self.envs[key]
+            self._drop(key)
 
     def invalidate_edge(self, n, m):
         self.invalidate_node(n)
@@ -268,20 +277,26 @@ class EnvCache:
         """E(u->v)[ket, op, bra], built lazily after its prerequisites (envcache.jl:1440-1476)."""
         key = (u, v)
         if key in self.envs:
+            self.envs.move_to_end(key)
             return self.envs[key]
         t = self.topo
-        for w in t.neighbors(u):
-            if w != v:
-                self.env(psi, H, w, u)
+        # prerequisites stay referenced here even if the byte budget evicts them meanwhile
+        pre = {w: self.env(psi, H, w, u) for w in t.neighbors(u) if w != v}
         A, W = psi.tensors[u], H.tensors[u]
         labels, conj, envs, has_cap = env_spec(t, u, v, A.dim(), W.dim())
-        ops = [A] + [self.envs[(w, u)] for w in envs]
+        ops = [A] + [pre[w] for w in envs]
         if has_cap:
             ops.append(psi.ctx.upload(np.ones((1, 1, 1))))
         ops += [W, A]
         E = psi.ctx.contract(ops, labels, conj)
         self.envs[key] = E
+        self.bytes += E.numel() * E.element_size()
         self.builds += 1
+        if self.max_env_bytes is not None:
+            while self.bytes > self.max_env_bytes and len(self.envs) > 1:
+                old = next(iter(self.envs))
+                self._drop(old)
+                self.evictions += 1
         return E
 
 
