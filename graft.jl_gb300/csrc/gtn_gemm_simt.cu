@@ -3,6 +3,9 @@
 // The output is written m-fastest so that each warp's stores are contiguous.
 #include "gtn_internal.h"
 
+#include <algorithm>
+#include <cstring>
+
 namespace {
 
 template <typename T> struct CT;
@@ -19,16 +22,14 @@ constexpr int BM = 64, BN = 64, BK = 16;
 
 // 256 threads; thread (tx = tid % 16, ty = tid / 16) owns m = tx + 16*i, n = ty + 16*j.
 template <typename T>
-__global__ void __launch_bounds__(256) gemm_simt_kernel(const T* __restrict__ A, const T* __restrict__ B,
-                                                        T* __restrict__ C, int64_t M, int64_t N,
-                                                        int64_t K) {
+__device__ __forceinline__ void gemm_simt_tile(const T* __restrict__ A, const T* __restrict__ B,
+                                               T* __restrict__ C, int64_t M, int64_t N, int64_t K,
+                                               int64_t m0, int64_t n0) {
   using R = typename CT<T>::R;
   __shared__ T As[BK][BM + 1];
   __shared__ T Bs[BK][BN + 1];
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  const int64_t m0 = (int64_t)blockIdx.x * BM;
-  const int64_t n0 = (int64_t)blockIdx.y * BN;
   R acc_r[4][4], acc_i[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -89,6 +90,55 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const T* __restrict__ A,
 }
 
 template <typename T>
+__global__ void __launch_bounds__(256) gemm_simt_kernel(const T* __restrict__ A, const T* __restrict__ B,
+                                                        T* __restrict__ C, int64_t M, int64_t N,
+                                                        int64_t K) {
+  gemm_simt_tile<T>(A, B, C, M, N, K, (int64_t)blockIdx.x * BM, (int64_t)blockIdx.y * BN);
+}
+
+struct GemmJobsP {
+  GemmJob j[kGemmJobMax];
+  int tile_start[kGemmJobMax + 1];
+  int tiles_m[kGemmJobMax];
+  int n;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_simt_grouped_kernel(const __grid_constant__ GemmJobsP g) {
+  const int b = blockIdx.x;
+  int p = 0;
+  while (p + 1 < g.n && g.tile_start[p + 1] <= b) ++p;
+  const GemmJob& J = g.j[p];
+  const int t = b - g.tile_start[p];
+  gemm_simt_tile<T>(static_cast<const T*>(J.A), static_cast<const T*>(J.B), static_cast<T*>(J.C), J.M, J.N, J.K,
+                    (int64_t)(t % g.tiles_m[p]) * BM, (int64_t)(t / g.tiles_m[p]) * BN);
+}
+
+template <typename T>
+cudaError_t launch_grouped(const GemmJob* jobs, int njobs, cudaStream_t s) {
+  for (int base = 0; base < njobs; base += kGemmJobMax) {
+    const int cnt = std::min(kGemmJobMax, njobs - base);
+    GemmJobsP g;
+    std::memset(&g, 0, sizeof(g));
+    int tiles = 0;
+    for (int q = 0; q < cnt; ++q) {
+      const GemmJob& J = jobs[base + q];
+      g.j[q] = J;
+      g.tiles_m[q] = (int)((J.M + BM - 1) / BM);
+      g.tile_start[q] = tiles;
+      tiles += (J.M > 0 && J.N > 0) ? g.tiles_m[q] * (int)((J.N + BN - 1) / BN) : 0;
+    }
+    g.tile_start[cnt] = tiles;
+    g.n = cnt;
+    if (tiles == 0) continue;
+    gemm_simt_grouped_kernel<T><<<tiles, 256, 0, s>>>(g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
 cudaError_t launch(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, cudaStream_t s) {
   if (M <= 0 || N <= 0) return cudaSuccess;
   const int64_t gx = (M + BM - 1) / BM, gy = (N + BN - 1) / BN;
@@ -102,6 +152,9 @@ cudaError_t launch(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K
 cudaError_t launch_zgemm_simt(const double2* A, const double2* B, double2* C, int64_t M, int64_t N,
                               int64_t K, cudaStream_t s) {
   return launch(A, B, C, M, N, K, s);
+}
+cudaError_t launch_gemm_simt_grouped(const GemmJob* jobs, int njobs, int is64, cudaStream_t s) {
+  return is64 ? launch_grouped<double2>(jobs, njobs, s) : launch_grouped<float2>(jobs, njobs, s);
 }
 cudaError_t launch_cgemm_simt(const float2* A, const float2* B, float2* C, int64_t M, int64_t N,
                               int64_t K, cudaStream_t s) {

@@ -17,12 +17,17 @@
 #include "gtn_internal.h"
 #include <cuda.h>
 
+#include <algorithm>
+#include <cstring>
+
 namespace {
 
 constexpr int BM = 128;
 constexpr int BKE = 64;  // bf16 elements per k-block = 128 bytes = one SW128 row
 constexpr int A_BYTES = BM * BKE * 2;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
+
+constexpr int kTcGroupMax = 56;
 
 struct ProdList {
   int n;
@@ -134,11 +139,11 @@ template <int BN> struct Cfg {
   static constexpr uint32_t TMEM_COLS = BN < 32 ? 32 : BN;
 };
 
+// One 128 x BN output tile of C = A * B'^T (all roles of the CTA).
 template <int BN>
-__global__ void __launch_bounds__(128, 1)
-    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                   float2* __restrict__ C, int64_t M, int64_t N, int nkb, ProdList prods,
-                   int* __restrict__ errflag) {
+__device__ __forceinline__ void tc_tile(const CUtensorMap* tmA, const CUtensorMap* tmB, float2* __restrict__ C,
+                                        int64_t M, int64_t N, int nkb, const ProdList& prods, int m0, int r0,
+                                        int* __restrict__ errflag) {
   using CF = Cfg<BN>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -161,8 +166,8 @@ __global__ void __launch_bounds__(128, 1)
     n_issued = 0;
     n_consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
-    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmB)) : "memory");
   }
   if (warp == 2) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -177,8 +182,6 @@ __global__ void __launch_bounds__(128, 1)
   const uint32_t tmem_d = tmem_slot;
 
   const int total = prods.n * nkb;
-  const int m0 = blockIdx.x * BM;
-  const int r0 = blockIdx.y * BN;  // first real output column (row of B')
 
   if (warp == 0 && lane == 0) {
     int it = 0;
@@ -194,8 +197,8 @@ __global__ void __launch_bounds__(128, 1)
       const uint32_t sa = smem_u32(smem + s * CF::STAGE_BYTES);
       const uint32_t sb = sa + A_BYTES;
       mbar_expect_tx(&full_bar[s], CF::STAGE_BYTES);
-      tma_load_3d(sa, &tmA, &full_bar[s], kb * BKE, m0, prods.a[p]);
-      tma_load_3d(sb, &tmB, &full_bar[s], kb * BKE, r0, prods.b[p]);
+      tma_load_3d(sa, tmA, &full_bar[s], kb * BKE, m0, prods.a[p]);
+      tma_load_3d(sb, tmB, &full_bar[s], kb * BKE, r0, prods.b[p]);
     }
     n_issued = it;
   } else if (warp == 1 && lane == 0) {
@@ -268,6 +271,40 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
+template <int BN>
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   float2* __restrict__ C, int64_t M, int64_t N, int nkb, ProdList prods,
+                   int* __restrict__ errflag) {
+  tc_tile<BN>(&tmA, &tmB, C, M, N, nkb, prods, blockIdx.x * BM, blockIdx.y * BN, errflag);
+}
+
+// Many independent problems in one launch: CTA b works on tile b - tile_start[p] of the
+// problem p whose tile range holds b (problems listed largest K first).
+struct GroupedTc {
+  CUtensorMap tmA[kTcGroupMax];
+  CUtensorMap tmB[kTcGroupMax];
+  float2* C[kTcGroupMax];
+  int64_t M[kTcGroupMax];
+  int64_t N[kTcGroupMax];
+  int nkb[kTcGroupMax];
+  int tiles_m[kTcGroupMax];
+  int tile_start[kTcGroupMax + 1];
+  int nprob;
+  ProdList prods;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(128, 1) tc_gemm_grouped_kernel(const __grid_constant__ GroupedTc g,
+                                                                 int* __restrict__ errflag) {
+  const int b = blockIdx.x;
+  int p = 0;
+  while (p + 1 < g.nprob && g.tile_start[p + 1] <= b) ++p;
+  const int t = b - g.tile_start[p];
+  const int tm = t % g.tiles_m[p], tn = t / g.tiles_m[p];
+  tc_tile<BN>(&g.tmA[p], &g.tmB[p], g.C[p], g.M[p], g.N[p], g.nkb[p], g.prods, tm * BM, tn * BN, errflag);
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
@@ -338,7 +375,71 @@ cudaError_t launch_bn(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::st
   return cudaGetLastError();
 }
 
+template <int BN>
+cudaError_t launch_grouped_bn(const TcGemmArgs* probs, int nprob, int* errflag, cudaStream_t s, std::string* why) {
+  using CF = Cfg<BN>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_grouped_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         CF::SMEM);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  for (int base = 0; base < nprob; base += kTcGroupMax) {
+    const int cnt = std::min(kTcGroupMax, nprob - base);
+    GroupedTc g;
+    std::memset(&g, 0, sizeof(g));
+    int tiles = 0;
+    for (int q = 0; q < cnt; ++q) {
+      const TcGemmArgs& a = probs[base + q];
+      if (!make_map(&g.tmA[q], a.A, a.Kp, a.M, a.a_planes, BM, why)) return cudaErrorInvalidValue;
+      if (!make_map(&g.tmB[q], a.B, a.Kp, 2 * a.N, a.b_planes, BN, why)) return cudaErrorInvalidValue;
+      g.C[q] = a.C;
+      g.M[q] = a.M;
+      g.N[q] = a.N;
+      g.nkb[q] = (int)((2 * a.Kp + BKE - 1) / BKE);
+      g.tiles_m[q] = (int)((a.M + BM - 1) / BM);
+      g.tile_start[q] = tiles;
+      tiles += g.tiles_m[q] * (int)((2 * a.N + BN - 1) / BN);
+    }
+    g.tile_start[cnt] = tiles;
+    g.nprob = cnt;
+    g.prods.n = probs[base].nprod;
+    for (int i = 0; i < 9; ++i) {
+      g.prods.a[i] = i < probs[base].nprod ? probs[base].prod_a[i] : 0;
+      g.prods.b[i] = i < probs[base].nprod ? probs[base].prod_b[i] : 0;
+    }
+    if (tiles == 0) continue;
+    tc_gemm_grouped_kernel<BN><<<tiles, 128, CF::SMEM, s>>>(g, errflag);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 }  // namespace
+
+cudaError_t launch_tc_gemm_grouped(const TcGemmArgs* probs, int nprob, int* errflag, cudaStream_t s,
+                                   std::string* why) {
+  int64_t maxn2 = 0;
+  for (int q = 0; q < nprob; ++q) {
+    const TcGemmArgs& a = probs[q];
+    if (a.Kp % 32 != 0 || a.nprod != probs[0].nprod || a.M <= 0 || a.N <= 0) {
+      if (why) *why = "tc_gemm_grouped: Kp multiple of 32, same product list, non-empty problems";
+      return cudaErrorInvalidValue;
+    }
+    if (reinterpret_cast<uintptr_t>(a.A) % 16 || reinterpret_cast<uintptr_t>(a.B) % 16) {
+      if (why) *why = "tc_gemm_grouped: operand planes must be 16-byte aligned";
+      return cudaErrorInvalidValue;
+    }
+    maxn2 = std::max(maxn2, 2 * a.N);
+  }
+  if (nprob == 0) return cudaSuccess;
+  if (maxn2 <= 32) return launch_grouped_bn<32>(probs, nprob, errflag, s, why);
+  if (maxn2 <= 64) return launch_grouped_bn<64>(probs, nprob, errflag, s, why);
+  if (maxn2 <= 128) return launch_grouped_bn<128>(probs, nprob, errflag, s, why);
+  return launch_grouped_bn<256>(probs, nprob, errflag, s, why);
+}
 
 bool tc_gemm_supported(int cc_major, int cc_minor) {
   (void)cc_minor;

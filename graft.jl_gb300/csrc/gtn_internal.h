@@ -79,6 +79,28 @@ cudaError_t launch_split_c64(const float2* T, const GroupSpec& mg, const GroupSp
 cudaError_t launch_pack_b_planes(const double2* B, int64_t N, int64_t K, int64_t Kp, int nplanes,
                                  int64_t pstride, __nv_bfloat16* out, cudaStream_t s);
 
+// Grouped variants: independent jobs in one launch (per 48 jobs).
+constexpr int kGatherJobMax = 48;
+struct GatherJob {
+  const void* T;
+  GroupSpec mg, kg;
+  int64_t M, K, Kw;
+  void* out;
+  int64_t ld;        // complex output: row pitch
+  int64_t pstride;   // split output: plane pitch (bf16 elements)
+  int nplanes;       // 0: complex output, 2 or 3: bf16 slice planes (row pitch 2*Kw)
+};
+struct SmallJob {
+  const void* A;
+  GroupSpec mg, kg;
+  int64_t M;
+  int K, N;
+  const void* B;
+  void* C;
+};
+cudaError_t launch_gather_grouped(const GatherJob* jobs, int njobs, int in_is64, int out_is64, cudaStream_t s);
+cudaError_t launch_small_grouped(const SmallJob* jobs, int njobs, int is64, cudaStream_t s);
+
 // C[n][m] = sum_k T[offM(m) + offK(k)] * B[n][k]   (small K; B in shared memory)
 cudaError_t launch_small_contract_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg,
                                        int64_t M, int K, int N, const double2* B, double2* C,
@@ -94,6 +116,15 @@ cudaError_t launch_zgemm_simt(const double2* A, const double2* B, double2* C, in
 cudaError_t launch_cgemm_simt(const float2* A, const float2* B, float2* C, int64_t M, int64_t N,
                               int64_t K, cudaStream_t s);
 
+constexpr int kGemmJobMax = 64;
+struct GemmJob {
+  const void* A;
+  const void* B;
+  void* C;
+  int64_t M, N, K;
+};
+cudaError_t launch_gemm_simt_grouped(const GemmJob* jobs, int njobs, int is64, cudaStream_t s);
+
 // ---- tcgen05 GEMM (gtn_gemm_tc.cu) ---------------------------------------------------
 // Real GEMM on bf16 slice planes: C (complex fp32, [N][M]) from A planes [P][M][2Kp] and
 // B planes [P][2N][2Kp].  prods lists (a_plane, b_plane) pairs accumulated in order.
@@ -108,6 +139,9 @@ struct TcGemmArgs {
 };
 cudaError_t launch_tc_gemm(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why);
 bool tc_gemm_supported(int cc_major, int cc_minor);
+// Independent problems in one launch per 56 problems (same product list for all).
+cudaError_t launch_tc_gemm_grouped(const TcGemmArgs* probs, int nprob, int* errflag, cudaStream_t s,
+                                   std::string* why);
 
 // ---- vector kernels (gtn_blas.cu) --------------------------------------------------
 cudaError_t launch_multidot(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
@@ -178,3 +212,4 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y);
 int map_run_profiled(gtn_map map, int precision, const double2* x, double2* y, int cap, double* ms,
                      int* kind, double* flops, int* count);
 void map_free(gtn_map map);
+int map_run_batched(gtn_map* maps, int n, int precision, const double2* const* xs, double2* const* ys);

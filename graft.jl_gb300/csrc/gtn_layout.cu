@@ -4,6 +4,9 @@
 // side are coalesced.
 #include "gtn_internal.h"
 
+#include <algorithm>
+#include <cstring>
+
 namespace {
 
 __device__ __forceinline__ int64_t decompose(int64_t i, const GroupSpec& g) {
@@ -75,14 +78,12 @@ struct SplitWriter {
 // Tile gather: rows m (M), columns k (K valid, Kw written).  m_fast selects whether the
 // load phase maps lanes to m (the running tensor's unit-stride leg is in M) or to k.
 template <typename Tin, class Writer>
-__global__ void __launch_bounds__(256) gather_tile_kernel(const Tin* __restrict__ T, GroupSpec mg,
-                                                          GroupSpec kg, int64_t M, int64_t K,
-                                                          int64_t Kw, int m_fast, Writer w) {
+__device__ __forceinline__ void gather_tile(const Tin* __restrict__ T, const GroupSpec& mg, const GroupSpec& kg,
+                                            int64_t M, int64_t K, int64_t Kw, int m_fast, const Writer& w,
+                                            int64_t m0, int64_t k0) {
   __shared__ int64_t offM[32];
   __shared__ int64_t offK[32];
   __shared__ Tin tile[32][33];
-  const int64_t m0 = (int64_t)blockIdx.x * 32;
-  const int64_t k0 = (int64_t)blockIdx.y * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
   if (ty == 0) {
     const int64_t m = m0 + tx;
@@ -103,6 +104,13 @@ __global__ void __launch_bounds__(256) gather_tile_kernel(const Tin* __restrict_
     const int64_t m = m0 + r, k = k0 + tx;
     if (m < M && k < Kw) w(m, k, tile[r][tx]);
   }
+}
+
+template <typename Tin, class Writer>
+__global__ void __launch_bounds__(256) gather_tile_kernel(const Tin* __restrict__ T, GroupSpec mg,
+                                                          GroupSpec kg, int64_t M, int64_t K,
+                                                          int64_t Kw, int m_fast, Writer w) {
+  gather_tile<Tin, Writer>(T, mg, kg, M, K, Kw, m_fast, w, (int64_t)blockIdx.x * 32, (int64_t)blockIdx.y * 32);
 }
 
 inline bool choose_m_fast(const GroupSpec& mg, const GroupSpec& kg) {
@@ -168,18 +176,17 @@ constexpr int kSmallSmemBytes = 48 * 1024;
 
 // C[n][m] = sum_k T[offM(m) + offK(k)] * B[n][k]; B and the K offsets live in shared memory.
 template <typename T, int NB>
-__global__ void __launch_bounds__(256) small_contract_kernel(const T* __restrict__ A, GroupSpec mg,
-                                                             GroupSpec kg, int64_t M, int K, int N,
-                                                             const T* __restrict__ B,
-                                                             T* __restrict__ C) {
+__device__ __forceinline__ void small_contract_body(const T* __restrict__ A, const GroupSpec& mg,
+                                                    const GroupSpec& kg, int64_t M, int K, int N,
+                                                    const T* __restrict__ B, T* __restrict__ C, int64_t blk,
+                                                    int64_t nblk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int64_t* offK = reinterpret_cast<int64_t*>(smem_raw);
   T* Bs = reinterpret_cast<T*>(smem_raw + ((K * sizeof(int64_t) + 15) / 16) * 16);
   for (int i = threadIdx.x; i < K; i += blockDim.x) offK[i] = decompose(i, kg);
   for (int i = threadIdx.x; i < N * K; i += blockDim.x) Bs[i] = B[i];
   __syncthreads();
-  for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < M;
-       m += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t m = blk * blockDim.x + threadIdx.x; m < M; m += nblk * blockDim.x) {
     const int64_t om = decompose(m, mg);
     for (int n0 = 0; n0 < N; n0 += NB) {
       T acc[NB];
@@ -198,6 +205,14 @@ __global__ void __launch_bounds__(256) small_contract_kernel(const T* __restrict
   }
 }
 
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) small_contract_kernel(const T* __restrict__ A, GroupSpec mg,
+                                                             GroupSpec kg, int64_t M, int K, int N,
+                                                             const T* __restrict__ B,
+                                                             T* __restrict__ C) {
+  small_contract_body<T, NB>(A, mg, kg, M, K, N, B, C, blockIdx.x, gridDim.x);
+}
+
 template <typename T>
 cudaError_t launch_small(const T* A, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int K,
                          int N, const T* B, T* C, cudaStream_t s) {
@@ -210,7 +225,119 @@ cudaError_t launch_small(const T* A, const GroupSpec& mg, const GroupSpec& kg, i
   return cudaGetLastError();
 }
 
+// ---- grouped (multi-problem) variants: one launch for many independent jobs -------------
+
+struct GatherJobsP {
+  GatherJob j[kGatherJobMax];
+  int tile_start[kGatherJobMax + 1];
+  int tiles_m[kGatherJobMax];
+  int m_fast[kGatherJobMax];
+  int n;
+};
+
+__device__ __forceinline__ int find_job(const int* start, int n, int b) {
+  int p = 0;
+  while (p + 1 < n && start[p + 1] <= b) ++p;
+  return p;
+}
+
+template <typename Tin, typename Tout>
+__global__ void __launch_bounds__(256) gather_grouped_kernel(const __grid_constant__ GatherJobsP g) {
+  const int b = blockIdx.x;
+  const int p = find_job(g.tile_start, g.n, b);
+  const GatherJob& J = g.j[p];
+  const int t = b - g.tile_start[p];
+  const int64_t m0 = (int64_t)(t % g.tiles_m[p]) * 32, k0 = (int64_t)(t / g.tiles_m[p]) * 32;
+  if (J.nplanes > 0) {
+    SplitWriter w{static_cast<__nv_bfloat16*>(J.out), 2 * J.Kw, J.pstride, J.nplanes};
+    gather_tile<Tin, SplitWriter>(static_cast<const Tin*>(J.T), J.mg, J.kg, J.M, J.K, J.Kw, g.m_fast[p], w, m0, k0);
+  } else {
+    ComplexWriter<Tout> w{static_cast<Tout*>(J.out), J.ld};
+    gather_tile<Tin, ComplexWriter<Tout>>(static_cast<const Tin*>(J.T), J.mg, J.kg, J.M, J.K, J.Kw, g.m_fast[p], w,
+                                          m0, k0);
+  }
+}
+
+struct SmallJobsP {
+  SmallJob j[kGatherJobMax];
+  int blk_start[kGatherJobMax + 1];
+  int n;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) small_grouped_kernel(const __grid_constant__ SmallJobsP g) {
+  const int b = blockIdx.x;
+  const int p = find_job(g.blk_start, g.n, b);
+  const SmallJob& J = g.j[p];
+  small_contract_body<T, 8>(static_cast<const T*>(J.A), J.mg, J.kg, J.M, J.K, J.N, static_cast<const T*>(J.B),
+                            static_cast<T*>(J.C), b - g.blk_start[p], g.blk_start[p + 1] - g.blk_start[p]);
+}
+
 }  // namespace
+
+template <typename Tin, typename Tout>
+static cudaError_t launch_gather_grouped_t(const GatherJob* jobs, int njobs, cudaStream_t s) {
+  for (int base = 0; base < njobs; base += kGatherJobMax) {
+    const int cnt = std::min(kGatherJobMax, njobs - base);
+    GatherJobsP g;
+    std::memset(&g, 0, sizeof(g));
+    int tiles = 0;
+    for (int q = 0; q < cnt; ++q) {
+      const GatherJob& J = jobs[base + q];
+      g.j[q] = J;
+      g.tiles_m[q] = (int)((J.M + 31) / 32);
+      g.m_fast[q] = choose_m_fast(J.mg, J.kg) ? 1 : 0;
+      g.tile_start[q] = tiles;
+      tiles += (J.M > 0 && J.Kw > 0) ? g.tiles_m[q] * (int)((J.Kw + 31) / 32) : 0;
+    }
+    g.tile_start[cnt] = tiles;
+    g.n = cnt;
+    if (tiles == 0) continue;
+    gather_grouped_kernel<Tin, Tout><<<tiles, dim3(32, 8), 0, s>>>(g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_gather_grouped(const GatherJob* jobs, int njobs, int in_is64, int out_is64, cudaStream_t s) {
+  if (in_is64 && out_is64) return launch_gather_grouped_t<double2, double2>(jobs, njobs, s);
+  if (in_is64) return launch_gather_grouped_t<double2, float2>(jobs, njobs, s);
+  if (out_is64) return launch_gather_grouped_t<float2, double2>(jobs, njobs, s);
+  return launch_gather_grouped_t<float2, float2>(jobs, njobs, s);
+}
+
+template <typename T>
+static cudaError_t launch_small_grouped_t(const SmallJob* jobs, int njobs, cudaStream_t s) {
+  for (int base = 0; base < njobs; base += kGatherJobMax) {
+    const int cnt = std::min(kGatherJobMax, njobs - base);
+    SmallJobsP g;
+    std::memset(&g, 0, sizeof(g));
+    int blocks = 0;
+    size_t smem = 0;
+    for (int q = 0; q < cnt; ++q) {
+      const SmallJob& J = jobs[base + q];
+      g.j[q] = J;
+      g.blk_start[q] = blocks;
+      int64_t nb = (J.M + 255) / 256;
+      if (nb > 512) nb = 512;
+      blocks += (int)nb;
+      smem = std::max(smem, ((J.K * sizeof(int64_t) + 15) / 16) * 16 + (size_t)J.N * J.K * sizeof(T));
+    }
+    g.blk_start[cnt] = blocks;
+    g.n = cnt;
+    if (blocks == 0) continue;
+    if (smem > (size_t)kSmallSmemBytes) return cudaErrorInvalidValue;
+    small_grouped_kernel<T><<<blocks, 256, smem, s>>>(g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_small_grouped(const SmallJob* jobs, int njobs, int is64, cudaStream_t s) {
+  return is64 ? launch_small_grouped_t<double2>(jobs, njobs, s) : launch_small_grouped_t<float2>(jobs, njobs, s);
+}
 
 bool small_contract_fits(int K, int N, size_t elem_bytes) {
   return ((K * sizeof(int64_t) + 15) / 16) * 16 + (size_t)N * K * elem_bytes <= (size_t)kSmallSmemBytes;

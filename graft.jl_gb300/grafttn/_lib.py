@@ -51,6 +51,10 @@ SIGNATURES = {
     "gtn_map_apply_host": (_i, [_p, _p, _p]),
     "gtn_map_apply_profiled": (_i, [_p, _i, _p, _p, _i, _pd, _pi, _pd, _pi]),
     "gtn_map_info": (_i, [_p, _pi64, _pi64, _pd, _pi, _pi64]),
+    "gtn_map_apply_batched": (_i, [_i, C.POINTER(_p), C.POINTER(_p), C.POINTER(_p), _i]),
+    "gtn_batch_create": (_i, [_i, C.POINTER(_p), C.POINTER(_p), C.POINTER(_p), _i, _i, C.POINTER(_p)]),
+    "gtn_batch_run": (_i, [_p]),
+    "gtn_batch_destroy": (_i, [_p]),
     "gtn_map_out_shape": (_i, [_p, _pi, _pi64]),
     "gtn_contract": (_i, [_p, _i, _pi, _pi64, _pi, _pi, _pi, C.POINTER(_p), _p, _i]),
     "gtn_permute": (_i, [_p, _i, _pi64, _pi, _p, _p]),

@@ -245,6 +245,47 @@ class EffectiveMap:
         return x, dict(substeps=info[0], matvecs=info[1])
 
 
+def apply_batched(maps, xs, ys=None, precision=None):
+    """y_i = H_i x_i for independent maps in grouped launches (one per step and kernel kind)."""
+    ctx = maps[0].ctx
+    prec = maps[0].precision if precision is None else precision
+    ys = ys if ys is not None else [ctx.empty(m.y_shape) for m in maps]
+    n = len(maps)
+    check(ctx.lib.gtn_map_apply_batched(n, ptr_array([m.h.value for m in maps]), ptr_array([x.data_ptr() for x in xs]),
+                                        ptr_array([y.data_ptr() for y in ys]), prec), ctx.h, "map_apply_batched")
+    return ys
+
+
+class MapBatch:
+    """A fixed batch of maps and buffers, optionally replayed as one CUDA graph."""
+
+    def __init__(self, maps, xs, ys, precision=None, graph=True):
+        self.ctx = maps[0].ctx
+        self.maps, self.xs, self.ys = list(maps), list(xs), list(ys)
+        prec = maps[0].precision if precision is None else precision
+        h = C.c_void_p()
+        n = len(maps)
+        check(self.ctx.lib.gtn_batch_create(n, ptr_array([m.h.value for m in maps]), ptr_array([x.data_ptr() for x in xs]),
+                                            ptr_array([y.data_ptr() for y in ys]), prec, 1 if graph else 0, C.byref(h)),
+              self.ctx.h, "batch_create")
+        self.h = h
+
+    def run(self):
+        check(self.ctx.lib.gtn_batch_run(self.h), self.ctx.h, "batch_run")
+        return self.ys
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gtn_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class EnvCache:
     """Directed-edge environments on the device (envcache.jl:61-109) with the reference's
     invalidation rule: an env is dropped when its contracted side contains a touched node

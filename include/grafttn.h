@@ -108,6 +108,21 @@ int gtn_map_apply_profiled(gtn_map map, int precision, const void* x, void* y, i
 /* Output leg dims of the map (rank written to *rank, dims to dims[0..rank-1]). */
 int gtn_map_out_shape(gtn_map map, int* rank, int64_t* dims);
 
+/* ---- batches of independent maps --------------------------------------------------
+ * Replaces the reference's threaded fan-out of many small maps (channel slices,
+ * lib/GraftContractions/src/Contractions/effective.jl:26-30,153-165; sibling environment
+ * staging, envcache.jl:1164-1304): step s of every map runs in one grouped launch per kernel
+ * kind.  All maps must belong to one context; xs/ys are device c128 buffers per map. */
+typedef struct gtn_batch_s* gtn_batch;
+int gtn_map_apply_batched(int n, const gtn_map* maps, const void* const* xs, void* const* ys,
+                          int precision);
+/* A fixed batch (maps and buffers); with use_graph != 0 the second gtn_batch_run captures
+ * the whole batched application into a CUDA graph and later runs replay it. */
+int gtn_batch_create(int n, const gtn_map* maps, const void* const* xs, void* const* ys,
+                     int precision, int use_graph, gtn_batch* out);
+int gtn_batch_run(gtn_batch batch);
+int gtn_batch_destroy(gtn_batch batch);
+
 /* One-shot contraction of a label graph where every operand is given (environment
  * builds, envcache.jl:1010-1101; two-site merge, effective.jl:827-843).  Operand 0 starts
  * the chain; out receives the tensor with legs ordered -1, -2, ... (c128). */
