@@ -119,6 +119,7 @@ int map_run_batched(gtn_map* maps_in, int n, int precision, const double2* const
       G.out = m->abuf;
       if (tc) {
         G.Kw = st.Kp;
+        G.ld = st.Kp;
         G.nplanes = P;
         G.pstride = st.M * 2 * st.Kp;
         TcGemmArgs a;

@@ -99,6 +99,22 @@ struct SmallJob {
   void* C;
 };
 cudaError_t launch_gather_grouped(const GatherJob* jobs, int njobs, int in_is64, int out_is64, cudaStream_t s);
+// Device-resident gather jobs (block-sparse maps): buffers resolved per launch.
+struct BlockBases {
+  void* buf[6];  // 0 x, 1 y, 2/3 running buffers, 4 staging, 5 unused
+};
+struct DevGatherJob {
+  GroupSpec mg, kg;
+  int64_t src_off, dst_off;
+  int64_t M, K, Kw, ld, pstride;
+  int src_buf, dst_buf;
+  int nplanes;   // > 0: bf16 slice planes (row pitch 2*ld), else complex
+  int dst_is64;  // complex output element type
+  int tiles_m, m_fast;
+};
+void finish_dev_gather_job(DevGatherJob* J);
+cudaError_t launch_block_gather(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
+                                const BlockBases& bases, int src_is64, cudaStream_t s);
 cudaError_t launch_small_grouped(const SmallJob* jobs, int njobs, int is64, cudaStream_t s);
 
 // C[n][m] = sum_k T[offM(m) + offK(k)] * B[n][k]   (small K; B in shared memory)

@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(256) gather_grouped_kernel(const __grid_consta
   const int t = b - g.tile_start[p];
   const int64_t m0 = (int64_t)(t % g.tiles_m[p]) * 32, k0 = (int64_t)(t / g.tiles_m[p]) * 32;
   if (J.nplanes > 0) {
-    SplitWriter w{static_cast<__nv_bfloat16*>(J.out), 2 * J.Kw, J.pstride, J.nplanes};
+    SplitWriter w{static_cast<__nv_bfloat16*>(J.out), 2 * (J.ld > 0 ? J.ld : J.Kw), J.pstride, J.nplanes};
     gather_tile<Tin, SplitWriter>(static_cast<const Tin*>(J.T), J.mg, J.kg, J.M, J.K, J.Kw, g.m_fast[p], w, m0, k0);
   } else {
     ComplexWriter<Tout> w{static_cast<Tout*>(J.out), J.ld};
@@ -273,7 +273,51 @@ __global__ void __launch_bounds__(256) small_grouped_kernel(const __grid_constan
                             static_cast<T*>(J.C), b - g.blk_start[p], g.blk_start[p + 1] - g.blk_start[p]);
 }
 
+// Device-resident job table (block-sparse maps): any number of jobs in one launch; sources
+// and destinations are (buffer id, element offset) resolved against the launch's bases.
+template <typename Tin, typename Tout>
+__global__ void __launch_bounds__(256) block_gather_kernel(const DevGatherJob* __restrict__ jobs,
+                                                           const int* __restrict__ tile_start, int njobs,
+                                                           BlockBases bases) {
+  const int b = blockIdx.x;
+  int lo = 0, hi = njobs - 1;  // last job with tile_start <= b
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tile_start[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  const DevGatherJob& J = jobs[lo];
+  const int t = b - tile_start[lo];
+  const int64_t m0 = (int64_t)(t % J.tiles_m) * 32, k0 = (int64_t)(t / J.tiles_m) * 32;
+  const Tin* src = static_cast<const Tin*>(bases.buf[J.src_buf]) + J.src_off;
+  if (J.nplanes > 0) {
+    SplitWriter w{static_cast<__nv_bfloat16*>(bases.buf[J.dst_buf]) + J.dst_off, 2 * J.ld, J.pstride, J.nplanes};
+    gather_tile<Tin, SplitWriter>(src, J.mg, J.kg, J.M, J.K, J.Kw, J.m_fast, w, m0, k0);
+  } else if (J.dst_is64) {
+    ComplexWriter<double2> w{static_cast<double2*>(bases.buf[J.dst_buf]) + J.dst_off, J.ld};
+    gather_tile<Tin, ComplexWriter<double2>>(src, J.mg, J.kg, J.M, J.K, J.Kw, J.m_fast, w, m0, k0);
+  } else {
+    ComplexWriter<float2> w{static_cast<float2*>(bases.buf[J.dst_buf]) + J.dst_off, J.ld};
+    gather_tile<Tin, ComplexWriter<float2>>(src, J.mg, J.kg, J.M, J.K, J.Kw, J.m_fast, w, m0, k0);
+  }
+  (void)sizeof(Tout);
+}
+
 }  // namespace
+
+void finish_dev_gather_job(DevGatherJob* J) {
+  J->tiles_m = (int)((J->M + 31) / 32);
+  J->m_fast = choose_m_fast(J->mg, J->kg) ? 1 : 0;
+}
+
+cudaError_t launch_block_gather(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
+                                const BlockBases& bases, int src_is64, cudaStream_t s) {
+  if (ntiles <= 0) return cudaSuccess;
+  if (src_is64)
+    block_gather_kernel<double2, double2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+  else
+    block_gather_kernel<float2, float2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+  return cudaGetLastError();
+}
 
 template <typename Tin, typename Tout>
 static cudaError_t launch_gather_grouped_t(const GatherJob* jobs, int njobs, cudaStream_t s) {

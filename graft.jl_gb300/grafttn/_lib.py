@@ -56,6 +56,12 @@ SIGNATURES = {
     "gtn_batch_run": (_i, [_p]),
     "gtn_batch_destroy": (_i, [_p]),
     "gtn_map_out_shape": (_i, [_p, _pi, _pi64]),
+    "gtn_blockmap_create": (_i, [_p, _i, _pi, _pi, _p, _p, _i, _p, _i, C.POINTER(_p), _pi64, _pi64, _i, _d,
+                                 C.POINTER(_p)]),
+    "gtn_blockmap_apply": (_i, [_p, _p, _p]),
+    "gtn_blockmap_set_graph": (_i, [_p, _i]),
+    "gtn_blockmap_info": (_i, [_p, _pd, _pi, _pi64]),
+    "gtn_blockmap_destroy": (_i, [_p]),
     "gtn_contract": (_i, [_p, _i, _pi, _pi64, _pi, _pi, _pi, C.POINTER(_p), _p, _i]),
     "gtn_permute": (_i, [_p, _i, _pi64, _pi, _p, _p]),
     "gtn_lanczos_min": (_i, [_p, _p, _i, _d, _i, _i, _pd, _pi, _pd]),
@@ -146,3 +152,16 @@ def i64_array(vals):
 def ptr_array(vals):
     vals = list(vals)
     return (C.c_void_p * max(len(vals), 1))(*[C.c_void_p(v) if v else None for v in vals])
+
+
+class BlockGather(C.Structure):
+    _fields_ = [("src_buf", C.c_int32), ("dst_index", C.c_int32), ("ng_m", C.c_int32), ("ng_k", C.c_int32),
+                ("src_off", C.c_int64), ("row_off", C.c_int64), ("col_off", C.c_int64),
+                ("M", C.c_int64), ("K", C.c_int64), ("Kw", C.c_int64), ("ld", C.c_int64),
+                ("m_dim", C.c_int64 * 8), ("m_str", C.c_int64 * 8), ("k_dim", C.c_int64 * 8),
+                ("k_str", C.c_int64 * 8)]
+
+
+class BlockGemm(C.Structure):
+    _fields_ = [("b_index", C.c_int32), ("c_buf", C.c_int32), ("c_off", C.c_int64), ("M", C.c_int64),
+                ("N", C.c_int64), ("K", C.c_int64)]

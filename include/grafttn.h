@@ -123,6 +123,48 @@ int gtn_batch_create(int n, const gtn_map* maps, const void* const* xs, void* co
 int gtn_batch_run(gtn_batch batch);
 int gtn_batch_destroy(gtn_batch batch);
 
+/* ---- abelian (U(1)) block-sparse maps ----------------------------------------------
+ * Replaces TensorKit's per-coupled-charge block GEMMs behind contract_pair for abelian
+ * unique-fusion sectors (cost model lib/GraftFoundation/src/Backend/Backend.jl:243-261,
+ * 309-368).  A host planner describes every step as GEMM problems (one per coupled charge q:
+ * C_q[N][M] = A_q[M][K] * B_q[N][K]^T, B_q a static) and block gathers that assemble A_q
+ * from the blocks of the running tensor; the library runs a step as one grouped gather and
+ * one grouped GEMM launch.  Buffers: 0 = input x (c128), 1 = output y (c128), 2 and 3 =
+ * running buffers (c128 in FP64 mode, c64 otherwise). */
+typedef struct {
+  int32_t src_buf;     /* 0 = x, 2 or 3 = running buffer */
+  int32_t dst_index;   /* step gathers: GEMM problem whose A_q is filled; final gathers: unused */
+  int32_t ng_m, ng_k;  /* number of row / column index groups */
+  int64_t src_off;     /* block offset in the source buffer (complex elements) */
+  int64_t row_off;     /* step: first row in A_q; final: element offset of the block in y */
+  int64_t col_off;     /* step: first column in A_q */
+  int64_t M, K, Kw;    /* rows, source columns, written columns (zero beyond K) */
+  int64_t ld;          /* final: row pitch of the block in y */
+  int64_t m_dim[8], m_str[8], k_dim[8], k_str[8];
+} gtn_block_gather;
+typedef struct {
+  int32_t b_index;     /* static B_q [N][K] */
+  int32_t c_buf;       /* 2 or 3 */
+  int64_t c_off;       /* C_q offset in that buffer (complex elements) */
+  int64_t M, N, K;
+} gtn_block_gemm;
+typedef struct gtn_blockmap_s* gtn_blockmap;
+/* statics: nstatics device c128 matrices (copied), static_nk: their (N, K);
+ * buffer_elems: complex elements of (x, y, running buffer 2, running buffer 3);
+ * flops: algorithmic FLOPs per application (recorded for reporting). */
+int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const int* step_ngemm,
+                        const gtn_block_gather* gathers, const gtn_block_gemm* gemms, int nfinal,
+                        const gtn_block_gather* final_gathers, int nstatics,
+                        const void* const* statics, const int64_t* static_nk,
+                        const int64_t* buffer_elems, int precision, double flops,
+                        gtn_blockmap* out);
+int gtn_blockmap_apply(gtn_blockmap map, const void* x, void* y);
+/* With use_graph != 0 an application on new (x, y) runs eagerly and is captured into a CUDA
+ * graph; later applications on the same (x, y) replay the graph. */
+int gtn_blockmap_set_graph(gtn_blockmap map, int use_graph);
+int gtn_blockmap_info(gtn_blockmap map, double* flops, int* n_problems, int64_t* bytes);
+int gtn_blockmap_destroy(gtn_blockmap map);
+
 /* One-shot contraction of a label graph where every operand is given (environment
  * builds, envcache.jl:1010-1101; two-site merge, effective.jl:827-843).  Operand 0 starts
  * the chain; out receives the tensor with legs ordered -1, -2, ... (c128). */
