@@ -239,6 +239,91 @@ def profile_traffic(kernel, workload):
     return None
 
 
+def _timed(stream, fn, reps):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def bench_u1(ctx, steps):
+    """U(1) Sz-conserving Heisenberg, block-sparse: eff_h2 on the same bin63 depth3->depth2
+    edge at total bond dimension 1024 (bond sectors: subtree charge counts, dims binomial
+    scaled to the bond dimension and clipped to [4, 256]); all coupled-charge blocks of a
+    step in one grouped launch, the application replayed as one CUDA graph."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from u1_cases import h2_u1_case
+    from grafttn import blocksparse as B
+    from oracle import u1_oracle as U
+    xs, labels, order, statics, x = h2_u1_case(5, "n3_1", 1024)
+    plan = B.BlockPlan(xs, labels[0], statics, order)
+    dx = ctx.upload(x)
+    out = {"theta_blocks": len(xs.blocks), "theta_elems": xs.size, "algorithmic_flops_per_apply": plan.flops}
+    for prec in ("bf16x6", "fp64"):
+        bm = B.BlockEffectiveMap(ctx, plan, prec, graph=True)
+        dy = ctx.empty((plan.y.size,))
+        for _ in range(3):
+            bm.apply_into(dx, dy)
+        ctx.sync()
+        l0 = ctx.launches
+        reps = steps if prec != "fp64" else max(2, steps // 4)
+        ms = _timed(ctx.stream, lambda: bm.apply_into(dx, dy), reps)
+        out[prec] = {"applies_per_s": 1000.0 / ms, "ms_per_apply": ms, "tflops": plan.flops / ms / 1e9,
+                     "launches_per_apply": (ctx.launches - l0) / reps}
+        if prec == "bf16x6":
+            y_mixed = ctx.download(dy)
+        else:
+            y64 = ctx.download(dy)
+        out["coupled_charge_problems"] = bm.n_problems
+        bm.close()
+    out["mixed_vs_fp64_rel_err"] = float(np.linalg.norm(y_mixed - y64) / np.linalg.norm(y64))
+    out["speedup_mixed_vs_fp64"] = out["bf16x6"]["applies_per_s"] / out["fp64"]["applies_per_s"]
+    blocks = [U.blocks_from_flat(xs, x)] + [U.blocks_from_flat(T, d) for T, _, d in statics]
+    t0 = time.perf_counter()
+    y_cpu = U.flat_from_blocks(plan.y, U.ncon_blocks(blocks, labels, order))
+    el = time.perf_counter() - t0
+    out["cpu_baseline"] = {"applies_per_s": 1.0 / el, "kind": "port (per-sector block tensordot, numpy)",
+                           "cores": blas_threads(), "sample": "1 application"}
+    out["fp64_vs_cpu_rel_err"] = float(np.linalg.norm(y64 - y_cpu) / np.linalg.norm(y_cpu))
+    return out
+
+
+def bench_batched(ctx, steps):
+    """64 independent eff_h1 maps with uneven bond dimensions in [16, 256] (chain nodes with
+    two bonds, tree nodes with three bonds <= 48): grouped launches per step replayed as one
+    CUDA graph, against 64 sequential single-map applications."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from test_gpu_batched import make_batch
+    from grafttn.contractions import MapBatch
+    rng = np.random.default_rng(64)
+    maps, xs, refs = make_batch(ctx, rng, 64, 16, 256, "bf16x6")
+    ys = [ctx.empty(m.y_shape) for m in maps]
+    b = MapBatch(maps, xs, ys, graph=True)
+    for _ in range(3):
+        b.run()
+    ctx.sync()
+    l0 = ctx.launches
+    ms_b = _timed(ctx.stream, b.run, steps)
+    launches = (ctx.launches - l0) / steps
+
+    def seq():
+        for m, x, y in zip(maps, xs, ys):
+            m.apply_into(x, y)
+    seq()
+    ms_s = _timed(ctx.stream, seq, max(2, steps // 2))
+    err = max(float(np.linalg.norm(ctx.download(y) - r) / np.linalg.norm(r)) for y, r in zip(ys, refs))
+    flops = sum(m.flops for m in maps)
+    b.close()
+    for m in maps:
+        m.close()
+    return {"instances": 64, "ms_batched_graph": ms_b, "ms_sequential": ms_s, "speedup": ms_s / ms_b,
+            "launches_per_batched_apply": launches, "tflops_batched": flops / ms_b / 1e9, "max_rel_err_vs_oracle": err}
+
+
 def run_ours(args, rank, world):
     import torch
     import grafttn as G
@@ -339,6 +424,14 @@ def run_ours(args, rank, world):
     cpu_rate, cpu_n, cpu_el = cpu_apply_rate(x_shape, labels, order, statics, theta, budget_s=20.0, max_applies=2)
     del statics
 
+    extra = {}
+    if not args.skip_extra:
+        for name, fn in (("u1_blocksparse", bench_u1), ("batched_eff_h1", bench_batched)):
+            try:
+                extra[name] = fn(ctx, args.steps)
+            except Exception as exc:  # reported, never hides the headline
+                extra[name] = {"error": f"{type(exc).__name__}: {exc}"}
+
     clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
@@ -366,7 +459,50 @@ def run_ours(args, rank, world):
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
+
+
+def run_dmrg(args):
+    """Two-site DMRG sweeps (dmrg2!) of the dense Heisenberg chain mps_topology(63) at bond
+    dimension --dmrg-D, from one seeded random state, for each precision: wall time per
+    sweep, matvecs and the final energy (mixed energies are FP64 Rayleigh quotients)."""
+    import torch
+    import grafttn as G
+    ctx = G.default_context(0)
+    L, D = args.dmrg_sites, args.dmrg_D
+    topo = G.mps_topology(L) if args.dmrg_topology == "mps" else G.binary_topology(int(np.log2(L + 1)) - 1)
+    H = G.TTNO.from_hamiltonian(G.heisenberg(topo), ctx)
+    bond = {}
+    for c in range(topo.nnodes):
+        if topo.parent[c] >= 0:
+            below = len(topo.subtree_nodes(c, topo.parent[c]))
+            bond[c] = int(min(D, 2 ** min(below, 40), 2 ** min(L - below, 40)))
+    psi0 = G.random_ttns(np.random.default_rng(7), topo, 2, bond, ctx=ctx)
+    out = {"metric": "DMRG sweep time", "unit": "s/sweep", "topology": f"{args.dmrg_topology}{L}", "bond_dim": D,
+           "model": "Heisenberg XX+YY+ZZ (Pauli), dense ComplexF64", "krylovdim": 20, "runs": {}}
+    for prec in args.dmrg_precisions.split(","):
+        psi = psi0.copy()
+        stats = {}
+        times, energies = [], []
+        for sweep in range(args.dmrg_sweeps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, Es = G.dmrg2(psi, H, G.TruncationScheme(maxdim=D), nsweeps=1, precision=prec, lanczos_tol=1e-10,
+                            stats=stats)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+            energies.append(Es[-1])
+        out["runs"][prec] = {"sweep_s": times, "energies": energies, "matvecs": stats.get("matvecs"),
+                             "steps": stats.get("steps")}
+    runs = out["runs"]
+    if "fp64" in runs and len(runs) > 1:
+        e64 = runs["fp64"]["energies"][-1]
+        for p, r in runs.items():
+            if p != "fp64":
+                r["rel_energy_vs_fp64"] = abs(r["energies"][-1] - e64) / abs(e64)
+                r["sweep_speedup_vs_fp64"] = float(np.mean(runs["fp64"]["sweep_s"]) / np.mean(r["sweep_s"]))
+    print(json.dumps(out), flush=True)
 
 
 def main():
@@ -376,6 +512,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--skip-extra", action="store_true", help="only the headline workload")
+    ap.add_argument("--dmrg", action="store_true", help="measure DMRG sweeps instead of map applications")
+    ap.add_argument("--dmrg-topology", default="mps", choices=["mps", "binary"])
+    ap.add_argument("--dmrg-sites", type=int, default=63)
+    ap.add_argument("--dmrg-D", type=int, default=256)
+    ap.add_argument("--dmrg-sweeps", type=int, default=2)
+    ap.add_argument("--dmrg-precisions", default="bf16x6,fp64")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -387,7 +530,10 @@ def main():
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
         dist.init_process_group(backend)
     try:
-        if args.impl == "reference":
+        if args.dmrg:
+            if rank == 0:
+                run_dmrg(args)
+        elif args.impl == "reference":
             run_reference(args, rank, world)
         else:
             run_ours(args, rank, world)

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 namespace {
 
@@ -25,6 +26,8 @@ struct Solver {
   decltype(&cusolverDnZgeqrf) geqrf = nullptr;
   decltype(&cusolverDnZungqr_bufferSize) ungqr_bs = nullptr;
   decltype(&cusolverDnZungqr) ungqr = nullptr;
+  decltype(&cusolverDnZheevd_bufferSize) heevd_bs = nullptr;
+  decltype(&cusolverDnZheevd) heevd = nullptr;
   bool ok = false;
 };
 
@@ -49,9 +52,11 @@ Solver& solver() {
   LOAD(geqrf, cusolverDnZgeqrf);
   LOAD(ungqr_bs, cusolverDnZungqr_bufferSize);
   LOAD(ungqr, cusolverDnZungqr);
+  LOAD(heevd_bs, cusolverDnZheevd_bufferSize);
+  LOAD(heevd, cusolverDnZheevd);
 #undef LOAD
   s.ok = s.create && s.destroy && s.set_stream && s.gesvd_bs && s.gesvd && s.geqrf_bs && s.geqrf &&
-         s.ungqr_bs && s.ungqr;
+         s.ungqr_bs && s.ungqr && s.heevd_bs && s.heevd;
   return s;
 }
 
@@ -80,6 +85,113 @@ void linalg_release(gtn_ctx ctx) {
   }
 }
 
+namespace {
+
+// Truncation rank (truncrank & trunctol & truncerror, Backend.jl:466-483) from singular
+// values sorted descending.
+int64_t trunc_rank(const std::vector<double>& hs, int64_t maxdim, double atol, double rtol, double dw) {
+  const int64_t k = (int64_t)hs.size();
+  int64_t r = k;
+  if (maxdim > 0) r = std::min(r, maxdim);
+  if (atol > 0 || rtol > 0) {
+    const double thr = std::max(atol, rtol * hs[0]);
+    int64_t c = 0;
+    for (int64_t i = 0; i < k; ++i) c += hs[i] > thr ? 1 : 0;
+    r = std::min(r, c);
+  }
+  if (dw > 0) {
+    double tot = 0;
+    for (double v : hs) tot += v * v;
+    double tail = 0;
+    int64_t rr = k;
+    for (int64_t i = k - 1; i >= 0; --i) {
+      tail += hs[i] * hs[i];
+      if (std::sqrt(tail) <= dw * std::sqrt(tot)) rr = i;
+      else break;
+    }
+    r = std::min(r, rr);
+  }
+  return std::max<int64_t>(r, 1);
+}
+
+// Thin SVD of a wide row-major m x n matrix (m <= n) through its Gram matrix:
+// G = A A^H (FP64 GEMM), G = W diag(w) W^H (cuSOLVER Zheevd), U = W reversed (descending),
+// S = sqrt(w), Vh = S^-1 U^H A (FP64 GEMM).  Used above the size where LAPACK-style
+// bidiagonalisation (gesvd) is slow on a GPU with a weak FP64 rate; singular values below
+// ~1e-8 of the largest lose relative accuracy, far below any kept weight that matters.
+int svd_gram(gtn_ctx ctx, cusolverDnHandle_t h, int64_t m, int64_t n, const double2* A, int64_t maxdim,
+             double atol, double rtol, double dw, double2* U, double* S, double2* Vh, int64_t* rank,
+             double* discarded) {
+  Solver& sv = solver();
+  cudaStream_t s = ctx->stream;
+  int lwork = 0;
+  if (sv.heevd_bs(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)m, nullptr, (int)m, nullptr, &lwork) !=
+      CUSOLVER_STATUS_SUCCESS)
+    return set_err(ctx, GTN_ERR_CUDA, "heevd_bufferSize failed");
+  const size_t bC = align256(m * n * sizeof(double2)), bG = align256(m * m * sizeof(double2)),
+               bw = align256(m * sizeof(double)), bW = align256((size_t)lwork * sizeof(double2)),
+               bT = align256(n * m * sizeof(double2)), bUt = align256(m * m * sizeof(double2));
+  void* ws = nullptr;
+  GTN_CUDA_TRY(ctx, ctx_workspace(ctx, bC + bG + bw + bW + bT + bUt + 256, &ws));
+  char* p = static_cast<char*>(ws);
+  double2* conjA = reinterpret_cast<double2*>(p); p += bC;
+  double2* G = reinterpret_cast<double2*>(p); p += bG;
+  double* w = reinterpret_cast<double*>(p); p += bw;
+  double2* work = reinterpret_cast<double2*>(p); p += bW;
+  double2* At = reinterpret_cast<double2*>(p); p += bT;
+  double2* Ut = reinterpret_cast<double2*>(p); p += bUt;
+  int* dinfo = reinterpret_cast<int*>(p);
+  // G (column-major) : C[j][i] = sum_l A[i][l] conj(A[j][l]) = G[i][j]
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(conjA, A, m * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  GTN_CUDA_TRY(ctx, launch_conj_inplace(conjA, m * n, s));
+  GTN_CUDA_TRY(ctx, launch_zgemm_simt(A, conjA, G, m, m, n, s));
+  ctx->launches += 2;
+  if (sv.heevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)m, reinterpret_cast<cuDoubleComplex*>(G),
+               (int)m, w, reinterpret_cast<cuDoubleComplex*>(work), lwork, dinfo) != CUSOLVER_STATUS_SUCCESS)
+    return set_err(ctx, GTN_ERR_CUDA, "cusolverDnZheevd failed");
+  std::vector<double> hw(m);
+  int hinfo = 0;
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(hw.data(), w, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  if (hinfo != 0) return set_err(ctx, GTN_ERR_CUDA, "heevd info = " + std::to_string(hinfo));
+  std::vector<double> hs(m);
+  for (int64_t i = 0; i < m; ++i) hs[i] = std::sqrt(std::max(hw[m - 1 - i], 0.0));
+  const int64_t r = trunc_rank(hs, maxdim, atol, rtol, dw);
+  double disc = 0;
+  for (int64_t i = r; i < m; ++i) disc += hs[i] * hs[i];
+  for (int64_t i = 0; i < r; ++i) S[i] = hs[i];
+  *rank = r;
+  if (discarded) *discarded = std::sqrt(disc);
+  // U[a][i] = W[a + (m-1-i) m]  (W column-major): gather with a negative column stride
+  GroupSpec mg, kg;
+  std::memset(&mg, 0, sizeof(mg));
+  std::memset(&kg, 0, sizeof(kg));
+  mg.n = 1; mg.dim[0] = m; mg.str[0] = 1;
+  kg.n = 1; kg.dim[0] = r; kg.str[0] = -m;
+  GTN_CUDA_TRY(ctx, launch_gather_c128_to_c128(G + (m - 1) * m, mg, kg, m, r, r, U, s));
+  // Ut[i][a] = conj(U[a][i]) : r x m
+  mg.dim[0] = r; mg.str[0] = -m;
+  kg.dim[0] = m; kg.str[0] = 1;
+  GTN_CUDA_TRY(ctx, launch_gather_c128_to_c128(G + (m - 1) * m, mg, kg, r, m, m, Ut, s));
+  GTN_CUDA_TRY(ctx, launch_conj_inplace(Ut, r * m, s));
+  // Vh[i][l] = sum_a Ut[i][a] A[a][l]: C[nn=i][mm=l] = sum_k X[l][k] Y[i][k], X = A^T, Y = Ut
+  GTN_CUDA_TRY(ctx, launch_transpose_c128(A, m, n, At, s));
+  GTN_CUDA_TRY(ctx, launch_zgemm_simt(At, Ut, Vh, n, r, m, s));
+  ctx->launches += 6;
+  std::vector<double> inv(r);
+  for (int64_t i = 0; i < r; ++i) inv[i] = hs[i] > 0 ? 1.0 / hs[i] : 0.0;
+  double* dinv = reinterpret_cast<double*>(conjA);  // conjA is no longer needed
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(dinv, inv.data(), r * sizeof(double), cudaMemcpyHostToDevice, s));
+  GTN_CUDA_TRY(ctx, launch_diag_scale(Vh, r, n, dinv, 1, s));
+  ctx->launches++;
+  return gtn_ctx_sync(ctx);
+}
+
+constexpr int64_t kGramMin = 384;
+
+}  // namespace
+
 extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, int64_t maxdim, double atol,
                              double rtol, double discarded_weight, void* U, double* S, void* Vh,
                              int64_t* rank, double* discarded) {
@@ -92,6 +204,37 @@ extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, i
   Solver& sv = solver();
   cudaStream_t s = ctx->stream;
   const int64_t k = std::min(m, n);
+  if (k >= kGramMin) {
+    if (m <= n)
+      return svd_gram(ctx, h, m, n, static_cast<const double2*>(A), maxdim, atol, rtol, discarded_weight,
+                      static_cast<double2*>(U), S, static_cast<double2*>(Vh), rank, discarded);
+    // tall: B = A^T (n x m, wide) = U_B S Vh_B  =>  U_A = Vh_B^T, Vh_A = U_B^T
+    double2* B = nullptr;
+    double2 *UB = nullptr, *VB = nullptr;
+    if (cudaMalloc(&B, m * n * sizeof(double2)) != cudaSuccess || cudaMalloc(&UB, n * k * sizeof(double2)) != cudaSuccess ||
+        cudaMalloc(&VB, k * m * sizeof(double2)) != cudaSuccess) {
+      cudaFree(B);
+      cudaFree(UB);
+      return set_err(ctx, GTN_ERR_MEMORY, "svd transpose staging");
+    }
+    st = GTN_OK;
+    cudaError_t e = launch_transpose_c128(static_cast<const double2*>(A), m, n, B, s);
+    if (e == cudaSuccess) st = svd_gram(ctx, h, n, m, B, maxdim, atol, rtol, discarded_weight, UB, S, VB, rank, discarded);
+    else st = set_err(ctx, GTN_ERR_CUDA, cudaGetErrorString(e));
+    if (st == GTN_OK) {
+      const int64_t r = *rank;
+      e = launch_transpose_c128(VB, r, m, static_cast<double2*>(U), s);       // (r x m)^T = m x r
+      if (e == cudaSuccess) e = launch_transpose_c128(UB, n, r, static_cast<double2*>(Vh), s);  // (n x r)^T
+      ctx->launches += 3;
+      if (e != cudaSuccess) st = set_err(ctx, GTN_ERR_CUDA, cudaGetErrorString(e));
+      else st = gtn_ctx_sync(ctx);
+    }
+    cudaStreamSynchronize(s);
+    cudaFree(B);
+    cudaFree(UB);
+    cudaFree(VB);
+    return st;
+  }
   // Column-major problem B (rows >= cols): for n >= m, B = A^T (the same buffer); else B =
   // column-major copy of A (a transpose).
   const bool wide = n >= m;
@@ -130,28 +273,7 @@ extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, i
   GTN_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
   GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
   if (hinfo != 0) return set_err(ctx, GTN_ERR_CUDA, "gesvd info = " + std::to_string(hinfo));
-  // truncation rank (truncrank & trunctol & truncerror)
-  int64_t r = k;
-  if (maxdim > 0) r = std::min(r, maxdim);
-  if (atol > 0 || rtol > 0) {
-    const double thr = std::max(atol, rtol * hs[0]);
-    int64_t c = 0;
-    for (int64_t i = 0; i < k; ++i) c += hs[i] > thr ? 1 : 0;
-    r = std::min(r, c);
-  }
-  double tot = 0;
-  for (double v : hs) tot += v * v;
-  if (discarded_weight > 0) {
-    double tail = 0;
-    int64_t rr = k;
-    for (int64_t i = k - 1; i >= 0; --i) {
-      tail += hs[i] * hs[i];
-      if (std::sqrt(tail) <= discarded_weight * std::sqrt(tot)) rr = i;
-      else break;
-    }
-    r = std::min(r, rr);
-  }
-  r = std::max<int64_t>(r, 1);
+  const int64_t r = trunc_rank(hs, maxdim, atol, rtol, discarded_weight);
   double disc = 0;
   for (int64_t i = r; i < k; ++i) disc += hs[i] * hs[i];
   for (int64_t i = 0; i < r; ++i) S[i] = hs[i];

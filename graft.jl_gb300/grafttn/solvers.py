@@ -32,22 +32,38 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
     energies = []
     bonds = [n for n in t.postorder() if t.parent[n] >= 0]
     sched = [(n, "m") for n in bonds] + [(n, "n") for n in reversed(bonds)]
+    timing = stats is not None and stats.get("timing", False)
+
+    def mark(key, t_start):
+        if timing:
+            psi.ctx.sync()
+            stats[key] = stats.get(key, 0.0) + time.perf_counter() - t_start
+        return time.perf_counter()
     for sweep in range(nsweeps):
         E = float("nan")
         t0 = time.perf_counter()
-        for n, center_on in sched:
+        for step, (n, center_on) in enumerate(sched):
+            if stats is not None and stats.get("max_steps") is not None and step >= stats["max_steps"]:
+                break
             m = t.parent[n]
+            tt = time.perf_counter()
             move_center(psi, n, cache)
+            tt = mark("t_gauge", tt)
             theta = two_site_tensor(psi, n, m)
+            tt = mark("t_merge", tt)
             h2 = eff_h2(cache, psi, H, n, m, prec)
+            tt = mark("t_env_and_map", tt)
             E, v, info = h2.lanczos_min(theta, krylovdim=krylovdim, tol=lanczos_tol, maxiter=maxiter,
                                         rq_fp64=rq_fp64)
+            tt = mark("t_lanczos", tt)
             if stats is not None:
-                stats.setdefault("matvecs", 0)
-                stats["matvecs"] += info["matvecs"]
+                stats["matvecs"] = stats.get("matvecs", 0) + info["matvecs"]
+                stats["steps"] = stats.get("steps", 0) + 1
+                stats.setdefault("energies", []).append(E)
             h2.close()
             cache.invalidate_edge(n, m)
             split_two_site(psi, v, n, m, trunc, center_on)
+            tt = mark("t_split", tt)
         energies.append(float(E))
         if verbose:
             print(f"dmrg2 sweep {sweep + 1}: E = {E:.15f}  ({time.perf_counter() - t0:.3f} s)")

@@ -25,3 +25,14 @@ def test_block_plan_matches_dense(depth, node, D):
     # the output has the input's block structure (the map conserves charge)
     assert [b[0] for b in plan.y.blocks] == [b[0] for b in xs.blocks]
     assert plan.flops > 0 and len(plan.steps) == len(order) - 1
+
+
+def test_u1_oracle_matches_dense_and_planner():
+    from oracle import u1_oracle as U
+    xs, labels, order, statics, x = h2_u1_case(3, "n2_2", 16)
+    blocks = [U.blocks_from_flat(xs, x)] + [U.blocks_from_flat(T, d) for T, _, d in statics]
+    plan = B.BlockPlan(xs, labels[0], statics, order)
+    y_or = U.flat_from_blocks(plan.y, U.ncon_blocks(blocks, labels, order))
+    ref = dense_reference(xs, labels, order, statics, x)
+    assert np.linalg.norm(plan.y.to_dense(y_or) - ref) <= 1e-12 * np.linalg.norm(ref)
+    assert np.linalg.norm(B.execute_numpy(plan, x) - y_or) <= 1e-12 * np.linalg.norm(y_or)

@@ -133,3 +133,24 @@ def test_lanczos_and_expm(ctx):
     ref = sla.expm(-0.3j * Hm) @ x0
     assert rel(ctx.download(y), ref) < 1e-10
     hm.close()
+
+
+@pytest.mark.parametrize("m,n", [(500, 700), (700, 500), (512, 512)])
+def test_svd_gram_path_large(ctx, m, n):
+    # above the Gram threshold: FP64 GEMM + Zheevd; decaying spectrum down to 1e-7
+    rng = np.random.default_rng(8)
+    k = min(m, n)
+    U0, _ = np.linalg.qr(crandn(rng, (m, k)))
+    V0, _ = np.linalg.qr(crandn(rng, (n, k)))
+    s0 = np.logspace(0, -7, k)
+    a = (U0 * s0) @ V0.conj().T
+    U, S, Vh, disc = ctx.svd_trunc(ctx.upload(a), maxdim=300)
+    U, Vh = ctx.download(U), ctx.download(Vh)
+    assert len(S) == 300
+    # the Gram path resolves sigma to ~eps * s_max^2 / sigma: ~1e-12 absolute here
+    assert np.allclose(S, s0[:300], rtol=1e-6, atol=1e-12)
+    ref = (U0[:, :300] * s0[:300]) @ V0[:, :300].conj().T
+    assert np.linalg.norm((U * S) @ Vh - ref) < 1e-9 * np.linalg.norm(ref)
+    assert np.allclose(U.conj().T @ U, np.eye(300), atol=1e-9)
+    # discarded 2-norm from Gram eigenvalues: absolute accuracy ~ sqrt(k) * eps / s_300
+    assert abs(disc - np.sqrt(np.sum(s0[300:] ** 2))) < 1e-8
