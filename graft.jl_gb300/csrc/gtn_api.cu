@@ -275,6 +275,16 @@ int gtn_axpby(gtn_ctx ctx, int64_t n, double a_re, double a_im, const void* x, d
   return GTN_OK;
 }
 
+int gtn_copy2d(gtn_ctx ctx, int64_t rows, int64_t cols, const void* src, int64_t src_ld, void* dst,
+               int64_t dst_ld) {
+  if (!ctx || !src || !dst || rows < 0 || cols < 0 || src_ld < cols || dst_ld < cols)
+    return set_err(ctx, GTN_ERR_INVALID, "gtn_copy2d: bad argument");
+  if (rows == 0 || cols == 0) return GTN_OK;
+  GTN_CUDA_TRY(ctx, cudaMemcpy2DAsync(dst, dst_ld * sizeof(double2), src, src_ld * sizeof(double2),
+                                      cols * sizeof(double2), rows, cudaMemcpyDeviceToDevice, ctx->stream));
+  return GTN_OK;
+}
+
 int gtn_diag_scale(gtn_ctx ctx, int64_t rows, int64_t cols, const double* d_host, int side, void* A) {
   if (!ctx || !d_host || !A || rows < 0 || cols < 0 || (side != 0 && side != 1))
     return set_err(ctx, GTN_ERR_INVALID, "gtn_diag_scale: bad argument");

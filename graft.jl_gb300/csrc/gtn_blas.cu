@@ -178,6 +178,33 @@ __global__ void diag_scale_kernel(double2* __restrict__ A, int64_t rows, int64_t
   }
 }
 
+// out[r] = ||A[r][:]||_2, one CTA per row
+__global__ void __launch_bounds__(256) row_norms_kernel(const double2* __restrict__ A, int64_t cols,
+                                                        double* __restrict__ out) {
+  __shared__ double red[256];
+  const double2* a = A + (int64_t)blockIdx.x * cols;
+  double acc = 0.0;
+  for (int64_t c = threadIdx.x; c < cols; c += 256) acc += a[c].x * a[c].x + a[c].y * a[c].y;
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sqrt(red[0]);
+}
+
+// A[r][c] = conj(ph[r] * A[r][c])
+__global__ void row_phase_conj_kernel(double2* __restrict__ A, int64_t rows, int64_t cols,
+                                      const double2* __restrict__ ph) {
+  const int64_t total = rows * cols;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 p = ph[i / cols], a = A[i];
+    A[i] = make_double2(p.x * a.x - p.y * a.y, -(p.x * a.y + p.y * a.x));
+  }
+}
+
 inline unsigned grid_for(int64_t n) {
   int64_t b = (n + 255) / 256;
   if (b > 152 * 8) b = 152 * 8;
@@ -238,5 +265,16 @@ cudaError_t launch_zero_lower(double2* R, int64_t rows, int64_t cols, cudaStream
 cudaError_t launch_diag_scale(double2* A, int64_t rows, int64_t cols, const double* d, int side,
                               cudaStream_t s) {
   diag_scale_kernel<<<grid_for(rows * cols), 256, 0, s>>>(A, rows, cols, d, side);
+  return cudaGetLastError();
+}
+cudaError_t launch_row_phase_conj(double2* A, int64_t rows, int64_t cols, const double2* ph, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return cudaSuccess;
+  row_phase_conj_kernel<<<grid_for(rows * cols), 256, 0, s>>>(A, rows, cols, ph);
+  return cudaGetLastError();
+}
+cudaError_t launch_row_norms(const double2* A, int64_t rows, int64_t cols, double* out, cudaStream_t s) {
+  if (rows <= 0) return cudaSuccess;
+  if (rows > 2147483647LL) return cudaErrorInvalidConfiguration;
+  row_norms_kernel<<<(unsigned)rows, 256, 0, s>>>(A, cols, out);
   return cudaGetLastError();
 }

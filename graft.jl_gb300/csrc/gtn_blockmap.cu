@@ -20,6 +20,7 @@ struct BMStep {
   int src_is64 = 0;
   std::vector<TcGemmArgs> tcp;   // tcgen05 problems (addresses fixed at creation)
   std::vector<GemmJob> simt;     // SIMT problems
+  std::vector<GemmJob> skinny;   // SIMT problems with N <= 32
 };
 
 struct gtn_blockmap_s {
@@ -49,7 +50,9 @@ struct gtn_blockmap_s {
 
 namespace {
 
-constexpr int64_t kTcMinK = 64;  // coupled-charge problems with smaller K run on the SIMT GEMM
+// Coupled-charge problems with K < 16 or N < 16 run on the SIMT GEMMs (FP32 in the mixed
+// modes): padding them to the tcgen05 tile costs more than their arithmetic.
+constexpr int64_t kTcMinK = 16, kTcMinN = 16;
 
 bool is_tc_p(int p) { return p == GTN_PREC_BF16X6 || p == GTN_PREC_BF16X3; }
 int planes_p(int p) { return p == GTN_PREC_BF16X6 ? 3 : 2; }
@@ -82,7 +85,8 @@ cudaError_t upload_jobs(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, BMStep
   for (size_t i = 0; i < jobs.size(); ++i) {
     finish_dev_gather_job(&jobs[i]);
     start[i] = tiles;
-    if (jobs[i].M > 0 && jobs[i].Kw > 0) tiles += jobs[i].tiles_m * (int)((jobs[i].Kw + 31) / 32);
+    if (jobs[i].M > 0 && jobs[i].Kw > 0)
+      tiles += jobs[i].tiles_m * (int)((jobs[i].Kw + (1 << jobs[i].tks) - 1) >> jobs[i].tks);
   }
   start[jobs.size()] = tiles;
   st->njobs = (int)jobs.size();
@@ -123,6 +127,10 @@ int run(gtn_blockmap bm, const double2* x, double2* y) {
     if (e == cudaSuccess && !st.simt.empty()) {
       e = launch_gemm_simt_grouped(st.simt.data(), (int)st.simt.size(), fp64 ? 1 : 0, s);
       ctx->launches += (int64_t)((st.simt.size() + kGemmJobMax - 1) / kGemmJobMax);
+    }
+    if (e == cudaSuccess && !st.skinny.empty()) {
+      e = launch_gemm_skinny_grouped(st.skinny.data(), (int)st.skinny.size(), fp64 ? 1 : 0, s);
+      ctx->launches += (int64_t)((st.skinny.size() + kGemmJobMax - 1) / kGemmJobMax);
     }
   }
   if (e == cudaSuccess) {
@@ -231,7 +239,7 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
       if (g.b_index < 0 || g.b_index >= nstatics || g.c_buf < 2 || g.c_buf > 3 || bm->bN[g.b_index] != g.N ||
           bm->bK[g.b_index] != g.K || g.M <= 0)
         return fail(GTN_ERR_INVALID, "bad GEMM descriptor in step " + std::to_string(s));
-      const bool t = tc && g.K >= kTcMinK;
+      const bool t = tc && g.K >= kTcMinK && g.N >= kTcMinN;
       use_tc.push_back(t ? 1 : 0);
       const int64_t k = t ? ((g.K + 31) / 32) * 32 : g.K;
       kp.push_back(k);
@@ -325,7 +333,10 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
         J.M = g.M;
         J.N = g.N;
         J.K = g.K;
-        st.simt.push_back(J);
+        if (gemm_skinny_fits(g.N, g.K, fp64 ? 1 : 0))
+          st.skinny.push_back(J);
+        else
+          st.simt.push_back(J);
       }
       bm->n_problems++;
     }

@@ -138,6 +138,112 @@ cudaError_t launch_grouped(const GemmJob* jobs, int njobs, cudaStream_t s) {
   return cudaSuccess;
 }
 
+// Skinny variant for N <= 32 (coupled-charge problems with a few output columns): B lives
+// in shared memory, A is staged in 128-row x 16-column chunks through shared memory, and
+// thread (r, g) of a 128*ng-thread CTA owns row r and the 8 columns n = 8g .. 8g+7.
+constexpr int SK_ROWS = 128, SK_KC = 16, kSkinnyMaxN = 32;
+
+struct SkinnyJobsP {
+  GemmJob j[kGemmJobMax];
+  int blk_start[kGemmJobMax + 1];
+  int n;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(512) gemm_skinny_grouped_kernel(const __grid_constant__ SkinnyJobsP g) {
+  extern __shared__ __align__(16) unsigned char sk_smem[];
+  const int b = blockIdx.x;
+  int p = 0;
+  while (p + 1 < g.n && g.blk_start[p + 1] <= b) ++p;
+  const GemmJob& J = g.j[p];
+  const int64_t blk = b - g.blk_start[p], nblk = g.blk_start[p + 1] - g.blk_start[p];
+  const T* __restrict__ A = static_cast<const T*>(J.A);
+  const T* __restrict__ B = static_cast<const T*>(J.B);
+  T* __restrict__ C = static_cast<T*>(J.C);
+  const int64_t M = J.M;
+  const int N = (int)J.N, K = (int)J.K;
+  T* Bs = reinterpret_cast<T*>(sk_smem);
+  T* As = Bs + (size_t)N * K;  // [SK_ROWS][SK_KC + 1]
+  const int nthr = blockDim.x, tid = threadIdx.x;
+  const int r = tid & (SK_ROWS - 1), n0 = (tid >> 7) * 8;
+  for (int i = tid; i < N * K; i += nthr) Bs[i] = B[i];
+  for (int64_t c0 = blk * SK_ROWS; c0 < M; c0 += nblk * SK_ROWS) {
+    const int rows = (int)(M - c0 < SK_ROWS ? M - c0 : SK_ROWS);
+    T acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = CT<T>::zero();
+    for (int k0 = 0; k0 < K; k0 += SK_KC) {
+      const int kc = K - k0 < SK_KC ? K - k0 : SK_KC;
+      __syncthreads();
+      for (int e = tid; e < SK_ROWS * SK_KC; e += nthr) {
+        const int rr = e >> 4, kk = e & (SK_KC - 1);
+        As[rr * (SK_KC + 1) + kk] = (rr < rows && kk < kc) ? A[(c0 + rr) * K + k0 + kk] : CT<T>::zero();
+      }
+      __syncthreads();
+      for (int kk = 0; kk < kc; ++kk) {
+        const T a = As[r * (SK_KC + 1) + kk];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (n0 + j < N) {
+            const T bv = Bs[(n0 + j) * K + k0 + kk];
+            acc[j].x = fma(a.x, bv.x, acc[j].x);
+            acc[j].x = fma(-a.y, bv.y, acc[j].x);
+            acc[j].y = fma(a.x, bv.y, acc[j].y);
+            acc[j].y = fma(a.y, bv.x, acc[j].y);
+          }
+        }
+      }
+    }
+    if (r < rows) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (n0 + j < N) C[(int64_t)(n0 + j) * M + c0 + r] = acc[j];
+    }
+  }
+}
+
+template <typename T>
+size_t skinny_smem(const GemmJob& J) {
+  return ((size_t)J.N * J.K + (size_t)SK_ROWS * (SK_KC + 1)) * sizeof(T);
+}
+
+template <typename T>
+cudaError_t launch_skinny(const GemmJob* jobs, int njobs, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(gemm_skinny_grouped_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kSkinnyMaxSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  for (int base = 0; base < njobs; base += kGemmJobMax) {
+    const int cnt = std::min(kGemmJobMax, njobs - base);
+    SkinnyJobsP g;
+    std::memset(&g, 0, sizeof(g));
+    int blocks = 0, maxn = 1;
+    size_t smem = 0;
+    for (int q = 0; q < cnt; ++q) {
+      const GemmJob& J = jobs[base + q];
+      if (J.N > kSkinnyMaxN || skinny_smem<T>(J) > (size_t)kSkinnyMaxSmem) return cudaErrorInvalidValue;
+      g.j[q] = J;
+      g.blk_start[q] = blocks;
+      int64_t nb = (J.M + SK_ROWS - 1) / SK_ROWS;
+      if (nb > 1024) nb = 1024;
+      blocks += (J.M > 0 && J.N > 0) ? (int)nb : 0;
+      smem = std::max(smem, skinny_smem<T>(J));
+      maxn = std::max(maxn, (int)J.N);
+    }
+    g.blk_start[cnt] = blocks;
+    g.n = cnt;
+    if (blocks == 0) continue;
+    const int threads = SK_ROWS * ((maxn + 7) / 8);
+    gemm_skinny_grouped_kernel<T><<<blocks, threads, smem, s>>>(g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 template <typename T>
 cudaError_t launch(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, cudaStream_t s) {
   if (M <= 0 || N <= 0) return cudaSuccess;
@@ -155,6 +261,13 @@ cudaError_t launch_zgemm_simt(const double2* A, const double2* B, double2* C, in
 }
 cudaError_t launch_gemm_simt_grouped(const GemmJob* jobs, int njobs, int is64, cudaStream_t s) {
   return is64 ? launch_grouped<double2>(jobs, njobs, s) : launch_grouped<float2>(jobs, njobs, s);
+}
+cudaError_t launch_gemm_skinny_grouped(const GemmJob* jobs, int njobs, int is64, cudaStream_t s) {
+  return is64 ? launch_skinny<double2>(jobs, njobs, s) : launch_skinny<float2>(jobs, njobs, s);
+}
+bool gemm_skinny_fits(int64_t N, int64_t K, int is64) {
+  const size_t e = is64 ? sizeof(double2) : sizeof(float2);
+  return N >= 1 && N <= kSkinnyMaxN && ((size_t)N * K + (size_t)SK_ROWS * (SK_KC + 1)) * e <= (size_t)kSkinnyMaxSmem;
 }
 cudaError_t launch_cgemm_simt(const float2* A, const float2* B, float2* C, int64_t M, int64_t N,
                               int64_t K, cudaStream_t s) {

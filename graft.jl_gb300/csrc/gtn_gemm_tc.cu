@@ -18,6 +18,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 namespace {
@@ -93,6 +94,17 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   d |= (uint64_t)(1024u >> 4) << 32;  // stride byte offset
   d |= (uint64_t)1u << 46;            // descriptor version
   d |= (uint64_t)2u << 61;            // SWIZZLE_128B
+  return d;
+}
+
+// Shared-memory matrix descriptor: K-major, SWIZZLE_64B, 8-row groups 512 B apart.
+__device__ __forceinline__ uint64_t sdesc64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;            // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512u >> 4) << 32;   // stride byte offset
+  d |= (uint64_t)1u << 46;            // descriptor version
+  d |= (uint64_t)4u << 61;            // SWIZZLE_64B
   return d;
 }
 
@@ -271,6 +283,181 @@ __device__ __forceinline__ void tc_tile(const CUtensorMap* tmA, const CUtensorMa
   }
 }
 
+// Variant: every stage holds all P slice planes of A and of B' for one 32-wide k-block
+// (SWIZZLE_64B rows of 64 B), and the MMA thread issues every slice product from that
+// stage.  Operand bytes per MAC drop by the number of products that share a plane
+// (6 products from 3+3 planes for bf16x6), relieving L2->SM bandwidth.  Because the
+// products of one k-block are interleaved, the leading product (plane 0 x plane 0) and
+// the correction products accumulate in two TMEM accumulators that the epilogue adds:
+// the corrections then never round against the leading product's running sum.
+constexpr int BKE2 = 32;
+template <int BN, int P> struct Cfg2 {
+  static constexpr int A_PLANE = BM * BKE2 * 2;   // 8 KB
+  static constexpr int B_PLANE = BN * BKE2 * 2;
+  static constexpr int STAGE_BYTES = P * (A_PLANE + B_PLANE);
+  static constexpr int ST = (228352 - 2048) / STAGE_BYTES;
+  static constexpr int STAGES = ST > 8 ? 8 : ST;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024;
+  static constexpr uint32_t ACC_COLS = BN < 32 ? 32 : BN;   // column offset of the correction accumulator
+  static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
+};
+
+template <int BN, int P>
+__device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtensorMap* tmB, float2* __restrict__ C,
+                                           int64_t M, int64_t N, int nkb, const ProdList& prods, int m0, int r0,
+                                           int* __restrict__ errflag) {
+  using CF = Cfg2<BN, P>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~static_cast<uintptr_t>(1023));
+  __shared__ __align__(8) uint64_t full_bar[CF::STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[CF::STAGES];
+  __shared__ __align__(8) uint64_t accum_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  __shared__ int n_issued, n_consumed;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < CF::STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(&accum_bar, 1);
+    abort_flag = 0;
+    n_issued = 0;
+    n_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmB)) : "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(CF::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem_d = tmem_slot;
+  const int total = nkb;
+
+  if (warp == 0 && lane == 0) {
+    int it = 0;
+    for (; it < total; ++it) {
+      const int s = it % CF::STAGES;
+      const uint32_t ph = (uint32_t)(it / CF::STAGES) & 1u;
+      if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_flag)) {
+        abort_flag = 1;
+        atomicCAS(errflag, 0, DEVERR_TMA_TIMEOUT);
+        break;
+      }
+      const uint32_t sa = smem_u32(smem + s * CF::STAGE_BYTES);
+      const uint32_t sb = sa + P * CF::A_PLANE;
+      mbar_expect_tx(&full_bar[s], CF::STAGE_BYTES);
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        tma_load_3d(sa + p * CF::A_PLANE, tmA, &full_bar[s], it * BKE2, m0, p);
+        tma_load_3d(sb + p * CF::B_PLANE, tmB, &full_bar[s], it * BKE2, r0, p);
+      }
+    }
+    n_issued = it;
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = idesc_bf16(BM, BN);
+    bool lead_started = false, corr_started = false;
+    int it = 0;
+    for (; it < total; ++it) {
+      const int s = it % CF::STAGES;
+      const uint32_t ph = (uint32_t)(it / CF::STAGES) & 1u;
+      if (!mbar_wait(&full_bar[s], ph, &abort_flag)) {
+        abort_flag = 1;
+        atomicCAS(errflag, 0, DEVERR_MMA_TIMEOUT);
+        break;
+      }
+      fence_after();
+      const uint32_t sa = smem_u32(smem + s * CF::STAGE_BYTES);
+      const uint32_t sb = sa + P * CF::A_PLANE;
+      for (int q = 0; q < prods.n; ++q) {
+        const uint32_t a0 = sa + prods.a[q] * CF::A_PLANE;
+        const uint32_t b0 = sb + prods.b[q] * CF::B_PLANE;
+        const bool lead = prods.a[q] == 0 && prods.b[q] == 0;
+        const uint32_t d = lead ? tmem_d : tmem_d + CF::ACC_COLS;
+#pragma unroll
+        for (int kk = 0; kk < BKE2 / 16; ++kk) {
+          umma_bf16(d, sdesc64(a0 + kk * 32), sdesc64(b0 + kk * 32), idesc,
+                    (lead ? lead_started : corr_started) ? 1u : 0u);
+          if (lead) lead_started = true; else corr_started = true;
+        }
+      }
+      umma_commit(&empty_bar[s]);
+    }
+    n_consumed = it;
+    umma_commit(&accum_bar);
+  }
+  __syncwarp();
+
+  const bool ok = mbar_wait(&accum_bar, 0u, &abort_flag);
+  if (!ok && lane == 0) {
+    abort_flag = 1;
+    atomicCAS(errflag, 0, DEVERR_EPI_TIMEOUT);
+  }
+  __syncwarp();
+  fence_after();
+  if (ok) {
+    const int row = warp * 32 + lane;
+    const int64_t m = (int64_t)m0 + row;
+    const uint32_t taddr = tmem_d + ((uint32_t)(warp * 32) << 16);
+    bool has_corr = false;
+    for (int q = 0; q < prods.n; ++q) has_corr |= !(prods.a[q] == 0 && prods.b[q] == 0);
+#pragma unroll 1
+    for (int c = 0; c < BN; c += 16) {
+      uint32_t v[16], w[16];
+      tmem_ld16(taddr + (uint32_t)c, v);
+      if (has_corr) {
+        tmem_ld16(taddr + CF::ACC_COLS + (uint32_t)c, w);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) w[j] = 0u;
+      }
+      if (m < M) {
+        const int64_t nb = (int64_t)(r0 + c) >> 1;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int64_t n = nb + j;
+          if (n < N)
+            C[n * M + m] = make_float2(__uint_as_float(v[2 * j]) + __uint_as_float(w[2 * j]),
+                                       __uint_as_float(v[2 * j + 1]) + __uint_as_float(w[2 * j + 1]));
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int it = n_consumed; it < n_issued; ++it) {
+      volatile int no_abort = 0;
+      mbar_wait(&full_bar[it % CF::STAGES], (uint32_t)(it / CF::STAGES) & 1u, &no_abort);
+    }
+  }
+  __syncthreads();
+  if (warp == 2) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d),
+                 "r"(CF::TMEM_COLS)
+                 : "memory");
+  }
+}
+
+template <int BN, int P>
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_ps_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      float2* __restrict__ C, int64_t M, int64_t N, int nkb, ProdList prods,
+                      int* __restrict__ errflag) {
+  tc_tile_ps<BN, P>(&tmA, &tmB, C, M, N, nkb, prods, blockIdx.x * BM, blockIdx.y * BN, errflag);
+}
+
 template <int BN>
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -293,6 +480,17 @@ struct GroupedTc {
   int nprob;
   ProdList prods;
 };
+
+template <int BN, int P>
+__global__ void __launch_bounds__(128, 1) tc_gemm_grouped_ps_kernel(const __grid_constant__ GroupedTc g,
+                                                                    int* __restrict__ errflag) {
+  const int b = blockIdx.x;
+  int p = 0;
+  while (p + 1 < g.nprob && g.tile_start[p + 1] <= b) ++p;
+  const int t = b - g.tile_start[p];
+  const int tm = t % g.tiles_m[p], tn = t / g.tiles_m[p];
+  tc_tile_ps<BN, P>(&g.tmA[p], &g.tmB[p], g.C[p], g.M[p], g.N[p], g.nkb[p], g.prods, tm * BM, tn * BN, errflag);
+}
 
 template <int BN>
 __global__ void __launch_bounds__(128, 1) tc_gemm_grouped_kernel(const __grid_constant__ GroupedTc g,
@@ -327,7 +525,7 @@ EncodeTiledFn get_encode() {
 
 // 3-D map over bf16 planes: (2Kp elements, rows, planes), box (64, box_rows, 1).
 bool make_map(CUtensorMap* tm, const void* base, int64_t Kp, int64_t rows, int planes, int box_rows,
-              std::string* why) {
+              std::string* why, int box_k = BKE) {
   EncodeTiledFn enc = get_encode();
   if (!enc) {
     if (why) *why = "cuTensorMapEncodeTiled unavailable";
@@ -335,16 +533,115 @@ bool make_map(CUtensorMap* tm, const void* base, int64_t Kp, int64_t rows, int p
   }
   cuuint64_t gdim[3] = {(cuuint64_t)(2 * Kp), (cuuint64_t)rows, (cuuint64_t)planes};
   cuuint64_t gstr[2] = {(cuuint64_t)(2 * Kp * 2), (cuuint64_t)(rows * 2 * Kp * 2)};
-  cuuint32_t box[3] = {(cuuint32_t)BKE, (cuuint32_t)box_rows, 1u};
+  cuuint32_t box[3] = {(cuuint32_t)box_k, (cuuint32_t)box_rows, 1u};
   cuuint32_t estr[3] = {1u, 1u, 1u};
   CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), gdim, gstr, box,
-                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   box_k == BKE ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     if (why) *why = "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")";
     return false;
   }
   return true;
+}
+
+// Kernel variant: 1 = all slice planes per stage (SWIZZLE_64B), 0 = one product per stage
+// (SWIZZLE_128B).  GTN_TC_VARIANT overrides the default.
+int tc_variant() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("GTN_TC_VARIANT");
+    v = (e && e[0] == '0') ? 0 : 1;
+  }
+  return v;
+}
+
+template <int BN, int P>
+cudaError_t launch_ps(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why) {
+  using CF = Cfg2<BN, P>;
+  CUtensorMap tmA, tmB;
+  if (!make_map(&tmA, a.A, a.Kp, a.M, a.a_planes, BM, why, BKE2)) return cudaErrorInvalidValue;
+  if (!make_map(&tmB, a.B, a.Kp, 2 * a.N, a.b_planes, BN, why, BKE2)) return cudaErrorInvalidValue;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_ps_kernel<BN, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         CF::SMEM);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  ProdList pl;
+  pl.n = a.nprod;
+  for (int i = 0; i < 9; ++i) {
+    pl.a[i] = i < a.nprod ? a.prod_a[i] : 0;
+    pl.b[i] = i < a.nprod ? a.prod_b[i] : 0;
+  }
+  const int nkb = (int)((2 * a.Kp + BKE2 - 1) / BKE2);
+  const int64_t gx = (a.M + BM - 1) / BM;
+  const int64_t gy = (2 * a.N + BN - 1) / BN;
+  if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
+  tc_gemm_ps_kernel<BN, P><<<dim3((unsigned)gx, (unsigned)gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb,
+                                                                                  pl, errflag);
+  return cudaGetLastError();
+}
+
+template <int BN, int P>
+cudaError_t launch_grouped_ps(const TcGemmArgs* probs, int nprob, int* errflag, cudaStream_t s, std::string* why) {
+  using CF = Cfg2<BN, P>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_grouped_ps_kernel<BN, P>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  for (int base = 0; base < nprob; base += kTcGroupMax) {
+    const int cnt = std::min(kTcGroupMax, nprob - base);
+    GroupedTc g;
+    std::memset(&g, 0, sizeof(g));
+    int tiles = 0;
+    for (int q = 0; q < cnt; ++q) {
+      const TcGemmArgs& a = probs[base + q];
+      if (!make_map(&g.tmA[q], a.A, a.Kp, a.M, a.a_planes, BM, why, BKE2)) return cudaErrorInvalidValue;
+      if (!make_map(&g.tmB[q], a.B, a.Kp, 2 * a.N, a.b_planes, BN, why, BKE2)) return cudaErrorInvalidValue;
+      g.C[q] = a.C;
+      g.M[q] = a.M;
+      g.N[q] = a.N;
+      g.nkb[q] = (int)((2 * a.Kp + BKE2 - 1) / BKE2);
+      g.tiles_m[q] = (int)((a.M + BM - 1) / BM);
+      g.tile_start[q] = tiles;
+      tiles += g.tiles_m[q] * (int)((2 * a.N + BN - 1) / BN);
+    }
+    g.tile_start[cnt] = tiles;
+    g.nprob = cnt;
+    g.prods.n = probs[base].nprod;
+    for (int i = 0; i < 9; ++i) {
+      g.prods.a[i] = i < probs[base].nprod ? probs[base].prod_a[i] : 0;
+      g.prods.b[i] = i < probs[base].nprod ? probs[base].prod_b[i] : 0;
+    }
+    if (tiles == 0) continue;
+    tc_gemm_grouped_ps_kernel<BN, P><<<tiles, 128, CF::SMEM, s>>>(g, errflag);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template <int P>
+cudaError_t launch_ps_bn(const TcGemmArgs& a, int64_t n2, int* errflag, cudaStream_t s, std::string* why) {
+  if (n2 <= 32) return launch_ps<32, P>(a, errflag, s, why);
+  if (n2 <= 64) return launch_ps<64, P>(a, errflag, s, why);
+  if (n2 <= 128) return launch_ps<128, P>(a, errflag, s, why);
+  return launch_ps<256, P>(a, errflag, s, why);
+}
+
+template <int P>
+cudaError_t launch_grouped_ps_bn(const TcGemmArgs* probs, int nprob, int64_t n2, int* errflag, cudaStream_t s,
+                                 std::string* why) {
+  if (n2 <= 32) return launch_grouped_ps<32, P>(probs, nprob, errflag, s, why);
+  if (n2 <= 64) return launch_grouped_ps<64, P>(probs, nprob, errflag, s, why);
+  if (n2 <= 128) return launch_grouped_ps<128, P>(probs, nprob, errflag, s, why);
+  return launch_grouped_ps<256, P>(probs, nprob, errflag, s, why);
 }
 
 template <int BN>
@@ -435,6 +732,12 @@ cudaError_t launch_tc_gemm_grouped(const TcGemmArgs* probs, int nprob, int* errf
     maxn2 = std::max(maxn2, 2 * a.N);
   }
   if (nprob == 0) return cudaSuccess;
+  const int P = probs[0].a_planes;
+  bool planes_ok = P == 2 || P == 3;
+  for (int q = 0; q < nprob; ++q) planes_ok = planes_ok && probs[q].a_planes == P && probs[q].b_planes == P;
+  if (tc_variant() == 1 && planes_ok)
+    return P == 3 ? launch_grouped_ps_bn<3>(probs, nprob, maxn2, errflag, s, why)
+                  : launch_grouped_ps_bn<2>(probs, nprob, maxn2, errflag, s, why);
   if (maxn2 <= 32) return launch_grouped_bn<32>(probs, nprob, errflag, s, why);
   if (maxn2 <= 64) return launch_grouped_bn<64>(probs, nprob, errflag, s, why);
   if (maxn2 <= 128) return launch_grouped_bn<128>(probs, nprob, errflag, s, why);
@@ -457,6 +760,9 @@ cudaError_t launch_tc_gemm(const TcGemmArgs& a, int* errflag, cudaStream_t s, st
     return cudaErrorInvalidValue;
   }
   const int64_t n2 = 2 * a.N;
+  const bool planes_ok = a.a_planes == a.b_planes && (a.a_planes == 2 || a.a_planes == 3);
+  if (tc_variant() == 1 && planes_ok)
+    return a.a_planes == 3 ? launch_ps_bn<3>(a, n2, errflag, s, why) : launch_ps_bn<2>(a, n2, errflag, s, why);
   if (n2 <= 32) return launch_bn<32>(a, errflag, s, why);
   if (n2 <= 64) return launch_bn<64>(a, errflag, s, why);
   if (n2 <= 128) return launch_bn<128>(a, errflag, s, why);

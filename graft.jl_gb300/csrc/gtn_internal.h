@@ -111,6 +111,10 @@ struct DevGatherJob {
   int nplanes;   // > 0: bf16 slice planes (row pitch 2*ld), else complex
   int dst_is64;  // complex output element type
   int tiles_m, m_fast;
+  int tks;                       // log2 of the tile width in K (tile = (1024 >> tks) x (1 << tks))
+  int fast_m;                    // M digits by 32-bit multiply-shift division (M < 2^31)
+  uint32_t m_mag[GTN_MAXG];      // round-up multipliers of mg.dim (Granlund-Montgomery)
+  uint32_t m_sh[GTN_MAXG];
 };
 void finish_dev_gather_job(DevGatherJob* J);
 cudaError_t launch_block_gather(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
@@ -140,6 +144,10 @@ struct GemmJob {
   int64_t M, N, K;
 };
 cudaError_t launch_gemm_simt_grouped(const GemmJob* jobs, int njobs, int is64, cudaStream_t s);
+// Skinny grouped GEMM (same contraction) for N <= 32; every job must pass gemm_skinny_fits.
+constexpr int kSkinnyMaxSmem = 96 * 1024;
+cudaError_t launch_gemm_skinny_grouped(const GemmJob* jobs, int njobs, int is64, cudaStream_t s);
+bool gemm_skinny_fits(int64_t N, int64_t K, int is64);
 
 // ---- tcgen05 GEMM (gtn_gemm_tc.cu) ---------------------------------------------------
 // Real GEMM on bf16 slice planes: C (complex fp32, [N][M]) from A planes [P][M][2Kp] and
@@ -173,6 +181,8 @@ cudaError_t launch_conj_inplace(double2* x, int64_t n, cudaStream_t s);
 cudaError_t launch_transpose_c128(const double2* in, int64_t rows, int64_t cols, double2* out,
                                   cudaStream_t s);  // out[c][r] = in[r][c]
 cudaError_t launch_zero_lower(double2* R, int64_t rows, int64_t cols, cudaStream_t s);
+cudaError_t launch_row_norms(const double2* A, int64_t rows, int64_t cols, double* out, cudaStream_t s);
+cudaError_t launch_row_phase_conj(double2* A, int64_t rows, int64_t cols, const double2* ph, cudaStream_t s);
 cudaError_t launch_diag_scale(double2* A, int64_t rows, int64_t cols, const double* d, int side,
                               cudaStream_t s);
 int multidot_blocks(gtn_ctx ctx);

@@ -273,9 +273,66 @@ __global__ void __launch_bounds__(256) small_grouped_kernel(const __grid_constan
                             static_cast<T*>(J.C), b - g.blk_start[p], g.blk_start[p + 1] - g.blk_start[p]);
 }
 
+// Row offset by 32-bit multiply-shift division: q = floor(i / d) = umulhi(i, mag) >> sh
+// for i < 2^31, with mag = floor(2^(31+l) / d) + 1, l = ceil(log2 d), sh = l - 1 (the
+// round-up method of Granlund and Montgomery, PLDI 1994, exact since mag*d - 2^(31+l) <= 2^l).
+__device__ __forceinline__ int64_t decompose_fast(int64_t m, const DevGatherJob& J) {
+  uint32_t i = (uint32_t)m;
+  int64_t off = 0;
+#pragma unroll 1
+  for (int j = J.mg.n - 1; j >= 0; --j) {
+    const uint32_t d = (uint32_t)J.mg.dim[j];
+    const uint32_t q = d == 1u ? i : (__umulhi(i, J.m_mag[j]) >> J.m_sh[j]);
+    off += (int64_t)(i - q * d) * J.mg.str[j];
+    i = q;
+  }
+  return off;
+}
+
+// Adaptive block-move tile: (1024 >> tks) rows x (1 << tks) columns, so that narrow
+// coupled-charge blocks (K of a few elements) still move 1024 elements per CTA.  The
+// shared tile is skewed by one element every 32 to spread the transposed accesses.
+template <typename Tin, class Writer>
+__device__ __forceinline__ void gather_tile_adaptive(const Tin* __restrict__ T, const DevGatherJob& J,
+                                                     const Writer& w, int64_t m0, int64_t k0) {
+  __shared__ int64_t offM[1024];
+  __shared__ int64_t offK[32];
+  __shared__ Tin tile[1024 + 32];
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  const int tks = J.tks, TK = 1 << tks, TM = 1024 >> tks;
+  for (int i = tid; i < TM; i += 256) {
+    const int64_t m = m0 + i;
+    offM[i] = m < J.M ? (J.fast_m ? decompose_fast(m, J) : decompose(m, J.mg)) : 0;
+  }
+  if (tid < TK) {
+    const int64_t k = k0 + tid;
+    offK[tid] = k < J.K ? decompose(k, J.kg) : 0;
+  }
+  __syncthreads();
+  for (int e = tid; e < 1024; e += 256) {
+    int im, ik;
+    if (J.m_fast) {
+      im = e & (TM - 1);
+      ik = e >> (10 - tks);
+    } else {
+      ik = e & (TK - 1);
+      im = e >> tks;
+    }
+    const int64_t m = m0 + im, k = k0 + ik;
+    const int sidx = im * TK + ik;
+    tile[sidx + (sidx >> 5)] = (m < J.M && k < J.K) ? T[offM[im] + offK[ik]] : Zero<Tin>::v();
+  }
+  __syncthreads();
+  for (int e = tid; e < 1024; e += 256) {
+    const int ik = e & (TK - 1), im = e >> tks;
+    const int64_t m = m0 + im, k = k0 + ik;
+    if (m < J.M && k < J.Kw) w(m, k, tile[e + (e >> 5)]);
+  }
+}
+
 // Device-resident job table (block-sparse maps): any number of jobs in one launch; sources
 // and destinations are (buffer id, element offset) resolved against the launch's bases.
-template <typename Tin, typename Tout>
+template <typename Tin>
 __global__ void __launch_bounds__(256) block_gather_kernel(const DevGatherJob* __restrict__ jobs,
                                                            const int* __restrict__ tile_start, int njobs,
                                                            BlockBases bases) {
@@ -287,35 +344,54 @@ __global__ void __launch_bounds__(256) block_gather_kernel(const DevGatherJob* _
   }
   const DevGatherJob& J = jobs[lo];
   const int t = b - tile_start[lo];
-  const int64_t m0 = (int64_t)(t % J.tiles_m) * 32, k0 = (int64_t)(t / J.tiles_m) * 32;
+  const int64_t m0 = (int64_t)(t % J.tiles_m) * (1024 >> J.tks), k0 = (int64_t)(t / J.tiles_m) << J.tks;
   const Tin* src = static_cast<const Tin*>(bases.buf[J.src_buf]) + J.src_off;
   if (J.nplanes > 0) {
     SplitWriter w{static_cast<__nv_bfloat16*>(bases.buf[J.dst_buf]) + J.dst_off, 2 * J.ld, J.pstride, J.nplanes};
-    gather_tile<Tin, SplitWriter>(src, J.mg, J.kg, J.M, J.K, J.Kw, J.m_fast, w, m0, k0);
+    gather_tile_adaptive<Tin, SplitWriter>(src, J, w, m0, k0);
   } else if (J.dst_is64) {
     ComplexWriter<double2> w{static_cast<double2*>(bases.buf[J.dst_buf]) + J.dst_off, J.ld};
-    gather_tile<Tin, ComplexWriter<double2>>(src, J.mg, J.kg, J.M, J.K, J.Kw, J.m_fast, w, m0, k0);
+    gather_tile_adaptive<Tin, ComplexWriter<double2>>(src, J, w, m0, k0);
   } else {
     ComplexWriter<float2> w{static_cast<float2*>(bases.buf[J.dst_buf]) + J.dst_off, J.ld};
-    gather_tile<Tin, ComplexWriter<float2>>(src, J.mg, J.kg, J.M, J.K, J.Kw, J.m_fast, w, m0, k0);
+    gather_tile_adaptive<Tin, ComplexWriter<float2>>(src, J, w, m0, k0);
   }
-  (void)sizeof(Tout);
 }
 
 }  // namespace
 
 void finish_dev_gather_job(DevGatherJob* J) {
-  J->tiles_m = (int)((J->M + 31) / 32);
+  int tks = 0;
+  while (tks < 5 && (int64_t(1) << tks) < J->Kw) ++tks;
+  J->tks = tks;
+  J->tiles_m = (int)((J->M + (1024 >> tks) - 1) / (1024 >> tks));
   J->m_fast = choose_m_fast(J->mg, J->kg) ? 1 : 0;
+  J->fast_m = J->M < (int64_t(1) << 31) ? 1 : 0;
+  for (int j = 0; j < J->mg.n; ++j) {
+    const int64_t d = J->mg.dim[j];
+    if (d < 1 || d >= (int64_t(1) << 31)) {
+      J->fast_m = 0;
+      continue;
+    }
+    int l = 0;
+    while ((int64_t(1) << l) < d) ++l;
+    if (d == 1) {
+      J->m_mag[j] = 0;
+      J->m_sh[j] = 0;
+    } else {
+      J->m_mag[j] = (uint32_t)(((uint64_t)1 << (31 + l)) / (uint64_t)d + 1);
+      J->m_sh[j] = (uint32_t)(l - 1);
+    }
+  }
 }
 
 cudaError_t launch_block_gather(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
                                 const BlockBases& bases, int src_is64, cudaStream_t s) {
   if (ntiles <= 0) return cudaSuccess;
   if (src_is64)
-    block_gather_kernel<double2, double2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+    block_gather_kernel<double2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
   else
-    block_gather_kernel<float2, float2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+    block_gather_kernel<float2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
   return cudaGetLastError();
 }
 

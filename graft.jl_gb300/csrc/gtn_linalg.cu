@@ -178,10 +178,19 @@ int svd_gram(gtn_ctx ctx, cusolverDnHandle_t h, int64_t m, int64_t n, const doub
   // Vh[i][l] = sum_a Ut[i][a] A[a][l]: C[nn=i][mm=l] = sum_k X[l][k] Y[i][k], X = A^T, Y = Ut
   GTN_CUDA_TRY(ctx, launch_transpose_c128(A, m, n, At, s));
   GTN_CUDA_TRY(ctx, launch_zgemm_simt(At, Ut, Vh, n, r, m, s));
-  ctx->launches += 6;
+  // s_i = ||A^H u_i|| (absolute accuracy ~ eps * s_max instead of the eigenvalues'
+  // sqrt(eps) * s_max, so singular values of a rank-deficient A come out near zero)
+  double* dnorm = reinterpret_cast<double*>(conjA);  // conjA is no longer needed
+  GTN_CUDA_TRY(ctx, launch_row_norms(Vh, r, n, dnorm, s));
+  ctx->launches += 7;
   std::vector<double> inv(r);
-  for (int64_t i = 0; i < r; ++i) inv[i] = hs[i] > 0 ? 1.0 / hs[i] : 0.0;
-  double* dinv = reinterpret_cast<double*>(conjA);  // conjA is no longer needed
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(inv.data(), dnorm, r * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  for (int64_t i = 0; i < r; ++i) {
+    S[i] = inv[i];
+    inv[i] = inv[i] > 0 ? 1.0 / inv[i] : 0.0;
+  }
+  double* dinv = dnorm;
   GTN_CUDA_TRY(ctx, cudaMemcpyAsync(dinv, inv.data(), r * sizeof(double), cudaMemcpyHostToDevice, s));
   GTN_CUDA_TRY(ctx, launch_diag_scale(Vh, r, n, dinv, 1, s));
   ctx->launches++;
@@ -191,6 +200,55 @@ int svd_gram(gtn_ctx ctx, cusolverDnHandle_t h, int64_t m, int64_t n, const doub
 constexpr int64_t kGramMin = 384;
 
 }  // namespace
+
+// Rows of Vh (r x n, r <= n) made orthonormal.  The Gram route forms Vh = S^-1 U^H A, whose
+// rows for singular values near sqrt(eps) * s_max (or zero) lose orthogonality; a thin
+// Householder QR Vh^H = Q R restores it.  Where the rows were already orthonormal Q equals
+// them up to the phase of R's diagonal, which is put back (Vh = (Q diag(ph))^H); for the
+// rest Q completes the orthonormal set, so U S Vh changes only at the level of those
+// singular values.
+static int orthonormalize_rows(gtn_ctx ctx, int64_t r, int64_t n, double2* Vh) {
+  cudaStream_t s = ctx->stream;
+  double2 *Y = nullptr, *Q = nullptr, *R = nullptr, *ph = nullptr;
+  if (cudaMalloc(&Y, n * r * sizeof(double2)) != cudaSuccess || cudaMalloc(&Q, n * r * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&R, r * r * sizeof(double2)) != cudaSuccess || cudaMalloc(&ph, r * sizeof(double2)) != cudaSuccess) {
+    cudaFree(Y);
+    cudaFree(Q);
+    cudaFree(R);
+    return set_err(ctx, GTN_ERR_MEMORY, "svd: orthonormalisation staging");
+  }
+  int st = GTN_OK;
+  cudaError_t e = launch_transpose_c128(Vh, r, n, Y, s);
+  if (e == cudaSuccess) e = launch_conj_inplace(Y, n * r, s);
+  ctx->launches += 2;
+  if (e != cudaSuccess) st = set_err(ctx, GTN_ERR_CUDA, cudaGetErrorString(e));
+  if (st == GTN_OK) st = gtn_qr(ctx, n, r, Y, Q, R);
+  std::vector<double2> d(r);
+  if (st == GTN_OK) {
+    e = cudaMemcpy2DAsync(d.data(), sizeof(double2), R, (r + 1) * sizeof(double2), sizeof(double2), r,
+                          cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = set_err(ctx, GTN_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (st == GTN_OK) {
+    for (auto& v : d) {
+      const double a = std::hypot(v.x, v.y);
+      v = a > 0 ? make_double2(v.x / a, v.y / a) : make_double2(1.0, 0.0);
+    }
+    e = cudaMemcpyAsync(ph, d.data(), r * sizeof(double2), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_transpose_c128(Q, n, r, Vh, s);
+    if (e == cudaSuccess) e = launch_row_phase_conj(Vh, r, n, ph, s);
+    ctx->launches += 2;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = set_err(ctx, GTN_ERR_CUDA, cudaGetErrorString(e));
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(Y);
+  cudaFree(Q);
+  cudaFree(R);
+  cudaFree(ph);
+  return st;
+}
 
 extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, int64_t maxdim, double atol,
                              double rtol, double discarded_weight, void* U, double* S, void* Vh,
@@ -205,9 +263,11 @@ extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, i
   cudaStream_t s = ctx->stream;
   const int64_t k = std::min(m, n);
   if (k >= kGramMin) {
-    if (m <= n)
-      return svd_gram(ctx, h, m, n, static_cast<const double2*>(A), maxdim, atol, rtol, discarded_weight,
-                      static_cast<double2*>(U), S, static_cast<double2*>(Vh), rank, discarded);
+    if (m <= n) {
+      st = svd_gram(ctx, h, m, n, static_cast<const double2*>(A), maxdim, atol, rtol, discarded_weight,
+                    static_cast<double2*>(U), S, static_cast<double2*>(Vh), rank, discarded);
+      return st == GTN_OK ? orthonormalize_rows(ctx, *rank, n, static_cast<double2*>(Vh)) : st;
+    }
     // tall: B = A^T (n x m, wide) = U_B S Vh_B  =>  U_A = Vh_B^T, Vh_A = U_B^T
     double2* B = nullptr;
     double2 *UB = nullptr, *VB = nullptr;
@@ -221,6 +281,7 @@ extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, i
     cudaError_t e = launch_transpose_c128(static_cast<const double2*>(A), m, n, B, s);
     if (e == cudaSuccess) st = svd_gram(ctx, h, n, m, B, maxdim, atol, rtol, discarded_weight, UB, S, VB, rank, discarded);
     else st = set_err(ctx, GTN_ERR_CUDA, cudaGetErrorString(e));
+    if (st == GTN_OK) st = orthonormalize_rows(ctx, *rank, m, VB);
     if (st == GTN_OK) {
       const int64_t r = *rank;
       e = launch_transpose_c128(VB, r, m, static_cast<double2*>(U), s);       // (r x m)^T = m x r

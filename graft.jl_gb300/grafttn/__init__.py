@@ -17,7 +17,7 @@ __all__ = [
 ]
 
 
-_DEVICE_MODULES = ("device", "networks", "contractions", "solvers")
+_DEVICE_MODULES = ("device", "networks", "contractions", "solvers", "cbe", "gradients", "blocksparse", "parallel")
 
 
 def __getattr__(name):

@@ -71,6 +71,7 @@ SIGNATURES = {
     "gtn_dot": (_i, [_p, _i64, _p, _p, _pd]),
     "gtn_axpby": (_i, [_p, _i64, _d, _d, _p, _d, _d, _p]),
     "gtn_diag_scale": (_i, [_p, _i64, _i64, _pd, _i, _p]),
+    "gtn_copy2d": (_i, [_p, _i64, _i64, _p, _i64, _p, _i64]),
     "gtn_multidot_noalloc": (_i, [_p, _i64, _i, _p, _i64, _p, _p]),
 }
 

@@ -130,11 +130,113 @@ def _row_major(dims):
     return st
 
 
+def contract_statics(a, b):
+    """Host contraction of two block-sparse statics (BlockTensor, labels, data) over their
+    shared labels; the result keeps the unshared legs (a's, then b's) and every block
+    allowed by the charge rule (zero where no block pair contributes)."""
+    Ta, la, da = a
+    Tb, lb, db = b
+    shared = [l for l in la if l > 0 and l in lb]
+    ia = [la.index(l) for l in shared]
+    ib = [lb.index(l) for l in shared]
+    fa = [i for i in range(len(la)) if i not in ia]
+    fb = [i for i in range(len(lb)) if i not in ib]
+    legs = [Ta.legs[i] for i in fa] + [Tb.legs[i] for i in fb]
+    out = BlockTensor(legs, Ta.qtot + Tb.qtot)
+    byk = {}
+    for qs, shape, off in Tb.blocks:
+        byk.setdefault(tuple(qs[i] for i in ib), []).append((qs, np.asarray(db[off: off + int(np.prod(shape))]).reshape(shape)))
+    acc = {}
+    for qs, shape, off in Ta.blocks:
+        blk = np.asarray(da[off: off + int(np.prod(shape))]).reshape(shape)
+        for qb, bb in byk.get(tuple(qs[i] for i in ia), []):
+            qc = tuple(qs[i] for i in fa) + tuple(qb[i] for i in fb)
+            c = np.tensordot(blk, bb, axes=(ia, ib))
+            acc[qc] = acc[qc] + c if qc in acc else c
+    data = np.zeros(out.size, dtype=np.complex128)
+    for qs, shape, off in out.blocks:
+        if qs in acc:
+            data[off: off + int(np.prod(shape))] = acc[qs].reshape(-1)
+    return out, [la[i] for i in fa] + [lb[i] for i in fb], data
+
+
+def _dense_step_time(M, K, N):
+    """Time model of one pair step on the mixed path (the plan compiler's model)."""
+    flops = 8.0 * M * K * N
+    if K <= 64:
+        return 5e-6 + (M * K + M * N) * 8 / 5e12 + flops / 15e12
+    Kp = math.ceil(K / 32) * 32
+    return 5e-6 + flops / 200e12 + (M * K * 8 + M * 2 * Kp * 6 + M * N * 8) / 5e12
+
+
+def choose_groups(x_labels, x_dims, statics, order, max_combined=1 << 20):
+    """Partition the absorbed statics into consecutive groups (pre-contracted on the host)
+    minimising the modelled chain time on the dense shapes; returns lists of static
+    indices (1-based operand numbers)."""
+    seq = list(order[1:])
+    dims = {}
+    for l, d in zip(x_labels, x_dims):
+        dims[l] = d
+    for T, lab, _ in statics:
+        for l, leg in zip(lab, T.legs):
+            dims[l] = leg.total
+
+    def ext(group):
+        cnt = {}
+        for j in group:
+            for l in statics[j - 1][1]:
+                cnt[l] = cnt.get(l, 0) + 1
+        return [l for j in group for l in statics[j - 1][1] if not (l > 0 and cnt[l] == 2)]
+
+    def chain_time(groups):
+        LT = list(x_labels)
+        t = 0.0
+        for g in groups:
+            LS = ext(g) if len(g) > 1 else list(statics[g[0] - 1][1])
+            sh = [l for l in LT if l > 0 and l in LS]
+            M = math.prod(dims[l] for l in LT if l not in sh)
+            K = math.prod(dims[l] for l in sh)
+            N = math.prod(dims[l] for l in LS if l not in sh)
+            t += _dense_step_time(M, K, N)
+            LT = [l for l in LS if l not in sh] + [l for l in LT if l not in sh]
+        return t
+    best = [[j] for j in seq]
+    best_t = chain_time(best)
+    ns = len(seq)
+    for mask in range(1 << max(ns - 1, 0)):
+        groups, cur = [], []
+        for i, j in enumerate(seq):
+            cur.append(j)
+            if i == ns - 1 or (mask >> i) & 1:
+                groups.append(cur)
+                cur = []
+        if any(len(g) > 1 and math.prod(dims[l] for l in ext(g)) > max_combined for g in groups):
+            continue
+        t = chain_time(groups)
+        if t < 0.9 * best_t:
+            best, best_t = groups, t
+    return best
+
+
 class BlockPlan:
     """Descriptors of a block-sparse map application (host side, precision independent)."""
 
-    def __init__(self, x: BlockTensor, x_labels, statics, order):
-        """statics: list (operand order 1..) of (BlockTensor, labels, host data 1-D)."""
+    def __init__(self, x: BlockTensor, x_labels, statics, order, group=True):
+        """statics: list (operand order 1..) of (BlockTensor, labels, host data 1-D).  With
+        ``group`` small consecutive statics are pre-contracted on the host first."""
+        if group and len(order) > 2:
+            groups = choose_groups(x_labels, [l.total for l in x.legs], statics, order)
+            merged = []
+            for g in groups:
+                acc = statics[g[0] - 1]
+                for j in g[1:]:
+                    acc = contract_statics(acc, statics[j - 1])
+                merged.append(acc)
+            statics = merged
+            order = [0] + list(range(1, len(merged) + 1))
+            self.groups = groups
+        else:
+            self.groups = [[j] for j in order[1:]]
         self.x = x
         self.steps = []           # list of (gathers, gemms)
         self.B = []               # host B_q matrices

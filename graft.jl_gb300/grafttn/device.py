@@ -135,6 +135,18 @@ class Context:
               "diag_scale")
         return A2
 
+    def concat_cols(self, A, B):
+        """[A B] for row-major matrices with equal row counts."""
+        rows = A.shape[0]
+        out = self.empty((rows, A.shape[1] + B.shape[1]))
+        ld = out.shape[1]
+        check(self.lib.gtn_copy2d(self.h, rows, A.shape[1], C.c_void_p(A.data_ptr()), A.shape[1],
+                                  C.c_void_p(out.data_ptr()), ld), self.h, "copy2d")
+        if B.shape[1]:
+            check(self.lib.gtn_copy2d(self.h, rows, B.shape[1], C.c_void_p(B.data_ptr()), B.shape[1],
+                                      C.c_void_p(out.data_ptr() + 16 * A.shape[1]), ld), self.h, "copy2d")
+        return out
+
     def dot(self, x, y):
         out = (C.c_double * 2)()
         check(self.lib.gtn_dot(self.h, x.numel(), C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), out),

@@ -223,6 +223,11 @@ int gtn_axpby(gtn_ctx ctx, int64_t n, double a_re, double a_im, const void* x,
 int gtn_multidot_noalloc(void* stream, int64_t n, int J, const void* V, int64_t ldv, const void* w,
                          void* out);
 
+/* Strided 2-D copy of c128 data: dst[i*dst_ld + j] = src[i*src_ld + j] for i < rows, j < cols
+ * (column concatenation of factors, e.g. the expanded isometry [Q E] of a bond expansion). */
+int gtn_copy2d(gtn_ctx ctx, int64_t rows, int64_t cols, const void* src, int64_t src_ld, void* dst,
+               int64_t dst_ld);
+
 /* In-place diagonal scaling of a row-major rows x cols c128 matrix by real HOST factors:
  * side 0 scales column j by d[j] (U * diag(S)), side 1 scales row i by d[i] (diag(S) * Vh). */
 int gtn_diag_scale(gtn_ctx ctx, int64_t rows, int64_t cols, const double* d_host, int side, void* A);

@@ -238,6 +238,32 @@ def dense_hamiltonian(H: NNHamiltonian):
     return Hd
 
 
+def sparse_hamiltonian(H: NNHamiltonian):
+    """The same matrix as ``dense_hamiltonian`` in scipy CSR form (site 0 slowest), for
+    systems too large for a dense matrix."""
+    import scipy.sparse as sp
+    n, d = H.topo.nnodes, H.d
+
+    def embed(ops):
+        out = sp.identity(1, dtype=np.complex128, format="csr")
+        for i in range(n):
+            out = sp.kron(out, sp.csr_matrix(ops.get(i, np.eye(d, dtype=np.complex128))), format="csr")
+        return out
+    Hs = sp.csr_matrix((d ** n, d ** n), dtype=np.complex128)
+    for i, h in H.onsite.items():
+        Hs = Hs + embed({i: h})
+    for (c, p), terms in H.bonds.items():
+        for coeff, oc, op in terms:
+            Hs = Hs + coeff * embed({c: oc, p: op})
+    return Hs
+
+
+def sparse_ground_energy(Hs):
+    """Lowest eigenvalue of a sparse Hermitian matrix (implicitly restarted Lanczos)."""
+    import scipy.sparse.linalg as spla
+    return float(spla.eigsh(Hs, k=1, which="SA", tol=1e-13)[0][0])
+
+
 def exact_groundstate(Hd):
     """(GraftTestUtils.jl:468-471)"""
     w, v = np.linalg.eigh((Hd + Hd.conj().T) / 2)
@@ -986,3 +1012,170 @@ def plan_macs(shapes, labels, order):
                  * math.prod(dims[l] for l in fb))
         cl = fa + fb
     return macs
+
+
+# ---------------------------------------------------------------------------
+# TDVP1_CBE with PredictorCBE (lib/GraftEvolution/src/Evolution/cbe.jl:132-148,240-259,
+# 308-352,418-589,741-806; factor frames lib/GraftContractions/src/Contractions/
+# two_site_factor_frame.jl:118-160,308-426), dense exact-SVD path
+# ---------------------------------------------------------------------------
+
+
+def _left_null(Q):
+    """Orthonormal complement of Q's columns (MatrixAlgebraKit left_null)."""
+    m, r = Q.shape
+    if r >= m:
+        return np.zeros((m, 0), dtype=Q.dtype)
+    full, _ = np.linalg.qr(np.concatenate([Q, randn_c(np.random.default_rng(0), (m, m - r))], axis=1))
+    N = full[:, r:]
+    N = N - Q @ (Q.conj().T @ N)
+    N, _ = np.linalg.qr(N)
+    return N
+
+
+def _edge_frames(psi, u, v):
+    """(active matrix ext_u x edge, partner matrix ext_v x edge, restore info) with the
+    active endpoint u (cbe.jl:270-295)."""
+    t = psi.topo
+    Au, Av = psi.tensors[u], psi.tensors[v]
+    if t.parent[u] == v:
+        ku = Au.ndim - 1                   # u's parent leg
+        kv = t.childslot(v, u)
+    else:
+        ku = t.childslot(u, v)
+        kv = Av.ndim - 1
+    act = np.moveaxis(Au, ku, -1)
+    par = np.moveaxis(Av, kv, -1)
+    return act.reshape(-1, act.shape[-1]), par.reshape(-1, par.shape[-1]), ku, kv, act.shape, par.shape
+
+
+def _site_half(cache, psi, Ws, site, peer, X, k_site):
+    """Half of the two-site sandwich at `site` (two_site_factor_frame.jl:308-403): X (the
+    site tensor in its original leg order; its leg k_site faces `peer`) contracted with W and
+    the environments of every neighbour except `peer`.  Result legs: (the external legs in
+    original order..., edge ket, edge op)."""
+    t = psi.topo
+    W = Ws[site]
+    N = X.ndim
+    order = [j for j in range(N) if j != k_site] + [k_site]
+    out_pos = {raw: j for j, raw in enumerate(order)}     # raw leg -> output position
+    K = t.nchildren(site)
+    xidx = [0] * N
+    widx = [0] * W.ndim
+    labels = [xidx, widx]
+    nxt = [0]
+
+    def fresh():
+        nxt[0] += 1
+        return nxt[0]
+    xidx[k_site] = -N
+    widx[opleg(t, site, peer)] = -(N + 1)
+    pin = fresh()
+    xidx[K] = pin
+    widx[K + 1] = pin
+    widx[K] = -(out_pos[K] + 1)
+    statics = [W]
+    for w in t.neighbors(site):
+        if w == peer:
+            continue
+        raw = stateleg(t, site, w)
+        kk, oo = fresh(), fresh()
+        xidx[raw] = kk
+        widx[opleg(t, site, w)] = oo
+        labels.append([kk, oo, -(out_pos[raw] + 1)])
+        statics.append(cache.env(psi, Ws, w, site))
+    if t.parent[site] < 0:
+        raw = N - 1
+        ka, ko = fresh(), fresh()
+        xidx[raw] = ka
+        widx[-1] = ko
+        labels.append([ka, ko, -(out_pos[raw] + 1)])
+        statics.append(root_cap())
+    return ncon([X] + statics, labels)
+
+
+def cbe_split(psi, Ws, cache, u, v, dz, maxdim, max_add=16, spawn_threshold=1e-10, neigs=2):
+    """PredictorCBE split of the active endpoint u towards v (cbe.jl:741-806): returns
+    (U as the new site tensor of u in its original leg order, the link R for the backward
+    step in (new, edge) orientation of an up move or (edge, new) of a down move)."""
+    t = psi.topo
+    act, par, ku, kv, ashape, pshape = _edge_frames(psi, u, v)
+    Q, link = np.linalg.qr(act)
+    r = Q.shape[1]
+    room = max(0, maxdim - r)
+    budget = min(room, max_add, neigs)
+    E = np.zeros((Q.shape[0], 0), dtype=Q.dtype)
+    if budget > 0 and dz != 0:
+        Na, Np = _left_null(Q), _left_null(par)
+        if Na.shape[1] > 0 and Np.shape[1] > 0:
+            Xq = np.moveaxis(Q.reshape(ashape[:-1] + (r,)), -1, ku)
+            Xp = psi.tensors[v]
+            S = _site_half(cache, psi, Ws, u, v, Xq, ku)          # ext_u..., a, o
+            T = _site_half(cache, psi, Ws, v, u, Xp, kv)          # ext_v..., b, o
+            S = S.reshape(-1, S.shape[-2], S.shape[-1])
+            T = T.reshape(-1, T.shape[-2], T.shape[-1])
+            # M = Na^H S link T^T conj(Np)  (biprojected core, contract_biprojected_two_site)
+            SL = np.einsum("xao,ab->xbo", S, link)
+            M = np.einsum("xi,xbo,ybo,yj->ij", Na.conj(), SL, T, Np.conj())
+            Uu, sv, _ = np.linalg.svd(M, full_matrices=False)
+            cutoff = spawn_threshold * max(np.linalg.norm(act), 1e-300) / abs(dz)
+            keep = [i for i in range(min(budget, len(sv))) if sv[i] >= cutoff]
+            E = Na @ Uu[:, keep]
+    Unew = np.concatenate([Q, E], axis=1)
+    R = Unew.conj().T @ act
+    Ut = np.moveaxis(Unew.reshape(ashape[:-1] + (Unew.shape[1],)), -1, ku)
+    return Ut, R
+
+
+def tdvp1_cbe_step(psi, Ws, dz, cache=None, maxdim=16, max_add=16, spawn_threshold=1e-10, neigs=2,
+                   krylovdim=30, tol=1e-12, enabled=True):
+    """Order-2 TDVP1_CBE step: the TDVP1 sweep with the link split replaced by the
+    PredictorCBE expansion (tdvp.jl:171-301 with cbe.jl:775-806)."""
+    cache = cache or EnvCache(psi.topo)
+    opts = dict(maxdim=maxdim, max_add=max_add, spawn_threshold=spawn_threshold, neigs=neigs, enabled=enabled)
+    _tdvp1_cbe_sweep(psi, Ws, dz / 2, cache, False, dz, False, krylovdim, tol, opts)
+    _tdvp1_cbe_sweep(psi, Ws, dz / 2, cache, True, None, True, krylovdim, tol, opts)
+    return cache
+
+
+def _tdvp1_cbe_sweep(psi, Ws, dz, cache, rev, terminal_dz, skip_initial, krylovdim, tol, opts):
+    t = psi.topo
+    order = t.postorder()
+    if rev:
+        order = order[::-1]
+    move_center(psi, order[0], cache.invalidate_edge)
+    for i, n in enumerate(order):
+        if not (skip_initial and i == 0):
+            sdz = terminal_dz if (terminal_dz is not None and i == len(order) - 1) else dz
+            h1 = eff_h1(cache, psi, Ws, n)
+            psi.tensors[n] = krylov_expm(h1, sdz, psi.tensors[n], krylovdim=krylovdim, tol=tol)
+            cache.invalidate_node(n)
+        if i == len(order) - 1:
+            break
+        seg = t.path_between(n, order[i + 1])
+        for j in range(1, len(seg)):
+            u, v = seg[j - 1], seg[j]
+            if (t.parent[u] == v) != rev:
+                _cbe_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol, opts)
+            else:
+                move_center(psi, v, cache.invalidate_edge)
+
+
+def _cbe_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol, opts):
+    t = psi.topo
+    if not opts["enabled"]:
+        return _evolve_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol)
+    Ut, R = cbe_split(psi, Ws, cache, u, v, dz, opts["maxdim"], opts["max_add"], opts["spawn_threshold"],
+                      opts["neigs"])
+    psi.tensors[u] = Ut
+    cache.invalidate_node(u)
+    if t.parent[u] == v:
+        k0 = eff_h0(cache, psi, Ws, u, v)
+        C = krylov_expm(k0, -dz, R, krylovdim=krylovdim, tol=tol)
+        psi.tensors[v] = absorb_on_leg(psi.tensors[v], C, t.childslot(v, u))
+    else:
+        k0 = eff_h0(cache, psi, Ws, v, u)
+        C = krylov_expm(k0, -dz, R.T, krylovdim=krylovdim, tol=tol)
+        psi.tensors[v] = np.tensordot(psi.tensors[v], C, axes=([psi.tensors[v].ndim - 1], [0]))
+    psi.center = v
+    cache.invalidate_node(v)

@@ -11,15 +11,29 @@ pytestmark = pytest.mark.gpu
 RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 1e-5, "bf16x3": 1e-3}
 
 
+@pytest.mark.parametrize("group", [True, False])
 @pytest.mark.parametrize("prec", ["fp64", "bf16x6", "bf16x3", "fp32"])
 @pytest.mark.parametrize("depth,node,D", [(3, "n2_2", 16), (4, "n3_1", 64)])
-def test_block_map_matches_dense(ctx, prec, depth, node, D):
+def test_block_map_matches_dense(ctx, prec, depth, node, D, group):
     xs, labels, order, statics, x = h2_u1_case(depth, node, D)
-    plan = B.BlockPlan(xs, labels[0], statics, order)
+    plan = B.BlockPlan(xs, labels[0], statics, order, group=group)
     ref = dense_reference(xs, labels, order, statics, x)
     bm = B.BlockEffectiveMap(ctx, plan, prec)
     y = ctx.download(bm(ctx.upload(x)))
     got = plan.y.to_dense(y)
+    assert np.linalg.norm(got - ref) <= RTOL[prec] * np.linalg.norm(ref)
+    bm.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "bf16x6"])
+def test_block_map_d128_skinny_and_tc(ctx, prec):
+    """Depth-5 binary tree at D = 128: coupled-charge problems of every kind (tcgen05,
+    skinny N < 16, narrow K < 16 block moves) in one map."""
+    xs, labels, order, statics, x = h2_u1_case(5, "n3_1", 128)
+    plan = B.BlockPlan(xs, labels[0], statics, order)
+    ref = dense_reference(xs, labels, order, statics, x)
+    bm = B.BlockEffectiveMap(ctx, plan, prec)
+    got = plan.y.to_dense(ctx.download(bm(ctx.upload(x))))
     assert np.linalg.norm(got - ref) <= RTOL[prec] * np.linalg.norm(ref)
     bm.close()
 

@@ -152,5 +152,21 @@ def test_svd_gram_path_large(ctx, m, n):
     ref = (U0[:, :300] * s0[:300]) @ V0[:, :300].conj().T
     assert np.linalg.norm((U * S) @ Vh - ref) < 1e-9 * np.linalg.norm(ref)
     assert np.allclose(U.conj().T @ U, np.eye(300), atol=1e-9)
+    assert np.allclose(Vh @ Vh.conj().T, np.eye(300), atol=1e-9)
     # discarded 2-norm from Gram eigenvalues: absolute accuracy ~ sqrt(k) * eps / s_300
     assert abs(disc - np.sqrt(np.sum(s0[300:] ** 2))) < 1e-8
+
+
+@pytest.mark.parametrize("m,n", [(512, 768), (768, 512)])
+def test_svd_gram_rank_deficient(ctx, m, n):
+    # rank 200 < maxdim: the kept directions beyond the rank still form isometries, so a
+    # two-site split of a low-rank tensor keeps a normalised state
+    rng = np.random.default_rng(9)
+    a = crandn(rng, (m, 200)) @ crandn(rng, (200, n))
+    U, S, Vh, disc = ctx.svd_trunc(ctx.upload(a), maxdim=400)
+    U, Vh = ctx.download(U), ctx.download(Vh)
+    assert len(S) == 400
+    assert np.allclose(U.conj().T @ U, np.eye(400), atol=1e-9)
+    assert np.allclose(Vh @ Vh.conj().T, np.eye(400), atol=1e-9)
+    assert np.linalg.norm((U * S) @ Vh - a) < 1e-9 * np.linalg.norm(a)
+    assert np.allclose(S[:200], np.linalg.svd(a, compute_uv=False)[:200], rtol=1e-9)

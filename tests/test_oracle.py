@@ -112,3 +112,34 @@ def test_package_specs_match_oracle(which):
             gl, go, _ = GC.h2_spec(gt, n, m, xr, K + 3, gt.nchildren(m) + 3, pn)
             ol, oo, _ = O.h2_spec(ot, n, m, xr, K + 3, gt.nchildren(m) + 3, pn)
             assert gl == ol and go == oo
+
+
+def test_tdvp1_cbe_oracle_vs_exact():
+    # test/runtests.jl:933-958: TDVP1_CBE from bond dimension 1 tracks exact evolution (1e-6),
+    # plain TDVP1 stays stuck, and disabled expansion reproduces TDVP1 exactly
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo, g=0.9)
+    Ws = O.ttno_nn(H)
+    Hd = O.dense_hamiltonian(H)
+    psi = O.random_ttns(np.random.default_rng(5), topo, 2, 1)
+    vex = O.exact_evolve(Hd, O.to_dense(psi), -1j * 0.02 * 10)
+    p = psi.copy()
+    cache = None
+    for _ in range(10):
+        cache = O.tdvp1_cbe_step(p, Ws, -1j * 0.02, cache, maxdim=16, max_add=8)
+    assert max(O.bond_dims(p)) > 1
+    assert abs(1 - abs(np.vdot(O.to_dense(p), vex))) < 1e-6
+    a, b = psi.copy(), psi.copy()
+    ca = cb = None
+    for _ in range(3):
+        ca = O.tdvp1_step(a, Ws, -1j * 0.02, ca)
+        cb = O.tdvp1_cbe_step(b, Ws, -1j * 0.02, cb, enabled=False)
+    assert np.linalg.norm(O.to_dense(a) - O.to_dense(b)) < 1e-14
+
+
+def test_sparse_hamiltonian_matches_dense():
+    topo = O.star_topology(2, 2)
+    H = O.heisenberg(topo)
+    Hs = O.sparse_hamiltonian(H)
+    assert np.abs(Hs.toarray() - O.dense_hamiltonian(H)).max() < 1e-14
+    assert abs(O.sparse_ground_energy(Hs) - O.exact_groundstate(O.dense_hamiltonian(H))[0]) < 1e-10
