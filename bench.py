@@ -30,7 +30,7 @@ for _p in (ROOT, PKG):
 
 import numpy as np  # noqa: E402
 
-METRIC = "eff_h2 applies/s at D=1024 (bin63 Heisenberg, depth3->depth2 edge), mixed bf16x6 tcgen05"
+METRIC = "eff_h2 applies/s at D=1024 (bin63 Heisenberg, depth3->depth2 edge), mixed split-product tcgen05"
 WORKLOAD = "heisenberg_bin63_d3d2_D1024_eff_h2"
 D, W_OP, d = 1024, 5, 2
 
@@ -45,6 +45,12 @@ WORKLOADS = {
     "heisenberg_bin63_d3d2_D256_eff_h2": ("binary", "n3_1", 256),
     "heisenberg_chain63_mid_D1024_eff_h2": ("mps", "site32", 1024),
 }
+
+
+DTYPES = {"bf16x6": "bf16x6 split products on tcgen05, f32 accumulate, c128 in/out",
+          "fp16x3": "fp16x3 split products (power-of-two row scales) on tcgen05, f32 accumulate, c128 in/out",
+          "bf16x3": "bf16x3 split products on tcgen05, f32 accumulate, c128 in/out"}
+PRODUCTS = {"bf16x6": 6, "fp16x3": 3, "bf16x3": 3}
 
 
 def workload_arrays(name=WORKLOAD, seed=7):
@@ -336,7 +342,7 @@ def run_ours(args, rank, world):
     flops = oracle_flops(x_shape, labels, order, statics)
     dstat = [ctx.upload(s) for s in statics]
     x = ctx.upload(theta)
-    hm = EffectiveMap(ctx, x_shape, labels, order, dstat, "bf16x6")
+    hm = EffectiveMap(ctx, x_shape, labels, order, dstat, args.precision)
     y = ctx.empty(hm.y_shape)
     assert abs(hm.flops - flops) / flops < 1e-12, (hm.flops, flops)
     stream = ctx.stream
@@ -405,7 +411,7 @@ def run_ours(args, rank, world):
     tc = by.get("tc_gemm", [1, 1e-9, 0.0])
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
     achieved = tc[2] / (tc[1] / 1000.0) / 1e12          # algorithmic complex flops / time
-    executed = achieved * 6                               # 6 bf16 products per complex MAC
+    executed = achieved * PRODUCTS[args.precision]        # slice products per complex MAC
     traffic = profile_traffic("tc_gemm", args.workload)
 
     # end to end through the C ABI with host buffers (pinned), copies inside the timed region
@@ -425,6 +431,28 @@ def run_ours(args, rank, world):
     del statics
 
     extra = {}
+    alt = {}
+    for prec in [p for p in ("bf16x6", "fp16x3") if p != args.precision]:
+        try:
+            hm2 = EffectiveMap(ctx, x_shape, labels, order, dstat, prec)
+            y2 = ctx.empty(hm2.y_shape)
+            for _ in range(2):
+                hm2.apply_into(x, y2)
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            for _ in range(args.steps):
+                hm2.apply_into(x, y2)
+            a1.record(stream)
+            torch.cuda.synchronize()
+            ctx.axpby(1.0, y2, 0.0, diff)
+            ctx.axpby(-1.0, y64, 1.0, diff)
+            alt[prec] = {"value": args.steps / (a0.elapsed_time(a1) / 1000.0), "unit": "applies/s",
+                         "rel_err_vs_fp64": ctx.norm(diff) / ctx.norm(y64)}
+            hm2.close()
+            del y2
+        except Exception as exc:
+            alt[prec] = {"error": f"{type(exc).__name__}: {exc}"}
+    extra["other_mixed_modes"] = alt
     if not args.skip_extra:
         for name, fn in (("u1_blocksparse", bench_u1), ("batched_eff_h1", bench_batched)):
             try:
@@ -436,7 +464,7 @@ def run_ours(args, rank, world):
     line = {
         "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16x6 split products on tcgen05, f32 accumulate, c128 in/out",
+        "vs_baseline": None, "dtype": DTYPES[args.precision],
         "data": "synthetic (seeded Gaussian tensors of the workload shapes)",
         "config": {"workload": args.workload, "theta_shape": list(x_shape), "bond_dim": D, "ttno_bond": W_OP,
                    "algorithmic_flops_per_apply": flops, "l2": "inputs larger than L2 (Θ and intermediates exceed 129 MB)",
@@ -505,6 +533,111 @@ def run_dmrg(args):
     print(json.dumps(out), flush=True)
 
 
+def run_grad(args):
+    """Gradient workload: XXZ (Delta = 0.7) on binary_topology(4) (31 sites) at bond
+    dimension --grad-D with per-edge couplings theta_e ~ U(0.5, 1.5): wall time of the
+    gradient with respect to every site tensor (one eff_h1 application per node) and every
+    coupling (one two-site expectation per edge), plus the identities <A_n, g_n> = E and
+    sum_e theta_e dE/dtheta_e = E and central finite differences (h = 1e-6) on a sample."""
+    import torch
+    import grafttn as G
+    from grafttn import gradients as GR
+    ctx = G.default_context(0)
+    topo = G.binary_topology(4)
+    rng = np.random.default_rng(11)
+    theta = {e: float(rng.uniform(0.5, 1.5)) for e in topo.edges()}
+    S = G.spin_ops()
+    terms = {e: [(1.0, S["X"], S["X"]), (1.0, S["Y"], S["Y"]), (0.7, S["Z"], S["Z"])] for e in topo.edges()}
+
+    def ttno(th):
+        return G.TTNO.from_hamiltonian(G.xxz(topo, th, 0.7), ctx)
+    H = ttno(theta)
+    bond = {}
+    for c in range(topo.nnodes):
+        if topo.parent[c] >= 0:
+            below = len(topo.subtree_nodes(c, topo.parent[c]))
+            bond[c] = int(min(args.grad_D, 2 ** below, 2 ** (topo.nnodes - below)))
+    psi = G.random_ttns(rng, topo, 2, bond, ctx=ctx)
+    E = GR.energy(psi, H).real
+    out = {"metric": "gradient time", "unit": "s", "topology": "binary31", "bond_dim": args.grad_D,
+           "model": "XXZ Delta=0.7, theta_e ~ U(0.5,1.5)", "energy": E, "runs": {}}
+    for prec in args.grad_precisions.split(","):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        grads = GR.site_gradients(psi, H, precision=prec)
+        torch.cuda.synchronize()
+        t_sites = time.perf_counter() - t0
+        closure = max(abs(ctx.dot(psi.tensors[n], grads[n]) - E) for n in range(topo.nnodes)) / abs(E)
+        out["runs"][prec] = {"site_gradients_s": t_sites, "max_rel_closure": closure}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g_theta = GR.coupling_gradients(psi, terms)
+    torch.cuda.synchronize()
+    out["coupling_gradients_s"] = time.perf_counter() - t0
+    out["linearity_rel_err"] = abs(sum(theta[e] * g_theta[e] for e in theta) - E) / abs(E)
+    h, fd_err = 1e-6, 0.0
+    for e in list(topo.edges())[:3]:
+        tp, tm = dict(theta), dict(theta)
+        tp[e] += h
+        tm[e] -= h
+        fd = (GR.energy(psi, ttno(tp)).real - GR.energy(psi, ttno(tm)).real) / (2 * h)
+        fd_err = max(fd_err, abs(fd - g_theta[e]) / max(1.0, abs(g_theta[e])))
+    grads = GR.site_gradients(psi, H)
+    for n in [0, topo.nnodes - 1]:
+        A = psi.tensors[n]
+        Dn = ctx.upload((rng.standard_normal(tuple(A.shape)) + 1j * rng.standard_normal(tuple(A.shape))) / 2)
+        pp, pm = psi.copy(), psi.copy()
+        pp.tensors[n] = ctx.axpby(h, Dn, 1.0, A.clone())
+        pm.tensors[n] = ctx.axpby(-h, Dn, 1.0, A.clone())
+        fd = (GR.energy(pp, H).real - GR.energy(pm, H).real) / (2 * h)
+        an = 2 * ctx.dot(Dn, grads[n]).real
+        fd_err = max(fd_err, abs(fd - an) / max(1.0, abs(an)))
+    out["max_fd_rel_err"] = fd_err
+    print(json.dumps(out), flush=True)
+
+
+def run_cbe(args):
+    """TDVP1_CBE workload: TFI (-1.0 ZZ, -0.9 X) on the complete 4-ary tree of depth 3
+    (85 sites), initial state the DMRG ground state at --cbe-maxdim (atol 1e-10) with X
+    applied on one leaf, dz = -0.05i, PredictorCBE(max_add=16), maps in --cbe-precision:
+    wall time per step, achieved bond dimensions, norm and energy drift."""
+    import torch
+    import grafttn as G
+    from grafttn import gradients as GR
+    from grafttn.cbe import TDVP1_CBE, PredictorCBE
+    ctx = G.default_context(0)
+    topo = G.kary_topology(4, 3)
+    H = G.TTNO.from_hamiltonian(G.tfi(topo, J=1.0, g=0.9), ctx)
+    psi = G.random_ttns(np.random.default_rng(1), topo, 2, 2, ctx=ctx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, Es = G.dmrg2(psi, H, G.TruncationScheme(maxdim=args.cbe_maxdim, atol=1e-10), nsweeps=args.cbe_dmrg_sweeps,
+                    precision=args.cbe_precision)
+    torch.cuda.synchronize()
+    t_dmrg = time.perf_counter() - t0
+    leaf = topo.nnodes - 1
+    X = ctx.upload(G.spin_ops()["X"])
+    psi.tensors[leaf] = ctx.contract([psi.tensors[leaf].contiguous(), X], [[1, -2], [-1, 1]])
+    E0 = GR.energy(psi, H).real
+    ev = TDVP1_CBE(PredictorCBE(max_add=16), maxdim=args.cbe_maxdim, precision=args.cbe_precision)
+    times = []
+    for _ in range(args.cbe_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev.step(psi, H, -0.05j)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    E1 = GR.energy(psi, H).real
+    dims = psi.bond_dims()
+    out = {"metric": "TDVP1_CBE step time", "unit": "s/step", "topology": "kary4_depth3 (85 sites)",
+           "model": "TFI -1.0 ZZ -0.9 X", "dz": "-0.05i", "maxdim": args.cbe_maxdim, "precision": args.cbe_precision,
+           "dmrg_groundstate": {"sweeps": args.cbe_dmrg_sweeps, "energies": Es, "seconds": t_dmrg},
+           "step_s": times, "mean_step_s": float(np.mean(times[1:] if len(times) > 1 else times)),
+           "bond_dims": {"max": int(max(dims)), "mean": float(np.mean(dims))},
+           "norm": psi.norm(), "energy_drift_rel": abs(E1 - E0) / abs(E0)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -513,12 +646,21 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--skip-extra", action="store_true", help="only the headline workload")
+    ap.add_argument("--precision", default="bf16x6", choices=sorted(DTYPES), help="mixed mode of the headline map")
     ap.add_argument("--dmrg", action="store_true", help="measure DMRG sweeps instead of map applications")
     ap.add_argument("--dmrg-topology", default="mps", choices=["mps", "binary"])
     ap.add_argument("--dmrg-sites", type=int, default=63)
     ap.add_argument("--dmrg-D", type=int, default=256)
     ap.add_argument("--dmrg-sweeps", type=int, default=2)
     ap.add_argument("--dmrg-precisions", default="bf16x6,fp64")
+    ap.add_argument("--grad", action="store_true", help="measure the gradient workload (bin31 XXZ)")
+    ap.add_argument("--grad-D", type=int, default=128)
+    ap.add_argument("--grad-precisions", default="fp64,bf16x6")
+    ap.add_argument("--cbe", action="store_true", help="measure TDVP1_CBE steps (85-site 4-ary TFI)")
+    ap.add_argument("--cbe-maxdim", type=int, default=32)
+    ap.add_argument("--cbe-steps", type=int, default=5)
+    ap.add_argument("--cbe-dmrg-sweeps", type=int, default=4)
+    ap.add_argument("--cbe-precision", default="bf16x6")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -530,9 +672,9 @@ def main():
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
         dist.init_process_group(backend)
     try:
-        if args.dmrg:
+        if args.dmrg or args.grad or args.cbe:
             if rank == 0:
-                run_dmrg(args)
+                (run_dmrg if args.dmrg else run_grad if args.grad else run_cbe)(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:

@@ -42,6 +42,8 @@ int map_run_batched(gtn_map* maps_in, int n, int precision, const double2* const
     if (m->ctx != ctx) return set_err(ctx, GTN_ERR_INVALID, "batched maps must share one context");
     maps[i] = (precision == GTN_PREC_FP64 && m->fp64_alt) ? m->fp64_alt : m;
   }
+  if (precision == GTN_PREC_FP16X3)
+    return set_err(ctx, GTN_ERR_UNSUPPORTED, "batched maps: fp16x3 planes are not implemented (use bf16x6)");
   const bool fp64 = precision == GTN_PREC_FP64;
   const bool tc = is_tc_prec(precision);
   const int P = tc ? planes_of(precision) : 0;

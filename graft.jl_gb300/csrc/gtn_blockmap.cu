@@ -160,6 +160,8 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
   if (!ctx || !out || nsteps < 1 || !step_ngather || !step_ngemm || !gathers || !gemms || !final_gathers ||
       !statics || !static_nk || !buffer_elems)
     return set_err(ctx, GTN_ERR_INVALID, "gtn_blockmap_create: null argument");
+  if (precision == GTN_PREC_FP16X3)
+    return set_err(ctx, GTN_ERR_UNSUPPORTED, "block maps: fp16x3 planes are not implemented (use bf16x6)");
   if (precision < 0 || precision > 3) return set_err(ctx, GTN_ERR_INVALID, "unknown precision");
   if (is_tc_p(precision) && !tc_gemm_supported(ctx->cc_major, ctx->cc_minor))
     return set_err(ctx, GTN_ERR_UNSUPPORTED, "tcgen05 precision modes need an sm_10x device");

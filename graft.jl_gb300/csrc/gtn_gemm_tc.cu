@@ -112,6 +112,10 @@ __device__ __forceinline__ uint64_t sdesc64(uint32_t saddr) {
 __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
+// The same with A=B=f16 (format code 0 in both operand fields).
+__host__ __device__ constexpr uint32_t idesc_f16(int m, int n) {
+  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
 
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
                                           uint32_t accumulate) {
@@ -302,10 +306,18 @@ template <int BN, int P> struct Cfg2 {
   static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
 };
 
+// Optional fp16 row scales of the slice planes (the scale that was applied to each row
+// of A and complex row of B, divided out in the epilogue).
+struct PlaneScales {
+  const float* amax;
+  const float* bmax;
+  int fp16;
+};
+
 template <int BN, int P>
 __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtensorMap* tmB, float2* __restrict__ C,
                                            int64_t M, int64_t N, int nkb, const ProdList& prods, int m0, int r0,
-                                           int* __restrict__ errflag) {
+                                           int* __restrict__ errflag, const PlaneScales& sc) {
   using CF = Cfg2<BN, P>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -365,7 +377,7 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
     }
     n_issued = it;
   } else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc = idesc_bf16(BM, BN);
+    const uint32_t idesc = sc.fp16 ? idesc_f16(BM, BN) : idesc_bf16(BM, BN);
     bool lead_started = false, corr_started = false;
     int it = 0;
     for (; it < total; ++it) {
@@ -411,6 +423,7 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
     const uint32_t taddr = tmem_d + ((uint32_t)(warp * 32) << 16);
     bool has_corr = false;
     for (int q = 0; q < prods.n; ++q) has_corr |= !(prods.a[q] == 0 && prods.b[q] == 0);
+    const float ainv = (sc.amax && m < M) ? 1.0f / fp16_row_scale(sc.amax[m]) : 1.0f;
 #pragma unroll 1
     for (int c = 0; c < BN; c += 16) {
       uint32_t v[16], w[16];
@@ -426,9 +439,11 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int64_t n = nb + j;
-          if (n < N)
-            C[n * M + m] = make_float2(__uint_as_float(v[2 * j]) + __uint_as_float(w[2 * j]),
-                                       __uint_as_float(v[2 * j + 1]) + __uint_as_float(w[2 * j + 1]));
+          if (n < N) {
+            const float f = sc.bmax ? ainv / fp16_row_scale(sc.bmax[n]) : ainv;
+            C[n * M + m] = make_float2((__uint_as_float(v[2 * j]) + __uint_as_float(w[2 * j])) * f,
+                                       (__uint_as_float(v[2 * j + 1]) + __uint_as_float(w[2 * j + 1])) * f);
+          }
         }
       }
     }
@@ -454,16 +469,19 @@ template <int BN, int P>
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_ps_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       float2* __restrict__ C, int64_t M, int64_t N, int nkb, ProdList prods,
-                      int* __restrict__ errflag) {
-  tc_tile_ps<BN, P>(&tmA, &tmB, C, M, N, nkb, prods, blockIdx.x * BM, blockIdx.y * BN, errflag);
+                      int* __restrict__ errflag, PlaneScales sc, int tiles_n) {
+  // N tile fastest: the CTAs that run together share their A tiles through L2
+  tc_tile_ps<BN, P>(&tmA, &tmB, C, M, N, nkb, prods, (int)(blockIdx.x / tiles_n) * BM, (int)(blockIdx.x % tiles_n) * BN,
+                    errflag, sc);
 }
 
 template <int BN>
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    float2* __restrict__ C, int64_t M, int64_t N, int nkb, ProdList prods,
-                   int* __restrict__ errflag) {
-  tc_tile<BN>(&tmA, &tmB, C, M, N, nkb, prods, blockIdx.x * BM, blockIdx.y * BN, errflag);
+                   int* __restrict__ errflag, int tiles_n) {
+  tc_tile<BN>(&tmA, &tmB, C, M, N, nkb, prods, (int)(blockIdx.x / tiles_n) * BM, (int)(blockIdx.x % tiles_n) * BN,
+              errflag);
 }
 
 // Many independent problems in one launch: CTA b works on tile b - tile_start[p] of the
@@ -475,9 +493,12 @@ struct GroupedTc {
   int64_t M[kTcGroupMax];
   int64_t N[kTcGroupMax];
   int nkb[kTcGroupMax];
-  int tiles_m[kTcGroupMax];
+  int tiles_n[kTcGroupMax];
   int tile_start[kTcGroupMax + 1];
+  const float* amax[kTcGroupMax];
+  const float* bmax[kTcGroupMax];
   int nprob;
+  int fp16;
   ProdList prods;
 };
 
@@ -488,8 +509,9 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_grouped_ps_kernel(const __grid
   int p = 0;
   while (p + 1 < g.nprob && g.tile_start[p + 1] <= b) ++p;
   const int t = b - g.tile_start[p];
-  const int tm = t % g.tiles_m[p], tn = t / g.tiles_m[p];
-  tc_tile_ps<BN, P>(&g.tmA[p], &g.tmB[p], g.C[p], g.M[p], g.N[p], g.nkb[p], g.prods, tm * BM, tn * BN, errflag);
+  const int tn = t % g.tiles_n[p], tm = t / g.tiles_n[p];  // N tile fastest
+  const PlaneScales sc{g.amax[p], g.bmax[p], g.fp16};
+  tc_tile_ps<BN, P>(&g.tmA[p], &g.tmB[p], g.C[p], g.M[p], g.N[p], g.nkb[p], g.prods, tm * BM, tn * BN, errflag, sc);
 }
 
 template <int BN>
@@ -499,7 +521,7 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_grouped_kernel(const __grid_co
   int p = 0;
   while (p + 1 < g.nprob && g.tile_start[p + 1] <= b) ++p;
   const int t = b - g.tile_start[p];
-  const int tm = t % g.tiles_m[p], tn = t / g.tiles_m[p];
+  const int tn = t % g.tiles_n[p], tm = t / g.tiles_n[p];  // N tile fastest
   tc_tile<BN>(&g.tmA[p], &g.tmB[p], g.C[p], g.M[p], g.N[p], g.nkb[p], g.prods, tm * BM, tn * BN, errflag);
 }
 
@@ -579,9 +601,10 @@ cudaError_t launch_ps(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::st
   const int nkb = (int)((2 * a.Kp + BKE2 - 1) / BKE2);
   const int64_t gx = (a.M + BM - 1) / BM;
   const int64_t gy = (2 * a.N + BN - 1) / BN;
-  if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
-  tc_gemm_ps_kernel<BN, P><<<dim3((unsigned)gx, (unsigned)gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb,
-                                                                                  pl, errflag);
+  if (gx * gy > 2147483647LL) return cudaErrorInvalidConfiguration;
+  const PlaneScales sc{a.a_max, a.b_max, a.fp16};
+  tc_gemm_ps_kernel<BN, P><<<(unsigned)(gx * gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb, pl, errflag, sc,
+                                                                     (int)gy);
   return cudaGetLastError();
 }
 
@@ -607,13 +630,16 @@ cudaError_t launch_grouped_ps(const TcGemmArgs* probs, int nprob, int* errflag, 
       g.C[q] = a.C;
       g.M[q] = a.M;
       g.N[q] = a.N;
+      g.amax[q] = a.a_max;
+      g.bmax[q] = a.b_max;
       g.nkb[q] = (int)((2 * a.Kp + BKE2 - 1) / BKE2);
-      g.tiles_m[q] = (int)((a.M + BM - 1) / BM);
+      g.tiles_n[q] = (int)((2 * a.N + BN - 1) / BN);
       g.tile_start[q] = tiles;
-      tiles += g.tiles_m[q] * (int)((2 * a.N + BN - 1) / BN);
+      tiles += (int)((a.M + BM - 1) / BM) * g.tiles_n[q];
     }
     g.tile_start[cnt] = tiles;
     g.nprob = cnt;
+    g.fp16 = probs[base].fp16;
     g.prods.n = probs[base].nprod;
     for (int i = 0; i < 9; ++i) {
       g.prods.a[i] = i < probs[base].nprod ? probs[base].prod_a[i] : 0;
@@ -666,9 +692,8 @@ cudaError_t launch_bn(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::st
   const int nkb = (int)((2 * a.Kp + BKE - 1) / BKE);
   const int64_t gx = (a.M + BM - 1) / BM;
   const int64_t gy = (2 * a.N + BN - 1) / BN;
-  if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
-  tc_gemm_kernel<BN><<<dim3((unsigned)gx, (unsigned)gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb,
-                                                                              pl, errflag);
+  if (gx * gy > 2147483647LL) return cudaErrorInvalidConfiguration;
+  tc_gemm_kernel<BN><<<(unsigned)(gx * gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb, pl, errflag, (int)gy);
   return cudaGetLastError();
 }
 
@@ -695,9 +720,9 @@ cudaError_t launch_grouped_bn(const TcGemmArgs* probs, int nprob, int* errflag, 
       g.M[q] = a.M;
       g.N[q] = a.N;
       g.nkb[q] = (int)((2 * a.Kp + BKE - 1) / BKE);
-      g.tiles_m[q] = (int)((a.M + BM - 1) / BM);
+      g.tiles_n[q] = (int)((2 * a.N + BN - 1) / BN);
       g.tile_start[q] = tiles;
-      tiles += g.tiles_m[q] * (int)((2 * a.N + BN - 1) / BN);
+      tiles += (int)((a.M + BM - 1) / BM) * g.tiles_n[q];
     }
     g.tile_start[cnt] = tiles;
     g.nprob = cnt;
@@ -735,7 +760,12 @@ cudaError_t launch_tc_gemm_grouped(const TcGemmArgs* probs, int nprob, int* errf
   const int P = probs[0].a_planes;
   bool planes_ok = P == 2 || P == 3;
   for (int q = 0; q < nprob; ++q) planes_ok = planes_ok && probs[q].a_planes == P && probs[q].b_planes == P;
-  if (tc_variant() == 1 && planes_ok)
+  for (int q = 0; q < nprob; ++q)
+    if (probs[q].fp16 != probs[0].fp16 || (probs[q].fp16 && !planes_ok)) {
+      if (why) *why = "tc_gemm_grouped: fp16 planes need one format and 2 or 3 planes per problem";
+      return cudaErrorInvalidValue;
+    }
+  if ((tc_variant() == 1 || probs[0].fp16) && planes_ok)
     return P == 3 ? launch_grouped_ps_bn<3>(probs, nprob, maxn2, errflag, s, why)
                   : launch_grouped_ps_bn<2>(probs, nprob, maxn2, errflag, s, why);
   if (maxn2 <= 32) return launch_grouped_bn<32>(probs, nprob, errflag, s, why);
@@ -761,7 +791,11 @@ cudaError_t launch_tc_gemm(const TcGemmArgs& a, int* errflag, cudaStream_t s, st
   }
   const int64_t n2 = 2 * a.N;
   const bool planes_ok = a.a_planes == a.b_planes && (a.a_planes == 2 || a.a_planes == 3);
-  if (tc_variant() == 1 && planes_ok)
+  if (a.fp16 && !planes_ok) {
+    if (why) *why = "tc_gemm: fp16 planes need 2 or 3 planes";
+    return cudaErrorInvalidValue;
+  }
+  if ((tc_variant() == 1 || a.fp16) && planes_ok)
     return a.a_planes == 3 ? launch_ps_bn<3>(a, n2, errflag, s, why) : launch_ps_bn<2>(a, n2, errflag, s, why);
   if (n2 <= 32) return launch_bn<32>(a, errflag, s, why);
   if (n2 <= 64) return launch_bn<64>(a, errflag, s, why);

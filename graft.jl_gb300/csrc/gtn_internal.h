@@ -3,7 +3,9 @@
 
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstdint>
+#include <cstring>
 #include <string>
 #include <vector>
 #include <memory>
@@ -76,6 +78,35 @@ cudaError_t launch_split_c64(const float2* T, const GroupSpec& mg, const GroupSp
                              __nv_bfloat16* out, cudaStream_t s);
 // Expanded real operand of a static B [N][K] (complex, row-major) for the tcgen05 path:
 // rows (n, c_out), columns (k, c_in): [[Br, -Bi], [Bi, Br]], split into bf16 planes.
+// Precomputed element offsets of a gather's rows and columns (device tables) and the
+// lane mapping of its load phase.
+struct GatherTab {
+  const int64_t* om = nullptr;
+  const int64_t* ok = nullptr;
+  int m_fast = 0;
+};
+bool gather_m_fast(const GroupSpec& mg, const GroupSpec& kg);
+cudaError_t launch_rowmax_tab(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, float* amax,
+                              cudaStream_t s);
+cudaError_t launch_split_tab(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                             int nplanes, int64_t pstride, __nv_bfloat16* out, cudaStream_t s);
+cudaError_t launch_split16_tab(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                               int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s);
+cudaError_t launch_gather_tab_to_c128(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t ldo,
+                                      double2* out, cudaStream_t s);
+// fp16 slice planes (2 planes, hi + lo) of a K-major gather, rows scaled by
+// fp16_row_scale(amax[m]); launch_rowmax_* first fills amax[m] = max_k max(|re|, |im|).
+cudaError_t launch_rowmax_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                               float* amax, cudaStream_t s);
+cudaError_t launch_rowmax_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                              float* amax, cudaStream_t s);
+cudaError_t launch_split16_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                                int64_t Kp, int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s);
+cudaError_t launch_split16_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                               int64_t Kp, int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s);
+// Static operand as fp16 planes of B' with per-complex-row maxima written to bmax[N].
+cudaError_t launch_pack_b_planes_f16(const double2* B, int64_t N, int64_t K, int64_t Kp, int64_t pstride,
+                                     __nv_bfloat16* out, float* bmax, cudaStream_t s);
 cudaError_t launch_pack_b_planes(const double2* B, int64_t N, int64_t K, int64_t Kp, int nplanes,
                                  int64_t pstride, __nv_bfloat16* out, cudaStream_t s);
 
@@ -160,7 +191,28 @@ struct TcGemmArgs {
   int a_planes, b_planes;  // number of planes stored (for the tensor-map extents)
   int nprod;
   int prod_a[9], prod_b[9];
+  // fp16 slice planes (the planes hold IEEE half bits): row m of A was scaled by
+  // fp16_row_scale(a_max[m]) and complex row n of B by fp16_row_scale(b_max[n]); the
+  // epilogue divides both out.  Null maxima and fp16 = 0 for bf16 planes.
+  int fp16 = 0;
+  const float* a_max = nullptr;
+  const float* b_max = nullptr;
 };
+
+// Power-of-two scale taking a row maximum mx into [2^14, 2^15) (fp16 holds up to 65504):
+// 2^(14 - floor(log2 mx)); 1 for a zero or subnormal maximum.
+__host__ __device__ inline float fp16_row_scale(float mx) {
+  uint32_t b;
+  memcpy(&b, &mx, 4);
+  const int e = (int)((b >> 23) & 0xffu);
+  if (e == 0) return 1.0f;
+  int te = 268 - e;  // biased exponent of 2^(14 - (e - 127))
+  te = te < 1 ? 1 : (te > 254 ? 254 : te);
+  const uint32_t o = (uint32_t)te << 23;
+  float r;
+  memcpy(&r, &o, 4);
+  return r;
+}
 cudaError_t launch_tc_gemm(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why);
 bool tc_gemm_supported(int cc_major, int cc_minor);
 // Independent problems in one launch per 56 problems (same product list for all).
@@ -202,6 +254,9 @@ struct PlanStep {
   float2* b32 = nullptr;           // [N][K] c64
   __nv_bfloat16* bpl = nullptr;    // [P][2N][2Kp] slice planes
   int bplanes = 0;
+  int bfp16 = 0;                   // planes hold fp16 slices scaled per complex row by bmax
+  float* bmax = nullptr;           // [N] row maxima of the static (fp16 planes)
+  GatherTab tab;                   // offset tables of the running tensor's [M, K] view (tc steps)
   double macs = 0;
 };
 
@@ -212,6 +267,7 @@ struct gtn_map_s {
   int64_t x_elems = 0, y_elems = 0;
   std::vector<PlanStep> steps;
   GroupSpec fin_mg, fin_kg;  // final permute of the last C into y order
+  GatherTab fin_tab;         // its offset tables
   int64_t fin_M = 0, fin_K = 0;
   bool fin_identity = false;
   double flops = 0;        // algorithmic FLOPs of the reference's env-first chain
@@ -221,6 +277,8 @@ struct gtn_map_s {
   int64_t max_t = 0;       // largest running tensor (elements)
   int64_t max_a = 0;       // largest A operand (elements, for permuted / split staging)
   int64_t max_apl = 0;     // largest split-plane staging (bf16 elements per plane * planes)
+  int64_t max_mtc = 0;     // largest M of a tensor-core step (fp16 row maxima)
+  float* amax = nullptr;   // [max_mtc] row maxima of the running operand (fp16 planes)
   // device workspace owned by the map
   void* buf0 = nullptr; void* buf1 = nullptr; void* abuf = nullptr;
   void* dx = nullptr; void* dy = nullptr;     // staging for the host-buffer entry point

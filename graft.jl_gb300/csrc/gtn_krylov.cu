@@ -229,7 +229,7 @@ extern "C" int gtn_lanczos_min(gtn_map map, void* xv, int krylovdim, double tol,
   // A mixed-precision map is accurate to ~1e-5 (bf16x6) relative: its Ritz residual cannot
   // drop below that level, so the requested tolerance is floored there; the energy is then
   // the FP64 Rayleigh quotient, whose error is quadratic in the vector error.
-  const double floor_tol = map->precision == GTN_PREC_BF16X6 ? 5e-6
+  const double floor_tol = (map->precision == GTN_PREC_BF16X6 || map->precision == GTN_PREC_FP16X3) ? 5e-6
                            : map->precision == GTN_PREC_BF16X3 ? 5e-4
                            : map->precision == GTN_PREC_FP32 ? 5e-6 : 0.0;
   tol = std::max(tol, floor_tol);

@@ -75,22 +75,35 @@ struct SplitWriter {
   }
 };
 
+// Element offsets of the rows m and columns k of a gather: decomposed through index groups,
+// or read from precomputed tables (dense maps, built once per plan step).
+struct GrpOff {
+  GroupSpec mg, kg;
+  __device__ int64_t m(int64_t i) const { return decompose(i, mg); }
+  __device__ int64_t k(int64_t i) const { return decompose(i, kg); }
+};
+struct TabOff {
+  const int64_t* __restrict__ om;
+  const int64_t* __restrict__ ok;
+  __device__ int64_t m(int64_t i) const { return om[i]; }
+  __device__ int64_t k(int64_t i) const { return ok[i]; }
+};
+
 // Tile gather: rows m (M), columns k (K valid, Kw written).  m_fast selects whether the
 // load phase maps lanes to m (the running tensor's unit-stride leg is in M) or to k.
-template <typename Tin, class Writer>
-__device__ __forceinline__ void gather_tile(const Tin* __restrict__ T, const GroupSpec& mg, const GroupSpec& kg,
-                                            int64_t M, int64_t K, int64_t Kw, int m_fast, const Writer& w,
-                                            int64_t m0, int64_t k0) {
+template <typename Tin, class Writer, class Off>
+__device__ __forceinline__ void gather_tile_o(const Tin* __restrict__ T, const Off& off, int64_t M, int64_t K,
+                                              int64_t Kw, int m_fast, const Writer& w, int64_t m0, int64_t k0) {
   __shared__ int64_t offM[32];
   __shared__ int64_t offK[32];
   __shared__ Tin tile[32][33];
   const int tx = threadIdx.x, ty = threadIdx.y;
   if (ty == 0) {
     const int64_t m = m0 + tx;
-    offM[tx] = m < M ? decompose(m, mg) : 0;
+    offM[tx] = m < M ? off.m(m) : 0;
   } else if (ty == 1) {
     const int64_t k = k0 + tx;
-    offK[tx] = k < K ? decompose(k, kg) : 0;
+    offK[tx] = k < K ? off.k(k) : 0;
   }
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
@@ -104,6 +117,67 @@ __device__ __forceinline__ void gather_tile(const Tin* __restrict__ T, const Gro
     const int64_t m = m0 + r, k = k0 + tx;
     if (m < M && k < Kw) w(m, k, tile[r][tx]);
   }
+}
+
+template <typename Tin, class Writer>
+__device__ __forceinline__ void gather_tile(const Tin* __restrict__ T, const GroupSpec& mg, const GroupSpec& kg,
+                                            int64_t M, int64_t K, int64_t Kw, int m_fast, const Writer& w,
+                                            int64_t m0, int64_t k0) {
+  gather_tile_o<Tin, Writer, GrpOff>(T, GrpOff{mg, kg}, M, K, Kw, m_fast, w, m0, k0);
+}
+
+// Table-driven tile of kTabRows x 32: every thread keeps kTabRows / 8 loads in flight
+// before the transpose (the gathers are latency-bound at 32 x 32).
+constexpr int kTabRows = 64;
+
+template <typename Tin, class Writer>
+__global__ void __launch_bounds__(256) gather_tab_kernel(const Tin* __restrict__ T, TabOff off, int64_t M,
+                                                         int64_t K, int64_t Kw, int m_fast, Writer w) {
+  __shared__ int64_t offM[kTabRows];
+  __shared__ int64_t offK[32];
+  __shared__ Tin tile[kTabRows][33];
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  const int64_t m0 = (int64_t)blockIdx.x * kTabRows, k0 = (int64_t)blockIdx.y * 32;
+  if (tid < kTabRows) {
+    offM[tid] = m0 + tid < M ? off.m(m0 + tid) : 0;
+  } else if (tid < kTabRows + 32) {
+    const int j = tid - kTabRows;
+    offK[j] = k0 + j < K ? off.k(k0 + j) : 0;
+  }
+  __syncthreads();
+  Tin v[kTabRows / 8];
+#pragma unroll
+  for (int it = 0; it < kTabRows / 8; ++it) {
+    const int e = it * 256 + tid;
+    const int im = m_fast ? (e % kTabRows) : (e >> 5);
+    const int ik = m_fast ? (e / kTabRows) : (e & 31);
+    v[it] = (m0 + im < M && k0 + ik < K) ? T[offM[im] + offK[ik]] : Zero<Tin>::v();
+  }
+#pragma unroll
+  for (int it = 0; it < kTabRows / 8; ++it) {
+    const int e = it * 256 + tid;
+    const int im = m_fast ? (e % kTabRows) : (e >> 5);
+    const int ik = m_fast ? (e / kTabRows) : (e & 31);
+    tile[im][ik] = v[it];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < kTabRows / 8; ++it) {
+    const int e = it * 256 + tid;
+    const int r = e >> 5, c = e & 31;
+    if (m0 + r < M && k0 + c < Kw) w(m0 + r, k0 + c, tile[r][c]);
+  }
+}
+
+template <typename Tin, class Writer>
+cudaError_t launch_gather_tab(const Tin* T, const int64_t* om, const int64_t* ok, int64_t M, int64_t K, int64_t Kw,
+                              int m_fast, const Writer& w, cudaStream_t s) {
+  if (M <= 0 || Kw <= 0) return cudaSuccess;
+  const int64_t gy = (Kw + 31) / 32, gx = (M + kTabRows - 1) / kTabRows;
+  if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
+  gather_tab_kernel<Tin, Writer><<<dim3((unsigned)gx, (unsigned)gy), dim3(32, 8), 0, s>>>(T, TabOff{om, ok}, M, K, Kw,
+                                                                                         m_fast, w);
+  return cudaGetLastError();
 }
 
 template <typename Tin, class Writer>
@@ -156,6 +230,114 @@ __global__ void pack_b_planes_kernel(const double2* __restrict__ B, int64_t N, i
       pr.y = s1[p];
       *reinterpret_cast<__nv_bfloat162*>(out + p * pstride + row * (2 * Kp) + 2 * k) = pr;
     }
+  }
+}
+
+// ---- fp16 slice planes: x * s = hi + lo, s a power-of-two row scale ---------------------
+__device__ __forceinline__ void split16(float x, __half* h, __half* l) {
+  *h = __float2half_rn(x);
+  *l = __float2half_rn(x - __half2float(*h));
+}
+__device__ __forceinline__ void split16(double x, __half* h, __half* l) {
+  *h = __double2half(x);
+  *l = __double2half(x - (double)__half2float(*h));
+}
+__device__ __forceinline__ float absmax2(float2 v) { return fmaxf(fabsf(v.x), fabsf(v.y)); }
+__device__ __forceinline__ float absmax2(double2 v) { return (float)fmax(fabs(v.x), fabs(v.y)); }
+
+struct Split16Writer {
+  __half* out;
+  int64_t ld2;      // row pitch in halves (= 2*Kp)
+  int64_t pstride;  // plane pitch in halves
+  const float* amax;
+  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v) const {
+    const float s = fp16_row_scale(amax[m]);
+    __half2 hi, lo;
+    split16(v.x * s, &hi.x, &lo.x);
+    split16(v.y * s, &hi.y, &lo.y);
+    __half2* row = reinterpret_cast<__half2*>(out + m * ld2 + 2 * k);
+    row[0] = hi;
+    *reinterpret_cast<__half2*>(reinterpret_cast<__half*>(row) + pstride) = lo;
+  }
+};
+
+// amax[m] = max over k of max(|re|, |im|) of the K-major gather (atomic max of the
+// non-negative float bits; amax zeroed before the launch).
+template <typename Tin, class Off>
+__global__ void __launch_bounds__(256) rowmax_kernel(const Tin* __restrict__ T, Off off, int64_t M, int64_t K,
+                                                     int m_fast, float* __restrict__ amax) {
+  constexpr int R = 64;  // rows per tile; every thread keeps R / 8 loads in flight
+  __shared__ int64_t offM[R];
+  __shared__ int64_t offK[32];
+  __shared__ float tile[R][33];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + 32 * ty;
+  const int64_t m0 = (int64_t)blockIdx.x * R, k0 = (int64_t)blockIdx.y * 32;
+  if (tid < R) {
+    offM[tid] = m0 + tid < M ? off.m(m0 + tid) : 0;
+  } else if (tid < R + 32) {
+    const int j = tid - R;
+    offK[j] = k0 + j < K ? off.k(k0 + j) : 0;
+  }
+  __syncthreads();
+  float v[R / 8];
+#pragma unroll
+  for (int it = 0; it < R / 8; ++it) {
+    const int e = it * 256 + tid;
+    const int im = m_fast ? (e % R) : (e >> 5);
+    const int ik = m_fast ? (e / R) : (e & 31);
+    v[it] = (m0 + im < M && k0 + ik < K) ? absmax2(T[offM[im] + offK[ik]]) : 0.f;
+  }
+#pragma unroll
+  for (int it = 0; it < R / 8; ++it) {
+    const int e = it * 256 + tid;
+    const int im = m_fast ? (e % R) : (e >> 5);
+    const int ik = m_fast ? (e / R) : (e & 31);
+    tile[im][ik] = v[it];
+  }
+  __syncthreads();
+  for (int r = ty; r < R; r += 8) {
+    float x = tile[r][tx];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (tx == 0 && m0 + r < M && x > 0.f) atomicMax(reinterpret_cast<unsigned int*>(amax) + m0 + r, __float_as_uint(x));
+  }
+}
+
+// bmax[n] = max over k of max(|re|, |im|) of B[n][:], one CTA per row
+__global__ void __launch_bounds__(256) bmax_kernel(const double2* __restrict__ B, int64_t K, float* __restrict__ bmax) {
+  __shared__ float red[256];
+  const double2* b = B + (int64_t)blockIdx.x * K;
+  float v = 0.f;
+  for (int64_t k = threadIdx.x; k < K; k += 256) v = fmaxf(v, absmax2(b[k]));
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) bmax[blockIdx.x] = red[0];
+}
+
+// B' = [[Br, -Bi], [Bi, Br]] as 2 fp16 planes, complex row n scaled by fp16_row_scale(bmax[n])
+__global__ void pack_b_planes_f16_kernel(const double2* __restrict__ B, int64_t N, int64_t K, int64_t Kp,
+                                         int64_t pstride, const float* __restrict__ bmax, __half* __restrict__ out) {
+  const int64_t total = 2 * N * Kp;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = idx / Kp;
+    const int64_t k = idx - row * Kp;
+    const int64_t n = row >> 1;
+    const double s = (double)fp16_row_scale(bmax[n]);
+    double v0 = 0.0, v1 = 0.0;
+    if (k < K) {
+      const double2 b = B[n * K + k];
+      if ((row & 1) == 0) { v0 = b.x; v1 = -b.y; } else { v0 = b.y; v1 = b.x; }
+    }
+    __half2 hi, lo;
+    split16(v0 * s, &hi.x, &lo.x);
+    split16(v1 * s, &hi.y, &lo.y);
+    *reinterpret_cast<__half2*>(out + row * (2 * Kp) + 2 * k) = hi;
+    *reinterpret_cast<__half2*>(out + pstride + row * (2 * Kp) + 2 * k) = lo;
   }
 }
 
@@ -488,6 +670,72 @@ cudaError_t launch_split_c64(const float2* T, const GroupSpec& mg, const GroupSp
                              int64_t K, int64_t Kp, int nplanes, int64_t pstride,
                              __nv_bfloat16* out, cudaStream_t s) {
   return launch_gather(T, mg, kg, M, K, Kp, SplitWriter{out, 2 * Kp, pstride, nplanes}, s);
+}
+template <typename Tin, class Off>
+static cudaError_t launch_rowmax(const Tin* T, const Off& off, int m_fast, int64_t M, int64_t K, float* amax,
+                                 cudaStream_t s) {
+  if (M <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(amax, 0, (size_t)M * sizeof(float), s);
+  if (e != cudaSuccess || K <= 0) return e;
+  const int64_t gx = (M + 63) / 64, gy = (K + 31) / 32;
+  if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
+  rowmax_kernel<Tin, Off><<<dim3((unsigned)gx, (unsigned)gy), dim3(32, 8), 0, s>>>(T, off, M, K, m_fast, amax);
+  return cudaGetLastError();
+}
+cudaError_t launch_rowmax_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                               float* amax, cudaStream_t s) {
+  return launch_rowmax(T, GrpOff{mg, kg}, choose_m_fast(mg, kg) ? 1 : 0, M, K, amax, s);
+}
+cudaError_t launch_rowmax_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                              float* amax, cudaStream_t s) {
+  return launch_rowmax(T, GrpOff{mg, kg}, choose_m_fast(mg, kg) ? 1 : 0, M, K, amax, s);
+}
+
+// ---- table-driven variants (offsets precomputed per plan step) --------------------------
+bool gather_m_fast(const GroupSpec& mg, const GroupSpec& kg) { return choose_m_fast(mg, kg); }
+cudaError_t launch_rowmax_tab(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, float* amax,
+                              cudaStream_t s) {
+  const TabOff off{t.om, t.ok};
+  return is64 ? launch_rowmax(static_cast<const double2*>(T), off, t.m_fast, M, K, amax, s)
+              : launch_rowmax(static_cast<const float2*>(T), off, t.m_fast, M, K, amax, s);
+}
+cudaError_t launch_split_tab(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                             int nplanes, int64_t pstride, __nv_bfloat16* out, cudaStream_t s) {
+  const SplitWriter w{out, 2 * Kp, pstride, nplanes};
+  return is64 ? launch_gather_tab(static_cast<const double2*>(T), t.om, t.ok, M, K, Kp, t.m_fast, w, s)
+              : launch_gather_tab(static_cast<const float2*>(T), t.om, t.ok, M, K, Kp, t.m_fast, w, s);
+}
+cudaError_t launch_split16_tab(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                               int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s) {
+  const Split16Writer w{reinterpret_cast<__half*>(out), 2 * Kp, pstride, amax};
+  return is64 ? launch_gather_tab(static_cast<const double2*>(T), t.om, t.ok, M, K, Kp, t.m_fast, w, s)
+              : launch_gather_tab(static_cast<const float2*>(T), t.om, t.ok, M, K, Kp, t.m_fast, w, s);
+}
+cudaError_t launch_gather_tab_to_c128(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t ldo,
+                                      double2* out, cudaStream_t s) {
+  const ComplexWriter<double2> w{out, ldo};
+  return is64 ? launch_gather_tab(static_cast<const double2*>(T), t.om, t.ok, M, K, K, t.m_fast, w, s)
+              : launch_gather_tab(static_cast<const float2*>(T), t.om, t.ok, M, K, K, t.m_fast, w, s);
+}
+cudaError_t launch_split16_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                                int64_t Kp, int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s) {
+  return launch_gather(T, mg, kg, M, K, Kp, Split16Writer{reinterpret_cast<__half*>(out), 2 * Kp, pstride, amax}, s);
+}
+cudaError_t launch_split16_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                               int64_t Kp, int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s) {
+  return launch_gather(T, mg, kg, M, K, Kp, Split16Writer{reinterpret_cast<__half*>(out), 2 * Kp, pstride, amax}, s);
+}
+cudaError_t launch_pack_b_planes_f16(const double2* B, int64_t N, int64_t K, int64_t Kp, int64_t pstride,
+                                     __nv_bfloat16* out, float* bmax, cudaStream_t s) {
+  if (N <= 0) return cudaSuccess;
+  if (N > 2147483647LL) return cudaErrorInvalidConfiguration;
+  bmax_kernel<<<(unsigned)N, 256, 0, s>>>(B, K, bmax);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int64_t total = 2 * N * Kp;
+  int64_t blocks = std::min<int64_t>(std::max<int64_t>((total + 255) / 256, 1), 152 * 32);
+  pack_b_planes_f16_kernel<<<(unsigned)blocks, 256, 0, s>>>(B, N, K, Kp, pstride, bmax, reinterpret_cast<__half*>(out));
+  return cudaGetLastError();
 }
 cudaError_t launch_pack_b_planes(const double2* B, int64_t N, int64_t K, int64_t Kp, int nplanes,
                                  int64_t pstride, __nv_bfloat16* out, cudaStream_t s) {

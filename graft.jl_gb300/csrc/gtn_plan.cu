@@ -66,8 +66,46 @@ template <typename T> cudaError_t dalloc(gtn_map map, T** p, size_t bytes) {
   return e;
 }
 
-bool is_tc(int precision) { return precision == GTN_PREC_BF16X6 || precision == GTN_PREC_BF16X3; }
+bool is_tc(int precision) {
+  return precision == GTN_PREC_BF16X6 || precision == GTN_PREC_BF16X3 || precision == GTN_PREC_FP16X3;
+}
 int nplanes_of(int precision) { return precision == GTN_PREC_BF16X6 ? 3 : 2; }
+bool is_fp16(int precision) { return precision == GTN_PREC_FP16X3; }
+
+// Device table of the element offsets of indices 0..n-1 of an index group (digits outer..
+// inner, the innermost one incremented first), owned by the map.
+cudaError_t upload_offsets(gtn_map map, const GroupSpec& g, int64_t n, const int64_t** out) {
+  std::vector<int64_t> h((size_t)std::max<int64_t>(n, 1), 0);
+  int64_t dig[GTN_MAXG] = {0};
+  int64_t off = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    h[(size_t)i] = off;
+    for (int j = g.n - 1; j >= 0; --j) {
+      ++dig[j];
+      off += g.str[j];
+      if (dig[j] < g.dim[j]) break;
+      off -= g.str[j] * g.dim[j];
+      dig[j] = 0;
+    }
+  }
+  int64_t* d = nullptr;
+  cudaError_t e = dalloc(map, &d, h.size() * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMemcpy(d, h.data(), h.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  *out = d;
+  return e;
+}
+
+// Offset tables of an [M, K] gather, or none (index-group decomposition) when they would
+// exceed 256 MiB.
+cudaError_t make_tab(gtn_map map, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K, GatherTab* t) {
+  *t = GatherTab();
+  if ((M + K) * (int64_t)sizeof(int64_t) > (int64_t(256) << 20)) return cudaSuccess;
+  cudaError_t e = upload_offsets(map, mg, M, &t->om);
+  if (e == cudaSuccess) e = upload_offsets(map, kg, K, &t->ok);
+  t->m_fast = gather_m_fast(mg, kg) ? 1 : 0;
+  if (e != cudaSuccess) *t = GatherTab();
+  return e;
+}
 
 }  // namespace
 
@@ -92,7 +130,7 @@ double est_step_time(int prec, double M, double K, double N) {
   if (small) return t + (M * K + M * N) * e / hbm + flops / (fp64 ? 1.1e12 : 15e12);
   if (fp64) return t + flops / 1.1e12 + (2 * M * K + M * N) * e / hbm;
   if (prec == GTN_PREC_FP32) return t + flops / 20e12 + (2 * M * K + M * N) * e / hbm;
-  const double rate = prec == GTN_PREC_BF16X6 ? 200e12 : 300e12;
+  const double rate = prec == GTN_PREC_BF16X6 ? 200e12 : 300e12;  // bf16x3 and fp16x3: 3 products
   const double P = prec == GTN_PREC_BF16X6 ? 3.0 : 2.0;
   const double Kp = std::ceil(K / 32.0) * 32.0;
   return t + flops / rate + (M * K * e + M * 2 * Kp * P * 2 + M * N * 8) / hbm;
@@ -164,7 +202,7 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
                const int* conj, const int* order, const void* const* statics, int precision,
                gtn_map map, bool allow_group, bool alloc_ws) {
   if (n < 2) return set_err(ctx, GTN_ERR_INVALID, "map needs the input and at least one static");
-  if (precision < 0 || precision > 3) return set_err(ctx, GTN_ERR_INVALID, "unknown precision");
+  if (precision < 0 || precision > GTN_PREC_FP16X3) return set_err(ctx, GTN_ERR_INVALID, "unknown precision");
   if (is_tc(precision) && !tc_gemm_supported(ctx->cc_major, ctx->cc_minor))
     return set_err(ctx, GTN_ERR_UNSUPPORTED, "tcgen05 precision modes need an sm_10x device");
   std::vector<std::vector<int64_t>> D(n);
@@ -360,6 +398,7 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
     if (!st.small) {
       map->max_a = std::max(map->max_a, st.M * st.K);
       if (st.tc) map->max_apl = std::max(map->max_apl, (int64_t)P * st.M * 2 * st.Kp);
+      if (st.tc) map->max_mtc = std::max(map->max_mtc, st.M);
     }
 
     // ---- pack the static: B[n][k] = S[freeS(n), shared(k)] (conj applied) -------------
@@ -390,12 +429,22 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
         st.bplanes = P;
         const int64_t pstride = 2 * st.N * 2 * st.Kp;
         e = dalloc(map, &st.bpl, (size_t)P * pstride * sizeof(__nv_bfloat16));
-        if (e == cudaSuccess) {
+        if (e == cudaSuccess && is_fp16(precision)) {
+          st.bfp16 = 1;
+          e = dalloc(map, &st.bmax, (size_t)st.N * sizeof(float));
+          if (e == cudaSuccess) e = launch_pack_b_planes_f16(st.b64, st.N, st.K, st.Kp, pstride, st.bpl, st.bmax,
+                                                             ctx->stream);
+          ctx->launches += 2;
+        } else if (e == cudaSuccess) {
           e = launch_pack_b_planes(st.b64, st.N, st.K, st.Kp, P, pstride, st.bpl, ctx->stream);
           ctx->launches++;
         }
       }
       if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("static packing: ") + cudaGetErrorString(e));
+    }
+    if (statics && st.tc) {
+      cudaError_t e = make_tab(map, st.mg, st.kg, st.M, st.K, &st.tab);
+      if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("offset tables: ") + cudaGetErrorString(e));
     }
     map->exec_flops += 8.0 * st.macs;
     map->steps.push_back(st);
@@ -425,6 +474,10 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   bool ident = true;
   for (int a = 0; a < R; ++a) ident = ident && ypos[a] == a;
   map->fin_identity = ident;
+  if (statics) {
+    cudaError_t e = make_tab(map, map->fin_mg, map->fin_kg, map->fin_M, map->fin_K, &map->fin_tab);
+    if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("offset tables: ") + cudaGetErrorString(e));
+  }
 
   // ---- an FP64 plan of its own when this plan's grouping was chosen for a mixed mode ------
   // (the Rayleigh quotient and FP64 comparisons then run the FP64-optimal chain; both plans
@@ -460,6 +513,9 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
                                             std::to_string(freeb >> 20) + " MiB");
   if (dalloc(map, &map->buf0, tbytes) != cudaSuccess || dalloc(map, &map->buf1, tbytes) != cudaSuccess ||
       dalloc(map, &map->abuf, std::max<size_t>(abytes, 256)) != cudaSuccess)
+    return set_err(ctx, GTN_ERR_MEMORY, "map workspace allocation failed");
+  if (is_fp16(precision) && map->max_mtc > 0 &&
+      dalloc(map, &map->amax, (size_t)map->max_mtc * sizeof(float)) != cudaSuccess)
     return set_err(ctx, GTN_ERR_MEMORY, "map workspace allocation failed");
   if (map->fp64_alt) {
     map->fp64_alt->buf0 = map->buf0;
@@ -516,7 +572,7 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
   const bool tc = is_tc(precision);
   if (tc) {
     for (auto& st : map->steps)
-      if (!st.small && (!st.bpl || st.bplanes != nplanes_of(precision)))
+      if (!st.small && (!st.bpl || st.bplanes != nplanes_of(precision) || st.bfp16 != (is_fp16(precision) ? 1 : 0)))
         return set_err(ctx, GTN_ERR_INVALID, "map was not created for this tcgen05 precision");
   }
   const bool fp64 = precision == GTN_PREC_FP64;
@@ -579,15 +635,42 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
       } else {
         __nv_bfloat16* Apl = static_cast<__nv_bfloat16*>(map->abuf);
         const int64_t pstride = st.M * 2 * st.Kp;
+        const bool f16 = is_fp16(precision);
         prof_begin(s);
-        if (cur64)
+        if (st.tab.om) {
+          // offsets from the step's tables
+          if (f16) {
+            e = launch_rowmax_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, map->amax, s);
+            if (e == cudaSuccess)
+              e = launch_split16_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, st.Kp, pstride, map->amax, Apl, s);
+            ctx->launches += 2;
+          } else {
+            e = launch_split_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, st.Kp, P, pstride, Apl, s);
+            ctx->launches++;
+          }
+        } else if (f16) {
+          // fp16 planes: per-row maxima first, then the scaled two-slice split
+          if (cur64)
+            e = launch_rowmax_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, map->amax, s);
+          else
+            e = launch_rowmax_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, map->amax, s);
+          if (e == cudaSuccess && cur64)
+            e = launch_split16_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
+                                    map->amax, Apl, s);
+          else if (e == cudaSuccess)
+            e = launch_split16_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
+                                   map->amax, Apl, s);
+          ctx->launches += 2;
+        } else if (cur64) {
           e = launch_split_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
                                 pstride, Apl, s);
-        else
+          ctx->launches++;
+        } else {
           e = launch_split_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
                                pstride, Apl, s);
+          ctx->launches++;
+        }
         prof_end(s, GTN_KERNEL_SPLIT, 0.0);
-        ctx->launches++;
         if (e == cudaSuccess) {
           TcGemmArgs a;
           a.A = Apl;
@@ -598,6 +681,11 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
           a.Kp = st.Kp;
           a.a_planes = P;
           a.b_planes = P;
+          if (f16) {
+            a.fp16 = 1;
+            a.a_max = map->amax;
+            a.b_max = st.bmax;
+          }
           // products accumulated small terms first
           if (P == 3) {
             const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
@@ -622,7 +710,9 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
   }
   if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("map step: ") + cudaGetErrorString(e));
   prof_begin(s);
-  if (cur64)
+  if (map->fin_tab.om)
+    e = launch_gather_tab_to_c128(cur, cur64 ? 1 : 0, map->fin_tab, map->fin_M, map->fin_K, map->fin_K, y, s);
+  else if (cur64)
     e = launch_gather_c128_to_c128(static_cast<const double2*>(cur), map->fin_mg, map->fin_kg, map->fin_M,
                                    map->fin_K, map->fin_K, y, s);
   else

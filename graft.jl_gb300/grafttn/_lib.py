@@ -24,9 +24,11 @@ PREC_FP64 = 0
 PREC_BF16X6 = 1
 PREC_BF16X3 = 2
 PREC_FP32 = 3
+PREC_FP16X3 = 4
 KERNEL_NAMES = {0: "small_contract", 1: "gather", 2: "split_bf16", 3: "zgemm_simt", 4: "cgemm_simt",
                 5: "tc_gemm", 6: "convert", 7: "output_permute"}
-PRECISIONS = {"fp64": PREC_FP64, "bf16x6": PREC_BF16X6, "bf16x3": PREC_BF16X3, "fp32": PREC_FP32}
+PRECISIONS = {"fp64": PREC_FP64, "bf16x6": PREC_BF16X6, "bf16x3": PREC_BF16X3, "fp32": PREC_FP32,
+              "fp16x3": PREC_FP16X3}
 
 # Every symbol declared in include/grafttn.h, with (restype, argtypes).
 _p = C.c_void_p

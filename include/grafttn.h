@@ -43,7 +43,9 @@ typedef enum {
   GTN_PREC_FP64 = 0,       /* complex FP64 throughout (DFMA SIMT kernels) */
   GTN_PREC_BF16X6 = 1,     /* tcgen05: 3 bf16 slices per operand, 6 products, FP32 accum */
   GTN_PREC_BF16X3 = 2,     /* tcgen05: 2 bf16 slices per operand, 3 products, FP32 accum */
-  GTN_PREC_FP32 = 3        /* complex FP32 SIMT kernels (diagnostic mode) */
+  GTN_PREC_FP32 = 3,       /* complex FP32 SIMT kernels (diagnostic mode) */
+  GTN_PREC_FP16X3 = 4      /* tcgen05: 2 fp16 slices per operand (22 bits, power-of-two row
+                              scales), 3 products, FP32 accum; dense maps only */
 } gtn_precision;
 
 typedef struct gtn_ctx_s* gtn_ctx;

@@ -6,7 +6,7 @@ from oracle import ttn_oracle as O
 
 pytestmark = pytest.mark.gpu
 
-RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 1e-5, "bf16x3": 1e-3}  # bf16x6: FP32 TMEM accumulation error grows with K
+RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 1e-5, "bf16x3": 1e-3, "fp16x3": 1e-5}  # FP32 TMEM accumulation error grows with K
 
 
 def crandn(rng, shape):
@@ -43,7 +43,7 @@ def test_contract_small_k(ctx, prec):
     assert _contract_case(ctx, rng, shapes, labels, [0, 1], prec) < RTOL[prec]
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "bf16x6", "bf16x3"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "bf16x6", "bf16x3", "fp16x3"])
 @pytest.mark.parametrize("mkn", [(130, 200, 70), (257, 1000, 129), (64, 96, 300), (1, 128, 1)])
 def test_contract_gemm(ctx, prec, mkn):
     # GEMM path (K > 64): tcgen05 for the bf16 modes, SIMT for fp64 / fp32
@@ -54,7 +54,7 @@ def test_contract_gemm(ctx, prec, mkn):
     assert _contract_case(ctx, rng, shapes, labels, [0, 1], prec) < RTOL[prec]
 
 
-@pytest.mark.parametrize("prec", ["fp64", "bf16x6"])
+@pytest.mark.parametrize("prec", ["fp64", "bf16x6", "fp16x3"])
 def test_contract_gemm_permuted(ctx, prec):
     # contracted legs not innermost in the running tensor, statics with conj
     rng = np.random.default_rng(3)
@@ -72,7 +72,7 @@ def test_tc_gemm_large(ctx):
     rng = np.random.default_rng(4)
     M, K, N = 700, 2000, 300
     from grafttn import _lib
-    for prec in ("bf16x6", "bf16x3"):
+    for prec in ("bf16x6", "bf16x3", "fp16x3"):
         assert _contract_case(ctx, rng, [(M, K), (K, N)], [[-1, 1], [1, -2]], [0, 1], prec) < RTOL[prec]
     ctx.sync()
 
@@ -88,7 +88,7 @@ def test_chain_map_all_precisions(ctx):
     labels = [[1, 2, 3, 4], [1, 5, -1], [5, -2, 2, 6], [6, -3, 3, 7], [4, 7, -4]]
     ref = O.ncon([theta, L, W1, W2, R], labels)
     from grafttn.contractions import EffectiveMap
-    for prec in ("fp64", "fp32", "bf16x6", "bf16x3"):
+    for prec in ("fp64", "fp32", "bf16x6", "bf16x3", "fp16x3"):
         hm = EffectiveMap(ctx, theta.shape, labels, [0, 1, 2, 3, 4],
                           [ctx.upload(x) for x in (L, W1, W2, R)], prec)
         y = ctx.download(hm(ctx.upload(theta)))
@@ -170,3 +170,20 @@ def test_svd_gram_rank_deficient(ctx, m, n):
     assert np.allclose(Vh @ Vh.conj().T, np.eye(400), atol=1e-9)
     assert np.linalg.norm((U * S) @ Vh - a) < 1e-9 * np.linalg.norm(a)
     assert np.allclose(S[:200], np.linalg.svd(a, compute_uv=False)[:200], rtol=1e-9)
+
+
+def test_fp16x3_wide_dynamic_range(ctx):
+    # rows whose magnitudes differ by 1e12 (power-of-two row scales keep each row's
+    # relative accuracy), plus an all-zero row
+    rng = np.random.default_rng(12)
+    M, K, N = 300, 700, 90
+    a = crandn(rng, (M, K)) * np.logspace(-6, 6, M)[:, None]
+    a[7] = 0
+    b = crandn(rng, (K, N)) * np.logspace(3, -3, N)[None, :]
+    from grafttn import _lib
+    out = ctx.download(ctx.contract([ctx.upload(a), ctx.upload(b)], [[-1, 1], [1, -2]], None, [0, 1],
+                                    _lib.PRECISIONS["fp16x3"]))
+    ref = a @ b
+    rows = np.linalg.norm(out - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+    assert np.all(rows[np.arange(M) != 7] < 1e-5)
+    assert np.all(out[7] == 0)

@@ -33,7 +33,7 @@ def test_dmrg_vs_ed_star31(ctx):
     assert abs(Es[-1] - E0) < 1e-10
 
 
-@pytest.mark.parametrize("precision", ["fp64", "bf16x6"])
+@pytest.mark.parametrize("precision", ["fp64", "bf16x6", "fp16x3"])
 def test_dmrg_star32_tfi(ctx, precision):
     # star_topology(3,2) TFI (-1.0 ZZ, -0.9 X), bond 2, maxdim 32, 10 sweeps (exactly ED-checkable)
     topo = G.star_topology(3, 2)
@@ -81,7 +81,8 @@ def test_h1_closure_and_hermitian(ctx):
     assert abs(ctx.dot(a, h1(b)) - ctx.dot(h1(a), b)) < 1e-11 * ctx.norm(a) * ctx.norm(b)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 2e-5), ("bf16x6", 2e-6), ("bf16x3", 1e-3)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 2e-5), ("bf16x6", 2e-6), ("bf16x3", 1e-3),
+                                           ("fp16x3", 4e-6)])
 def test_h2_matches_oracle_binary_heisenberg(ctx, precision, tol):
     # planned GPU map == oracle ncon on every bond of a binary tree (contraction_planning.jl:111-160)
     topo = G.binary_topology(3)
