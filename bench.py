@@ -268,8 +268,11 @@ def bench_u1(ctx, steps):
     xs, labels, order, statics, x = h2_u1_case(5, "n3_1", 1024)
     plan = B.BlockPlan(xs, labels[0], statics, order)
     dx = ctx.upload(x)
-    out = {"theta_blocks": len(xs.blocks), "theta_elems": xs.size, "algorithmic_flops_per_apply": plan.flops}
-    for prec in ("bf16x6", "fp64"):
+    out = {"theta_blocks": len(xs.blocks), "theta_elems": xs.size, "algorithmic_flops_per_apply": plan.flops,
+           "static_groups": plan.groups,
+           "sector_gemms_mkn_per_step": [sorted([int(g.M), int(g.K), int(g.N)] for g in gm) for _, gm in plan.steps]}
+    ys = {}
+    for prec in ("bf16x6", "fp16x3", "fp64"):
         bm = B.BlockEffectiveMap(ctx, plan, prec, graph=True)
         dy = ctx.empty((plan.y.size,))
         for _ in range(3):
@@ -280,14 +283,13 @@ def bench_u1(ctx, steps):
         ms = _timed(ctx.stream, lambda: bm.apply_into(dx, dy), reps)
         out[prec] = {"applies_per_s": 1000.0 / ms, "ms_per_apply": ms, "tflops": plan.flops / ms / 1e9,
                      "launches_per_apply": (ctx.launches - l0) / reps}
-        if prec == "bf16x6":
-            y_mixed = ctx.download(dy)
-        else:
-            y64 = ctx.download(dy)
+        ys[prec] = ctx.download(dy)
         out["coupled_charge_problems"] = bm.n_problems
         bm.close()
-    out["mixed_vs_fp64_rel_err"] = float(np.linalg.norm(y_mixed - y64) / np.linalg.norm(y64))
-    out["speedup_mixed_vs_fp64"] = out["bf16x6"]["applies_per_s"] / out["fp64"]["applies_per_s"]
+    y64 = ys["fp64"]
+    for prec in ("bf16x6", "fp16x3"):
+        out[prec]["rel_err_vs_fp64"] = float(np.linalg.norm(ys[prec] - y64) / np.linalg.norm(y64))
+        out[prec]["speedup_vs_fp64"] = out[prec]["applies_per_s"] / out["fp64"]["applies_per_s"]
     blocks = [U.blocks_from_flat(xs, x)] + [U.blocks_from_flat(T, d) for T, _, d in statics]
     t0 = time.perf_counter()
     y_cpu = U.flat_from_blocks(plan.y, U.ncon_blocks(blocks, labels, order))
@@ -598,9 +600,11 @@ def run_grad(args):
 
 def run_cbe(args):
     """TDVP1_CBE workload: TFI (-1.0 ZZ, -0.9 X) on the complete 4-ary tree of depth 3
-    (85 sites), initial state the DMRG ground state at --cbe-maxdim (atol 1e-10) with X
-    applied on one leaf, dz = -0.05i, PredictorCBE(max_add=16), maps in --cbe-precision:
-    wall time per step, achieved bond dimensions, norm and energy drift."""
+    (85 sites); initial state the one-site DMRG ground state at bond --cbe-maxdim / 2 (the
+    two-site blocks of the root edges, D^7 d^2 elements, do not fit for two-site DMRG at
+    these bonds) with X applied on one leaf; dz = -0.05i, PredictorCBE(max_add=16) growing
+    the bonds up to --cbe-maxdim, maps in --cbe-precision: wall time per step, achieved
+    bond dimensions, norm and energy drift."""
     import torch
     import grafttn as G
     from grafttn import gradients as GR
@@ -608,11 +612,11 @@ def run_cbe(args):
     ctx = G.default_context(0)
     topo = G.kary_topology(4, 3)
     H = G.TTNO.from_hamiltonian(G.tfi(topo, J=1.0, g=0.9), ctx)
-    psi = G.random_ttns(np.random.default_rng(1), topo, 2, 2, ctx=ctx)
+    psi = G.random_ttns(np.random.default_rng(1), topo, 2, max(1, args.cbe_maxdim // 2), ctx=ctx)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    _, Es = G.dmrg2(psi, H, G.TruncationScheme(maxdim=args.cbe_maxdim, atol=1e-10), nsweeps=args.cbe_dmrg_sweeps,
-                    precision=args.cbe_precision)
+    _, Es = G.dmrg1(psi, H, nsweeps=args.cbe_dmrg_sweeps, precision=args.cbe_precision, lanczos_tol=1e-10)
+    dims0 = psi.bond_dims()
     torch.cuda.synchronize()
     t_dmrg = time.perf_counter() - t0
     leaf = topo.nnodes - 1
@@ -633,6 +637,7 @@ def run_cbe(args):
            "model": "TFI -1.0 ZZ -0.9 X", "dz": "-0.05i", "maxdim": args.cbe_maxdim, "precision": args.cbe_precision,
            "dmrg_groundstate": {"sweeps": args.cbe_dmrg_sweeps, "energies": Es, "seconds": t_dmrg},
            "step_s": times, "mean_step_s": float(np.mean(times[1:] if len(times) > 1 else times)),
+           "bond_dims_start": {"max": int(max(dims0)), "mean": float(np.mean(dims0))},
            "bond_dims": {"max": int(max(dims)), "mean": float(np.mean(dims))},
            "norm": psi.norm(), "energy_drift_rel": abs(E1 - E0) / abs(E0)}
     print(json.dumps(out), flush=True)

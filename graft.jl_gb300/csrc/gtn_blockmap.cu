@@ -17,6 +17,10 @@ struct BMStep {
   DevGatherJob* jobs = nullptr;  // device table
   int* tiles = nullptr;          // device prefix sums
   int njobs = 0, ntiles = 0;
+  DevGatherJob* mjobs = nullptr; // fp16 row-maxima pass (before the split)
+  int* mtiles = nullptr;
+  int nmjobs = 0, nmtiles = 0;
+  int64_t amax_elems = 0;        // row maxima zeroed before that pass
   int src_is64 = 0;
   std::vector<TcGemmArgs> tcp;   // tcgen05 problems (addresses fixed at creation)
   std::vector<GemmJob> simt;     // SIMT problems
@@ -38,6 +42,8 @@ struct gtn_blockmap_s {
   std::vector<double2*> b64;
   std::vector<float2*> b32;
   std::vector<__nv_bfloat16*> bpl;
+  std::vector<float*> bmax;      // fp16 planes: per-row maxima of B_q
+  float* amax = nullptr;         // fp16 planes: row maxima of the A_q of a step
   std::vector<void*> owned;
   // graph cache keyed by (x, y)
   const void* gx = nullptr;
@@ -54,7 +60,7 @@ namespace {
 // modes): padding them to the tcgen05 tile costs more than their arithmetic.
 constexpr int64_t kTcMinK = 16, kTcMinN = 16;
 
-bool is_tc_p(int p) { return p == GTN_PREC_BF16X6 || p == GTN_PREC_BF16X3; }
+bool is_tc_p(int p) { return p == GTN_PREC_BF16X6 || p == GTN_PREC_BF16X3 || p == GTN_PREC_FP16X3; }
 int planes_p(int p) { return p == GTN_PREC_BF16X6 ? 3 : 2; }
 
 void to_groups(const gtn_block_gather& d, GroupSpec* mg, GroupSpec* kg) {
@@ -79,7 +85,15 @@ void set_prods(TcGemmArgs& a, int P) {
 }
 
 // Upload a job table with its tile prefix sums.
+cudaError_t upload_table(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, DevGatherJob** djobs, int** dtiles,
+                         int* njobs, int* ntiles);
+
 cudaError_t upload_jobs(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, BMStep* st) {
+  return upload_table(bm, jobs, &st->jobs, &st->tiles, &st->njobs, &st->ntiles);
+}
+
+cudaError_t upload_table(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, DevGatherJob** djobs, int** dtiles,
+                         int* njobs, int* ntiles) {
   std::vector<int> start(jobs.size() + 1, 0);
   int tiles = 0;
   for (size_t i = 0; i < jobs.size(); ++i) {
@@ -89,18 +103,18 @@ cudaError_t upload_jobs(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, BMStep
       tiles += jobs[i].tiles_m * (int)((jobs[i].Kw + (1 << jobs[i].tks) - 1) >> jobs[i].tks);
   }
   start[jobs.size()] = tiles;
-  st->njobs = (int)jobs.size();
-  st->ntiles = tiles;
+  *njobs = (int)jobs.size();
+  *ntiles = tiles;
   if (jobs.empty()) return cudaSuccess;
-  cudaError_t e = cudaMalloc(&st->jobs, jobs.size() * sizeof(DevGatherJob));
+  cudaError_t e = cudaMalloc(djobs, jobs.size() * sizeof(DevGatherJob));
   if (e != cudaSuccess) return e;
-  bm->owned.push_back(st->jobs);
-  e = cudaMalloc(&st->tiles, start.size() * sizeof(int));
+  bm->owned.push_back(*djobs);
+  e = cudaMalloc(dtiles, start.size() * sizeof(int));
   if (e != cudaSuccess) return e;
-  bm->owned.push_back(st->tiles);
-  e = cudaMemcpy(st->jobs, jobs.data(), jobs.size() * sizeof(DevGatherJob), cudaMemcpyHostToDevice);
+  bm->owned.push_back(*dtiles);
+  e = cudaMemcpy(*djobs, jobs.data(), jobs.size() * sizeof(DevGatherJob), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return e;
-  return cudaMemcpy(st->tiles, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice);
+  return cudaMemcpy(*dtiles, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice);
 }
 
 int run(gtn_blockmap bm, const double2* x, double2* y) {
@@ -114,10 +128,17 @@ int run(gtn_blockmap bm, const double2* x, double2* y) {
   bases.buf[2] = bm->T[0];
   bases.buf[3] = bm->T[1];
   bases.buf[4] = bm->A;
+  bases.buf[5] = bm->amax;
   cudaError_t e = cudaSuccess;
   std::string why;
   for (size_t si = 0; si < bm->steps.size() && e == cudaSuccess; ++si) {
     const BMStep& st = bm->steps[si];
+    if (st.nmjobs > 0) {
+      e = cudaMemsetAsync(bm->amax, 0, (size_t)st.amax_elems * sizeof(float), s);
+      if (e == cudaSuccess) e = launch_block_rowmax(st.mjobs, st.mtiles, st.nmjobs, st.nmtiles, bases, st.src_is64, s);
+      ctx->launches++;
+      if (e != cudaSuccess) break;
+    }
     e = launch_block_gather(st.jobs, st.tiles, st.njobs, st.ntiles, bases, st.src_is64, s);
     ctx->launches++;
     if (e == cudaSuccess && !st.tcp.empty()) {
@@ -160,9 +181,7 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
   if (!ctx || !out || nsteps < 1 || !step_ngather || !step_ngemm || !gathers || !gemms || !final_gathers ||
       !statics || !static_nk || !buffer_elems)
     return set_err(ctx, GTN_ERR_INVALID, "gtn_blockmap_create: null argument");
-  if (precision == GTN_PREC_FP16X3)
-    return set_err(ctx, GTN_ERR_UNSUPPORTED, "block maps: fp16x3 planes are not implemented (use bf16x6)");
-  if (precision < 0 || precision > 3) return set_err(ctx, GTN_ERR_INVALID, "unknown precision");
+  if (precision < 0 || precision > GTN_PREC_FP16X3) return set_err(ctx, GTN_ERR_INVALID, "unknown precision");
   if (is_tc_p(precision) && !tc_gemm_supported(ctx->cc_major, ctx->cc_minor))
     return set_err(ctx, GTN_ERR_UNSUPPORTED, "tcgen05 precision modes need an sm_10x device");
   *out = nullptr;
@@ -175,6 +194,7 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
   bm->y_elems = buffer_elems[1];
   const bool fp64 = precision == GTN_PREC_FP64;
   const bool tc = is_tc_p(precision);
+  const bool f16 = precision == GTN_PREC_FP16X3;
   const int P = tc ? planes_p(precision) : 0;
   auto fail = [&](int code, const std::string& msg) {
     cudaStreamSynchronize(ctx->stream);
@@ -209,15 +229,25 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
         return fail(GTN_ERR_CUDA, "static conversion");
       ctx->launches++;
     }
+    float* bmx = nullptr;
     if (tc) {
       const int64_t pstride = 2 * N * 2 * Kp;
       if (cudaMalloc(&bpl, (size_t)P * pstride * sizeof(__nv_bfloat16)) != cudaSuccess)
         return fail(GTN_ERR_MEMORY, "static allocation");
       bm->owned.push_back(bpl);
-      if (launch_pack_b_planes(b64, N, K, Kp, P, pstride, bpl, ctx->stream) != cudaSuccess)
-        return fail(GTN_ERR_CUDA, "static packing");
-      ctx->launches++;
+      if (f16) {
+        if (cudaMalloc(&bmx, N * sizeof(float)) != cudaSuccess) return fail(GTN_ERR_MEMORY, "static allocation");
+        bm->owned.push_back(bmx);
+        if (launch_pack_b_planes_f16(b64, N, K, Kp, pstride, bpl, bmx, ctx->stream) != cudaSuccess)
+          return fail(GTN_ERR_CUDA, "static packing");
+        ctx->launches += 2;
+      } else {
+        if (launch_pack_b_planes(b64, N, K, Kp, P, pstride, bpl, ctx->stream) != cudaSuccess)
+          return fail(GTN_ERR_CUDA, "static packing");
+        ctx->launches++;
+      }
     }
+    bm->bmax.push_back(bmx);
     bm->b64.push_back(b64);
     bm->b32.push_back(b32);
     bm->bpl.push_back(bpl);
@@ -230,6 +260,9 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
   std::vector<std::vector<size_t>> step_aoff;  // staging byte offsets per problem
   std::vector<std::vector<int64_t>> step_kp;
   std::vector<std::vector<char>> step_tc;
+  std::vector<std::vector<int64_t>> step_mbase;  // fp16: first row-maximum slot of each problem
+  std::vector<int64_t> step_mrows;
+  int64_t amax_need = 0;
   for (int s = 0; s < nsteps; ++s) {
     std::vector<gtn_block_gemm> gm(gemms + mo, gemms + mo + step_ngemm[s]);
     mo += step_ngemm[s];
@@ -250,6 +283,15 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
       off = (off + 255) / 256 * 256;
     }
     a_need = std::max(a_need, off);
+    int64_t mrows = 0;
+    std::vector<int64_t> mbase;
+    for (size_t q = 0; q < gm.size(); ++q) {
+      mbase.push_back(mrows);
+      if (use_tc[q]) mrows += gm[q].M;
+    }
+    step_mbase.push_back(mbase);
+    step_mrows.push_back(mrows);
+    amax_need = std::max(amax_need, mrows);
     step_gemms.push_back(gm);
     step_aoff.push_back(aoff);
     step_kp.push_back(kp);
@@ -266,13 +308,18 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
   bm->owned.push_back(bm->T[0]);
   bm->owned.push_back(bm->T[1]);
   bm->owned.push_back(bm->A);
+  if (f16 && amax_need > 0) {
+    if (cudaMalloc(&bm->amax, (size_t)amax_need * sizeof(float)) != cudaSuccess)
+      return fail(GTN_ERR_MEMORY, "block map workspace allocation failed");
+    bm->owned.push_back(bm->amax);
+  }
   for (int s = 0; s < nsteps; ++s) {
     BMStep st;
     const auto& gm = step_gemms[s];
-    std::vector<DevGatherJob> jobs;
+    std::vector<DevGatherJob> jobs, mjobs;
     for (int i = 0; i < step_ngather[s]; ++i) {
       const gtn_block_gather& d = gathers[go + i];
-      if (d.dst_index < 0 || d.dst_index >= (int)gm.size() || d.ng_m > GTN_MAXG || d.ng_k > GTN_MAXG ||
+      if (d.dst_index < 0 || d.dst_index >= (int)gm.size() || d.ng_m > GTN_BLOCK_MAXG || d.ng_k > GTN_BLOCK_MAXG ||
           (d.src_buf != 0 && d.src_buf != 2 && d.src_buf != 3))
         return fail(GTN_ERR_INVALID, "bad gather descriptor in step " + std::to_string(s));
       const int q = d.dst_index;
@@ -290,6 +337,11 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
         J.ld = step_kp[s][q];
         J.pstride = gm[q].M * 2 * step_kp[s][q];
         J.dst_off = (int64_t)(step_aoff[s][q] / sizeof(__nv_bfloat16)) + d.row_off * 2 * J.ld + 2 * d.col_off;
+        if (f16) {
+          J.mode = 2;
+          J.amax_off = step_mbase[s][q] + d.row_off;
+          mjobs.push_back(J);
+        }
       } else {
         J.ld = gm[q].K;
         J.dst_is64 = fp64 ? 1 : 0;
@@ -313,6 +365,10 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
           J.ld = step_kp[s][q];
           J.pstride = g.M * 2 * step_kp[s][q];
           J.dst_off = (int64_t)(step_aoff[s][q] / sizeof(__nv_bfloat16)) + 2 * g.K;
+          if (f16) {
+            J.mode = 2;
+            J.amax_off = step_mbase[s][q];
+          }
           jobs.push_back(J);
         }
         TcGemmArgs a;
@@ -325,6 +381,11 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
         a.a_planes = P;
         a.b_planes = P;
         set_prods(a, P);
+        if (f16) {
+          a.fp16 = 1;
+          a.a_max = bm->amax + step_mbase[s][q];
+          a.b_max = bm->bmax[g.b_index];
+        }
         st.tcp.push_back(a);
         bm->n_tc++;
       } else {
@@ -345,13 +406,17 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
     std::stable_sort(st.tcp.begin(), st.tcp.end(), [](const TcGemmArgs& a, const TcGemmArgs& b) { return a.Kp > b.Kp; });
     st.src_is64 = (s == 0 || fp64) ? 1 : 0;
     if (upload_jobs(bm, jobs, &st) != cudaSuccess) return fail(GTN_ERR_CUDA, "job table upload");
+    st.amax_elems = step_mrows[s];
+    if (!mjobs.empty() &&
+        upload_table(bm, mjobs, &st.mjobs, &st.mtiles, &st.nmjobs, &st.nmtiles) != cudaSuccess)
+      return fail(GTN_ERR_CUDA, "job table upload");
     bm->steps.push_back(st);
   }
   {
     std::vector<DevGatherJob> jobs;
     for (int i = 0; i < nfinal; ++i) {
       const gtn_block_gather& d = final_gathers[i];
-      if (d.ng_m > GTN_MAXG || d.ng_k > GTN_MAXG || (d.src_buf != 0 && d.src_buf != 2 && d.src_buf != 3))
+      if (d.ng_m > GTN_BLOCK_MAXG || d.ng_k > GTN_BLOCK_MAXG || (d.src_buf != 0 && d.src_buf != 2 && d.src_buf != 3))
         return fail(GTN_ERR_INVALID, "bad final gather descriptor");
       DevGatherJob J;
       std::memset(&J, 0, sizeof(J));

@@ -86,6 +86,25 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* tm,
       : "memory");
 }
 
+// The same load delivered to the shared memory (and mbarrier) at the same offset in every
+// CTA of the cluster named by cta_mask (TMA multicast within this GPU's memory).
+__device__ __forceinline__ void tma_load_3d_mc(uint32_t dst, const CUtensorMap* tm, uint64_t* bar, int x, int y,
+                                               int z, uint16_t cta_mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster "
+      "[%0], [%1, {%3, %4, %5}], [%2], %6;" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z), "h"(cta_mask)
+      : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // Shared-memory matrix descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart.
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   uint64_t d = 0;
@@ -124,6 +143,15 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
       "l"(da), "l"(db), "r"(idesc), "r"(accumulate));
+}
+// Arrive on the mbarrier at the same offset in every CTA of cta_mask when the MMAs issued
+// so far complete.
+__device__ __forceinline__ void umma_commit_mc(uint64_t* bar, uint16_t cta_mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(cta_mask)
+      : "memory");
 }
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -295,15 +323,19 @@ __device__ __forceinline__ void tc_tile(const CUtensorMap* tmA, const CUtensorMa
 // the correction products accumulate in two TMEM accumulators that the epilogue adds:
 // the corrections then never round against the leading product's running sum.
 constexpr int BKE2 = 32;
-template <int BN, int P> struct Cfg2 {
+// CPS = CTAs resident per SM: with 2, one CTA's epilogue overlaps the other's mainloop
+// (short-K steps, where the prologue and epilogue of a one-tile CTA dominate).
+template <int BN, int P, int CPS = 1> struct Cfg2 {
   static constexpr int A_PLANE = BM * BKE2 * 2;   // 8 KB
   static constexpr int B_PLANE = BN * BKE2 * 2;
   static constexpr int STAGE_BYTES = P * (A_PLANE + B_PLANE);
-  static constexpr int ST = (228352 - 2048) / STAGE_BYTES;
+  static constexpr int ST = (228352 / CPS - 2048) / STAGE_BYTES;
   static constexpr int STAGES = ST > 8 ? 8 : ST;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024;
   static constexpr uint32_t ACC_COLS = BN < 32 ? 32 : BN;   // column offset of the correction accumulator
   static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
+  static_assert(STAGES >= 2, "the operand ring needs two stages");
+  static_assert(CPS * TMEM_COLS <= 512, "TMEM columns of the resident CTAs");
 };
 
 // Optional fp16 row scales of the slice planes (the scale that was applied to each row
@@ -314,11 +346,15 @@ struct PlaneScales {
   int fp16;
 };
 
-template <int BN, int P>
+// MC: the CTA is one of a cluster pair with the same N tile and adjacent M tiles; each
+// CTA loads half of the B' tile and multicasts it to both, and both MMA threads release a
+// stage to both producers (empty barriers count two arrivals).
+template <int BN, int P, int CPS, bool MC = false>
 __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtensorMap* tmB, float2* __restrict__ C,
                                            int64_t M, int64_t N, int nkb, const ProdList& prods, int m0, int r0,
                                            int* __restrict__ errflag, const PlaneScales& sc) {
-  using CF = Cfg2<BN, P>;
+  using CF = Cfg2<BN, P, CPS>;
+  const uint32_t crank = MC ? cluster_ctarank() : 0u;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
@@ -333,7 +369,7 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
   if (threadIdx.x == 0) {
     for (int s = 0; s < CF::STAGES; ++s) {
       mbar_init(&full_bar[s], 1);
-      mbar_init(&empty_bar[s], 1);
+      mbar_init(&empty_bar[s], MC ? 2 : 1);
     }
     mbar_init(&accum_bar, 1);
     abort_flag = 0;
@@ -352,6 +388,9 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
   }
   fence_before();
   __syncthreads();
+  // the peer's multicast loads and commits target this CTA's barriers: both CTAs finish
+  // initialising them before either producer starts
+  if (MC) cluster_sync_all();
   fence_after();
   const uint32_t tmem_d = tmem_slot;
   const int total = nkb;
@@ -372,7 +411,11 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
 #pragma unroll
       for (int p = 0; p < P; ++p) {
         tma_load_3d(sa + p * CF::A_PLANE, tmA, &full_bar[s], it * BKE2, m0, p);
-        tma_load_3d(sb + p * CF::B_PLANE, tmB, &full_bar[s], it * BKE2, r0, p);
+        if (MC)
+          tma_load_3d_mc(sb + p * CF::B_PLANE + crank * (CF::B_PLANE / 2), tmB, &full_bar[s], it * BKE2,
+                         r0 + (int)crank * (BN / 2), p, (uint16_t)3);
+        else
+          tma_load_3d(sb + p * CF::B_PLANE, tmB, &full_bar[s], it * BKE2, r0, p);
       }
     }
     n_issued = it;
@@ -403,7 +446,10 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
           if (lead) lead_started = true; else corr_started = true;
         }
       }
-      umma_commit(&empty_bar[s]);
+      if (MC)
+        umma_commit_mc(&empty_bar[s], (uint16_t)3);
+      else
+        umma_commit(&empty_bar[s]);
     }
     n_consumed = it;
     umma_commit(&accum_bar);
@@ -457,6 +503,8 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
     }
   }
   __syncthreads();
+  // neither CTA of a pair leaves while the other may still deliver into its shared memory
+  if (MC) cluster_sync_all();
   if (warp == 2) {
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d),
@@ -465,13 +513,26 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
   }
 }
 
+// Cluster pairs: CTAs 2p and 2p+1 share N tile p % tiles_n and take M tiles 2 (p / tiles_n)
+// and 2 (p / tiles_n) + 1 (the second may lie past M: its loads read the fill value and its
+// epilogue stores nothing).
 template <int BN, int P>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
+    tc_gemm_mc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      float2* __restrict__ C, int64_t M, int64_t N, int nkb, ProdList prods,
+                      int* __restrict__ errflag, PlaneScales sc, int tiles_n) {
+  const int pair = (int)(blockIdx.x >> 1);
+  const int tm = 2 * (pair / tiles_n) + (int)cluster_ctarank();
+  tc_tile_ps<BN, P, 1, true>(&tmA, &tmB, C, M, N, nkb, prods, tm * BM, (pair % tiles_n) * BN, errflag, sc);
+}
+
+template <int BN, int P, int CPS>
+__global__ void __launch_bounds__(128, CPS)
     tc_gemm_ps_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       float2* __restrict__ C, int64_t M, int64_t N, int nkb, ProdList prods,
                       int* __restrict__ errflag, PlaneScales sc, int tiles_n) {
   // N tile fastest: the CTAs that run together share their A tiles through L2
-  tc_tile_ps<BN, P>(&tmA, &tmB, C, M, N, nkb, prods, (int)(blockIdx.x / tiles_n) * BM, (int)(blockIdx.x % tiles_n) * BN,
+  tc_tile_ps<BN, P, CPS>(&tmA, &tmB, C, M, N, nkb, prods, (int)(blockIdx.x / tiles_n) * BM, (int)(blockIdx.x % tiles_n) * BN,
                     errflag, sc);
 }
 
@@ -505,13 +566,15 @@ struct GroupedTc {
 template <int BN, int P>
 __global__ void __launch_bounds__(128, 1) tc_gemm_grouped_ps_kernel(const __grid_constant__ GroupedTc g,
                                                                     int* __restrict__ errflag) {
+  constexpr int CPS = 1;
   const int b = blockIdx.x;
   int p = 0;
   while (p + 1 < g.nprob && g.tile_start[p + 1] <= b) ++p;
   const int t = b - g.tile_start[p];
   const int tn = t % g.tiles_n[p], tm = t / g.tiles_n[p];  // N tile fastest
   const PlaneScales sc{g.amax[p], g.bmax[p], g.fp16};
-  tc_tile_ps<BN, P>(&g.tmA[p], &g.tmB[p], g.C[p], g.M[p], g.N[p], g.nkb[p], g.prods, tm * BM, tn * BN, errflag, sc);
+  tc_tile_ps<BN, P, CPS>(&g.tmA[p], &g.tmB[p], g.C[p], g.M[p], g.N[p], g.nkb[p], g.prods, tm * BM, tn * BN, errflag,
+                         sc);
 }
 
 template <int BN>
@@ -579,15 +642,15 @@ int tc_variant() {
   return v;
 }
 
-template <int BN, int P>
+template <int BN, int P, int CPS = 1>
 cudaError_t launch_ps(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why) {
-  using CF = Cfg2<BN, P>;
+  using CF = Cfg2<BN, P, CPS>;
   CUtensorMap tmA, tmB;
   if (!make_map(&tmA, a.A, a.Kp, a.M, a.a_planes, BM, why, BKE2)) return cudaErrorInvalidValue;
   if (!make_map(&tmB, a.B, a.Kp, 2 * a.N, a.b_planes, BN, why, BKE2)) return cudaErrorInvalidValue;
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(tc_gemm_ps_kernel<BN, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_ps_kernel<BN, P, CPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          CF::SMEM);
     if (e != cudaSuccess) return e;
     attr_set = true;
@@ -603,7 +666,7 @@ cudaError_t launch_ps(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::st
   const int64_t gy = (2 * a.N + BN - 1) / BN;
   if (gx * gy > 2147483647LL) return cudaErrorInvalidConfiguration;
   const PlaneScales sc{a.a_max, a.b_max, a.fp16};
-  tc_gemm_ps_kernel<BN, P><<<(unsigned)(gx * gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb, pl, errflag, sc,
+  tc_gemm_ps_kernel<BN, P, CPS><<<(unsigned)(gx * gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb, pl, errflag, sc,
                                                                      (int)gy);
   return cudaGetLastError();
 }
@@ -653,8 +716,60 @@ cudaError_t launch_grouped_ps(const TcGemmArgs* probs, int nprob, int* errflag, 
   return cudaSuccess;
 }
 
+template <int BN, int P>
+cudaError_t launch_mc(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why) {
+  using CF = Cfg2<BN, P, 1>;
+  CUtensorMap tmA, tmB;
+  if (!make_map(&tmA, a.A, a.Kp, a.M, a.a_planes, BM, why, BKE2)) return cudaErrorInvalidValue;
+  if (!make_map(&tmB, a.B, a.Kp, 2 * a.N, a.b_planes, BN / 2, why, BKE2)) return cudaErrorInvalidValue;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_mc_kernel<BN, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         CF::SMEM);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  ProdList pl;
+  pl.n = a.nprod;
+  for (int i = 0; i < 9; ++i) {
+    pl.a[i] = i < a.nprod ? a.prod_a[i] : 0;
+    pl.b[i] = i < a.nprod ? a.prod_b[i] : 0;
+  }
+  const int nkb = (int)((2 * a.Kp + BKE2 - 1) / BKE2);
+  const int64_t pairs_m = ((a.M + BM - 1) / BM + 1) / 2;
+  const int64_t gy = (2 * a.N + BN - 1) / BN;
+  if (2 * pairs_m * gy > 2147483647LL) return cudaErrorInvalidConfiguration;
+  const PlaneScales sc{a.a_max, a.b_max, a.fp16};
+  tc_gemm_mc_kernel<BN, P><<<(unsigned)(2 * pairs_m * gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb, pl,
+                                                                               errflag, sc, (int)gy);
+  return cudaGetLastError();
+}
+
+// Cluster-pair B multicast for long-K steps with 256-wide tiles (GTN_TC_MC=1 selects it).
+bool tc_use_mc() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("GTN_TC_MC");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
+}
+
+// Short-K steps (at most 16 k-blocks of 32) run 128-wide tiles two CTAs per SM.
+int tc_short_k_blocks() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("GTN_TC_SHORTK");
+    v = e ? atoi(e) : 16;
+  }
+  return v;
+}
+
 template <int P>
 cudaError_t launch_ps_bn(const TcGemmArgs& a, int64_t n2, int* errflag, cudaStream_t s, std::string* why) {
+  const int nkb = (int)((2 * a.Kp + BKE2 - 1) / BKE2);
+  if (n2 > 64 && nkb <= tc_short_k_blocks()) return launch_ps<128, P, 2>(a, errflag, s, why);
+  if (n2 > 128 && tc_use_mc()) return launch_mc<256, P>(a, errflag, s, why);
   if (n2 <= 32) return launch_ps<32, P>(a, errflag, s, why);
   if (n2 <= 64) return launch_ps<64, P>(a, errflag, s, why);
   if (n2 <= 128) return launch_ps<128, P>(a, errflag, s, why);

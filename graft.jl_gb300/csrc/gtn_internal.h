@@ -12,7 +12,8 @@
 
 #include "../../include/grafttn.h"
 
-#define GTN_MAXG 8
+#define GTN_MAXG 12   // index groups per gather (a two-site tensor of a 4-ary tree has 10 legs)
+#define GTN_BLOCK_MAXG 8  // index groups of a gtn_block_gather (the ABI struct's arrays)
 
 // A multi-index group: index i in [0, prod(dim)) decomposes into digits (outer..inner)
 // whose strides (in elements) give the offset into a row-major tensor.
@@ -132,7 +133,7 @@ struct SmallJob {
 cudaError_t launch_gather_grouped(const GatherJob* jobs, int njobs, int in_is64, int out_is64, cudaStream_t s);
 // Device-resident gather jobs (block-sparse maps): buffers resolved per launch.
 struct BlockBases {
-  void* buf[6];  // 0 x, 1 y, 2/3 running buffers, 4 staging, 5 unused
+  void* buf[6];  // 0 x, 1 y, 2/3 running buffers, 4 staging, 5 fp16 row maxima
 };
 struct DevGatherJob {
   GroupSpec mg, kg;
@@ -142,12 +143,16 @@ struct DevGatherJob {
   int nplanes;   // > 0: bf16 slice planes (row pitch 2*ld), else complex
   int dst_is64;  // complex output element type
   int tiles_m, m_fast;
+  int mode;                      // 0 copy / bf16 split, 2 fp16 split (row maxima: launch_block_rowmax)
+  int64_t amax_off;              // row maxima of this job's rows: (float*)bases.buf[5] + amax_off
   int tks;                       // log2 of the tile width in K (tile = (1024 >> tks) x (1 << tks))
   int fast_m;                    // M digits by 32-bit multiply-shift division (M < 2^31)
   uint32_t m_mag[GTN_MAXG];      // round-up multipliers of mg.dim (Granlund-Montgomery)
   uint32_t m_sh[GTN_MAXG];
 };
 void finish_dev_gather_job(DevGatherJob* J);
+cudaError_t launch_block_rowmax(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
+                                const BlockBases& bases, int src_is64, cudaStream_t s);
 cudaError_t launch_block_gather(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
                                 const BlockBases& bases, int src_is64, cudaStream_t s);
 cudaError_t launch_small_grouped(const SmallJob* jobs, int njobs, int is64, cudaStream_t s);

@@ -78,7 +78,8 @@ struct SplitWriter {
 // Element offsets of the rows m and columns k of a gather: decomposed through index groups,
 // or read from precomputed tables (dense maps, built once per plan step).
 struct GrpOff {
-  GroupSpec mg, kg;
+  const GroupSpec& mg;
+  const GroupSpec& kg;
   __device__ int64_t m(int64_t i) const { return decompose(i, mg); }
   __device__ int64_t k(int64_t i) const { return decompose(i, kg); }
 };
@@ -89,14 +90,24 @@ struct TabOff {
   __device__ int64_t k(int64_t i) const { return ok[i]; }
 };
 
+// Shared-memory staging of a 32 x 32 tile.  Kernels declare it once and pass it to every
+// writer variant they instantiate (a static array inside a templated device function would
+// be allocated once per instantiation).
+template <typename Tin> struct Smem32 {
+  int64_t offM[32];
+  int64_t offK[32];
+  Tin tile[32][33];
+};
+
 // Tile gather: rows m (M), columns k (K valid, Kw written).  m_fast selects whether the
 // load phase maps lanes to m (the running tensor's unit-stride leg is in M) or to k.
 template <typename Tin, class Writer, class Off>
 __device__ __forceinline__ void gather_tile_o(const Tin* __restrict__ T, const Off& off, int64_t M, int64_t K,
-                                              int64_t Kw, int m_fast, const Writer& w, int64_t m0, int64_t k0) {
-  __shared__ int64_t offM[32];
-  __shared__ int64_t offK[32];
-  __shared__ Tin tile[32][33];
+                                              int64_t Kw, int m_fast, const Writer& w, int64_t m0, int64_t k0,
+                                              Smem32<Tin>& sm) {
+  int64_t* offM = sm.offM;
+  int64_t* offK = sm.offK;
+  auto& tile = sm.tile;
   const int tx = threadIdx.x, ty = threadIdx.y;
   if (ty == 0) {
     const int64_t m = m0 + tx;
@@ -122,8 +133,8 @@ __device__ __forceinline__ void gather_tile_o(const Tin* __restrict__ T, const O
 template <typename Tin, class Writer>
 __device__ __forceinline__ void gather_tile(const Tin* __restrict__ T, const GroupSpec& mg, const GroupSpec& kg,
                                             int64_t M, int64_t K, int64_t Kw, int m_fast, const Writer& w,
-                                            int64_t m0, int64_t k0) {
-  gather_tile_o<Tin, Writer, GrpOff>(T, GrpOff{mg, kg}, M, K, Kw, m_fast, w, m0, k0);
+                                            int64_t m0, int64_t k0, Smem32<Tin>& sm) {
+  gather_tile_o<Tin, Writer, GrpOff>(T, GrpOff{mg, kg}, M, K, Kw, m_fast, w, m0, k0, sm);
 }
 
 // Table-driven tile of kTabRows x 32: every thread keeps kTabRows / 8 loads in flight
@@ -184,7 +195,8 @@ template <typename Tin, class Writer>
 __global__ void __launch_bounds__(256) gather_tile_kernel(const Tin* __restrict__ T, GroupSpec mg,
                                                           GroupSpec kg, int64_t M, int64_t K,
                                                           int64_t Kw, int m_fast, Writer w) {
-  gather_tile<Tin, Writer>(T, mg, kg, M, K, Kw, m_fast, w, (int64_t)blockIdx.x * 32, (int64_t)blockIdx.y * 32);
+  __shared__ Smem32<Tin> sm;
+  gather_tile<Tin, Writer>(T, mg, kg, M, K, Kw, m_fast, w, (int64_t)blockIdx.x * 32, (int64_t)blockIdx.y * 32, sm);
 }
 
 inline bool choose_m_fast(const GroupSpec& mg, const GroupSpec& kg) {
@@ -430,13 +442,15 @@ __global__ void __launch_bounds__(256) gather_grouped_kernel(const __grid_consta
   const GatherJob& J = g.j[p];
   const int t = b - g.tile_start[p];
   const int64_t m0 = (int64_t)(t % g.tiles_m[p]) * 32, k0 = (int64_t)(t / g.tiles_m[p]) * 32;
+  __shared__ Smem32<Tin> sm;
   if (J.nplanes > 0) {
     SplitWriter w{static_cast<__nv_bfloat16*>(J.out), 2 * (J.ld > 0 ? J.ld : J.Kw), J.pstride, J.nplanes};
-    gather_tile<Tin, SplitWriter>(static_cast<const Tin*>(J.T), J.mg, J.kg, J.M, J.K, J.Kw, g.m_fast[p], w, m0, k0);
+    gather_tile<Tin, SplitWriter>(static_cast<const Tin*>(J.T), J.mg, J.kg, J.M, J.K, J.Kw, g.m_fast[p], w, m0, k0,
+                                  sm);
   } else {
     ComplexWriter<Tout> w{static_cast<Tout*>(J.out), J.ld};
     gather_tile<Tin, ComplexWriter<Tout>>(static_cast<const Tin*>(J.T), J.mg, J.kg, J.M, J.K, J.Kw, g.m_fast[p], w,
-                                          m0, k0);
+                                          m0, k0, sm);
   }
 }
 
@@ -474,12 +488,18 @@ __device__ __forceinline__ int64_t decompose_fast(int64_t m, const DevGatherJob&
 // Adaptive block-move tile: (1024 >> tks) rows x (1 << tks) columns, so that narrow
 // coupled-charge blocks (K of a few elements) still move 1024 elements per CTA.  The
 // shared tile is skewed by one element every 32 to spread the transposed accesses.
+template <typename Tin> struct SmemA {
+  int64_t offM[1024];
+  int64_t offK[32];
+  Tin tile[1024 + 32];
+};
+
 template <typename Tin, class Writer>
 __device__ __forceinline__ void gather_tile_adaptive(const Tin* __restrict__ T, const DevGatherJob& J,
-                                                     const Writer& w, int64_t m0, int64_t k0) {
-  __shared__ int64_t offM[1024];
-  __shared__ int64_t offK[32];
-  __shared__ Tin tile[1024 + 32];
+                                                     const Writer& w, int64_t m0, int64_t k0, SmemA<Tin>& sm) {
+  int64_t* offM = sm.offM;
+  int64_t* offK = sm.offK;
+  Tin* tile = sm.tile;
   const int tid = threadIdx.x + 32 * threadIdx.y;
   const int tks = J.tks, TK = 1 << tks, TM = 1024 >> tks;
   for (int i = tid; i < TM; i += 256) {
@@ -512,6 +532,33 @@ __device__ __forceinline__ void gather_tile_adaptive(const Tin* __restrict__ T, 
   }
 }
 
+// Row maxima of an adaptive tile (fp16 split of block maps): segmented max over the TK
+// lanes of a row, one atomic max per row and tile.
+template <typename Tin>
+__device__ __forceinline__ void rowmax_tile_adaptive(const Tin* __restrict__ T, const DevGatherJob& J,
+                                                     float* __restrict__ amax, int64_t m0, int64_t k0) {
+  __shared__ int64_t offM[1024];
+  __shared__ int64_t offK[32];
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  const int tks = J.tks, TK = 1 << tks, TM = 1024 >> tks;
+  for (int i = tid; i < TM; i += 256) {
+    const int64_t m = m0 + i;
+    offM[i] = m < J.M ? (J.fast_m ? decompose_fast(m, J) : decompose(m, J.mg)) : 0;
+  }
+  if (tid < TK) {
+    const int64_t k = k0 + tid;
+    offK[tid] = k < J.K ? decompose(k, J.kg) : 0;
+  }
+  __syncthreads();
+  for (int e = tid; e < 1024; e += 256) {
+    const int ik = e & (TK - 1), im = e >> tks;
+    const int64_t m = m0 + im, k = k0 + ik;
+    float v = (m < J.M && k < J.K) ? absmax2(T[offM[im] + offK[ik]]) : 0.f;
+    for (int o = TK >> 1; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (ik == 0 && m < J.M && v > 0.f) atomicMax(reinterpret_cast<unsigned int*>(amax) + m, __float_as_uint(v));
+  }
+}
+
 // Device-resident job table (block-sparse maps): any number of jobs in one launch; sources
 // and destinations are (buffer id, element offset) resolved against the launch's bases.
 template <typename Tin>
@@ -528,19 +575,53 @@ __global__ void __launch_bounds__(256) block_gather_kernel(const DevGatherJob* _
   const int t = b - tile_start[lo];
   const int64_t m0 = (int64_t)(t % J.tiles_m) * (1024 >> J.tks), k0 = (int64_t)(t / J.tiles_m) << J.tks;
   const Tin* src = static_cast<const Tin*>(bases.buf[J.src_buf]) + J.src_off;
-  if (J.nplanes > 0) {
+  __shared__ SmemA<Tin> sm;
+  if (J.mode == 2) {
+    Split16Writer w{reinterpret_cast<__half*>(static_cast<__nv_bfloat16*>(bases.buf[J.dst_buf]) + J.dst_off), 2 * J.ld,
+                    J.pstride, static_cast<const float*>(bases.buf[5]) + J.amax_off};
+    gather_tile_adaptive<Tin, Split16Writer>(src, J, w, m0, k0, sm);
+  } else if (J.nplanes > 0) {
     SplitWriter w{static_cast<__nv_bfloat16*>(bases.buf[J.dst_buf]) + J.dst_off, 2 * J.ld, J.pstride, J.nplanes};
-    gather_tile_adaptive<Tin, SplitWriter>(src, J, w, m0, k0);
+    gather_tile_adaptive<Tin, SplitWriter>(src, J, w, m0, k0, sm);
   } else if (J.dst_is64) {
     ComplexWriter<double2> w{static_cast<double2*>(bases.buf[J.dst_buf]) + J.dst_off, J.ld};
-    gather_tile_adaptive<Tin, ComplexWriter<double2>>(src, J, w, m0, k0);
+    gather_tile_adaptive<Tin, ComplexWriter<double2>>(src, J, w, m0, k0, sm);
   } else {
     ComplexWriter<float2> w{static_cast<float2*>(bases.buf[J.dst_buf]) + J.dst_off, J.ld};
-    gather_tile_adaptive<Tin, ComplexWriter<float2>>(src, J, w, m0, k0);
+    gather_tile_adaptive<Tin, ComplexWriter<float2>>(src, J, w, m0, k0, sm);
   }
 }
 
+// Row maxima of the jobs of a table (fp16 split of block maps), a kernel of its own so
+// that the block moves keep their shared-memory footprint.
+template <typename Tin>
+__global__ void __launch_bounds__(256) block_rowmax_kernel(const DevGatherJob* __restrict__ jobs,
+                                                           const int* __restrict__ tile_start, int njobs,
+                                                           BlockBases bases) {
+  const int b = blockIdx.x;
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tile_start[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  const DevGatherJob& J = jobs[lo];
+  const int t = b - tile_start[lo];
+  const int64_t m0 = (int64_t)(t % J.tiles_m) * (1024 >> J.tks), k0 = (int64_t)(t / J.tiles_m) << J.tks;
+  rowmax_tile_adaptive<Tin>(static_cast<const Tin*>(bases.buf[J.src_buf]) + J.src_off, J,
+                            static_cast<float*>(bases.buf[5]) + J.amax_off, m0, k0);
+}
+
 }  // namespace
+
+cudaError_t launch_block_rowmax(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
+                                const BlockBases& bases, int src_is64, cudaStream_t s) {
+  if (ntiles <= 0) return cudaSuccess;
+  if (src_is64)
+    block_rowmax_kernel<double2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+  else
+    block_rowmax_kernel<float2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+  return cudaGetLastError();
+}
 
 void finish_dev_gather_job(DevGatherJob* J) {
   int tks = 0;

@@ -1,9 +1,10 @@
 """grafttn: GB300 (sm_103a) tree-tensor-network effective-Hamiltonian hot path.
 
 Host-side mirror of GraftTN/Graft.jl's interface for that path (TTNS, TTNO, EnvCache,
-eff_h1 / eff_h2 / eff_h0, dmrg2!, TDVP1) over the C ABI of libgrafttn.so.  Host metadata
-(topologies, operators) is importable without a GPU; the device layer needs the built
-library and a CUDA device and fails loudly otherwise.
+eff_h1 / eff_h2 / eff_h0, dmrg1!, dmrg2!, TDVP1, TDVP2, TDVP1_CBE, inner / expect, TTNO
+apply) over the C ABI of libgrafttn.so.  Host metadata (topologies, operators) is
+importable without a GPU; the device layer needs the built library and a CUDA device and
+fails loudly otherwise.
 """
 from .topology import (TreeTopology, binary_topology, fork_topology, kary_topology, mps_topology,
                        star_topology)
@@ -17,7 +18,8 @@ __all__ = [
 ]
 
 
-_DEVICE_MODULES = ("device", "networks", "contractions", "solvers", "cbe", "gradients", "blocksparse", "parallel")
+_DEVICE_MODULES = ("device", "networks", "contractions", "solvers", "cbe", "gradients", "blocksparse", "parallel",
+                   "observables")
 
 
 def __getattr__(name):

@@ -20,7 +20,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .contractions import EnvCache, eff_h0
+from .contractions import EnvCache, choose_order, eff_h0
 from .networks import TTNO, TTNS, absorb_on_leg
 
 
@@ -90,7 +90,8 @@ def site_half(cache: EnvCache, psi: TTNS, H: TTNO, site, peer, X, k_site):
         widx[-1] = ko
         labels.append([ka, ko, -(out_pos[raw] + 1)])
         ops.append(ctx.upload(np.ones((1, 1, 1))))
-    return ctx.contract(ops, labels)
+    order = choose_order([tuple(o.shape) for o in ops], labels, list(range(len(ops))))
+    return ctx.contract(ops, labels, None, order)
 
 
 def _mat(ctx, A, k):

@@ -9,6 +9,7 @@ the device) and is then applied many times by the Krylov solvers.
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
@@ -150,6 +151,97 @@ def h2_spec(t, n, m, x_rank, wn_rank, wm_rank, pn):
         caps.append(len(labels) - 1)
     order = [0] + envn + [1] + envmc + [2] + envmp + caps
     return labels, order, envs
+
+
+def chain_cost(shapes, labels, order):
+    """(complex MACs, largest intermediate in elements) of the pairwise chain that starts
+    at operand order[0] and absorbs the others in order."""
+    dims = {}
+    for shp, lab in zip(shapes, labels):
+        for l, d in zip(lab, shp):
+            dims[l] = int(d)
+    cur = list(labels[order[0]])
+    macs, peak = 0, math.prod(dims[l] for l in cur)
+    for j in order[1:]:
+        L = labels[j]
+        sh = [l for l in cur if l > 0 and l in L]
+        M = math.prod(dims[l] for l in cur if l not in sh)
+        K = math.prod(dims[l] for l in sh)
+        N = math.prod(dims[l] for l in L if l not in sh)
+        macs += M * K * N
+        peak = max(peak, M * N)
+        cur = [l for l in L if l not in sh] + [l for l in cur if l not in sh]
+    return macs, peak
+
+
+def best_order(shapes, labels, first=0, out_weight=8):
+    """Cheapest left-deep chain from operand ``first``: dynamic programming over the set
+    of absorbed operands (the running tensor's legs depend only on that set), minimising
+    sum over steps of M*K*N + out_weight * M*N (MACs plus the written intermediate)."""
+    dims = {}
+    for shp, lab in zip(shapes, labels):
+        for l, d in zip(lab, shp):
+            dims[l] = int(d)
+    others = [j for j in range(len(labels)) if j != first]
+    n = len(others)
+
+    def legs(mask):
+        cnt = {}
+        for l in labels[first]:
+            cnt[l] = cnt.get(l, 0) + 1
+        for b in range(n):
+            if mask >> b & 1:
+                for l in labels[others[b]]:
+                    cnt[l] = cnt.get(l, 0) + 1
+        return [l for l, c in cnt.items() if not (l > 0 and c == 2)]
+    best = {0: (0.0, [])}
+    for mask in sorted(range(1 << n), key=lambda m: bin(m).count("1")):
+        if mask not in best:
+            continue
+        cost, seq = best[mask]
+        cur = legs(mask)
+        for b in range(n):
+            if mask >> b & 1:
+                continue
+            L = labels[others[b]]
+            sh = [l for l in cur if l > 0 and l in L]
+            M = math.prod(dims[l] for l in cur if l not in sh)
+            K = math.prod(dims[l] for l in sh)
+            N = math.prod(dims[l] for l in L if l not in sh)
+            c = cost + M * K * N + out_weight * M * N
+            nm = mask | (1 << b)
+            if nm not in best or c < best[nm][0]:
+                best[nm] = (c, seq + [others[b]])
+    return [first] + best[(1 << n) - 1][1]
+
+
+def _objective(shapes, labels, order, out_weight=8):
+    macs = 0
+    dims = {}
+    for shp, lab in zip(shapes, labels):
+        for l, d in zip(lab, shp):
+            dims[l] = int(d)
+    cur = list(labels[order[0]])
+    for j in order[1:]:
+        L = labels[j]
+        sh = [l for l in cur if l > 0 and l in L]
+        M = math.prod(dims[l] for l in cur if l not in sh)
+        K = math.prod(dims[l] for l in sh)
+        N = math.prod(dims[l] for l in L if l not in sh)
+        macs += M * K * N + out_weight * M * N
+        cur = [l for l in L if l not in sh] + [l for l in cur if l not in sh]
+    return macs
+
+
+def choose_order(shapes, labels, order):
+    """The given (env-first) order unless the cheapest chain is clearly cheaper (by 1.5x in
+    MACs plus written intermediates).  This matters at high-degree nodes, where absorbing
+    every environment before the TTNO tensor multiplies the running tensor by w per leg;
+    on binary trees and chains the env-first chain is kept."""
+    if len(labels) > 13:
+        return list(order)
+    b = best_order(shapes, labels, order[0])
+    return b if 3 * _objective(shapes, labels, b) < 2 * _objective(shapes, labels, order) else list(order)
 
 
 class EffectiveMap:
@@ -329,7 +421,8 @@ class EnvCache:
         if has_cap:
             ops.append(psi.ctx.upload(np.ones((1, 1, 1))))
         ops += [W, A]
-        E = psi.ctx.contract(ops, labels, conj)
+        order = choose_order([tuple(o.shape) for o in ops], labels, list(range(len(ops))))
+        E = psi.ctx.contract(ops, labels, conj, order)
         self.envs[key] = E
         self.bytes += E.numel() * E.element_size()
         self.builds += 1
@@ -353,6 +446,7 @@ def eff_h1(cache: EnvCache, psi: TTNS, H: TTNO, n, precision=_lib.PREC_FP64):
     statics = [H.tensors[n]] + [cache.env(psi, H, w, u) for (w, u) in envs]
     if t.parent[n] < 0:
         statics.append(_cap(psi.ctx))
+    order = choose_order([tuple(x.shape)] + [tuple(s.shape) for s in statics], labels, order)
     return EffectiveMap(psi.ctx, x.shape, labels, order, statics, precision)
 
 
@@ -372,6 +466,7 @@ def eff_h2(cache: EnvCache, psi: TTNS, H: TTNO, n, m, precision=_lib.PREC_FP64):
     statics = [H.tensors[n], H.tensors[m]] + [cache.env(psi, H, w, u) for (w, u) in envs]
     if t.parent[m] < 0:
         statics.append(_cap(psi.ctx))
+    order = choose_order([tuple(xs)] + [tuple(s.shape) for s in statics], labels, order)
     return EffectiveMap(psi.ctx, xs, labels, order, statics, precision)
 
 

@@ -72,6 +72,38 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
     return psi, energies
 
 
+def dmrg1(psi: TTNS, H: TTNO, nsweeps=10, tol=1e-10, krylovdim=20, precision="fp64", rq_fp64=None,
+          lanczos_tol=1e-12, maxiter=100, stats=None):
+    """Single-site DMRG (GroundState.jl:51-84): bond dimensions stay those of psi; postorder
+    then reverse postorder, the local ground state of eff_h1 at every node; returns
+    (psi, energies per sweep), stopping early when the energy change drops below tol."""
+    if not H.ishermitian:
+        raise ValueError("dmrg1: DMRG requires ishermitian(H) == true")
+    prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
+    if rq_fp64 is None:
+        rq_fp64 = prec != _lib.PREC_FP64
+    t = psi.topo
+    cache = EnvCache(t)
+    order = t.postorder()
+    energies = []
+    for sweep in range(nsweeps):
+        E = float("nan")
+        for n in list(order) + list(reversed(order)):
+            move_center(psi, n, cache)
+            h1 = eff_h1(cache, psi, H, n, prec)
+            E, v, info = h1.lanczos_min(psi.tensors[n], krylovdim=krylovdim, tol=lanczos_tol, maxiter=maxiter,
+                                        rq_fp64=rq_fp64)
+            h1.close()
+            if stats is not None:
+                stats["matvecs"] = stats.get("matvecs", 0) + info["matvecs"]
+            psi.tensors[n] = v
+            cache.invalidate_node(n)
+        energies.append(float(E))
+        if len(energies) >= 2 and abs(energies[-1] - energies[-2]) < tol:
+            break
+    return psi, energies
+
+
 class TDVP1:
     """One-site TDVP with order-2 splitting (tdvp.jl:31-44, 171-301)."""
 
@@ -148,7 +180,75 @@ class TDVP1:
         cache.invalidate_node(v)
 
 
-def evolve(ev: TDVP1, psi: TTNS, H: TTNO, dz, nsteps):
+class TDVP2:
+    """Two-site TDVP (tdvp.jl:67-84, 307-431): every bond is evolved forward as a two-site
+    block and split by truncated SVD (bond dimensions adapt up to ``trunc.maxdim``), with a
+    backward one-site evolution of the connecting parent between consecutive bonds.  Order
+    2 fuses the turning bond's two half steps into one full step and one split."""
+
+    def __init__(self, order=2, trunc: TruncationScheme | None = None, krylovdim=30, tol=1e-12,
+                 precision="fp64", fuse_turning=True):
+        if order not in (1, 2):
+            raise ValueError("order must be 1 or 2")
+        self.order = order
+        self.trunc = trunc or TruncationScheme()
+        self.krylovdim = krylovdim
+        self.tol = tol
+        self.fuse_turning = fuse_turning
+        self.precision = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
+        self.cache = None
+
+    def step(self, psi: TTNS, H: TTNO, dz):
+        if self.cache is None or self.cache.topo != psi.topo:
+            self.cache = EnvCache(psi.topo)
+        if self.order == 1:
+            self._sweep(psi, H, dz, rev=False)
+        elif self.fuse_turning:
+            self._sweep(psi, H, dz / 2, rev=False, terminal_dz=dz)
+            self._sweep(psi, H, dz / 2, rev=True, skip_initial=True)
+        else:
+            self._sweep(psi, H, dz / 2, rev=False)
+            self._sweep(psi, H, dz / 2, rev=True)
+        return psi
+
+    def _sweep(self, psi, H, dz, rev, terminal_dz=None, skip_initial=False):
+        t = psi.topo
+        bonds = [n for n in t.postorder() if t.parent[n] >= 0]
+        last = len(bonds) - 1
+        for j in (range(last, -1, -1) if rev else range(last + 1)):
+            if rev and skip_initial and j == last:
+                continue
+            n = bonds[j]
+            m = t.parent[n]
+            move_center(psi, m, self.cache)
+            if rev:
+                if j != last:
+                    self._site_backward(psi, H, m, dz)
+                self._bond_forward(psi, H, n, m, dz, "n")
+            else:
+                term = terminal_dz is not None and j == last
+                self._bond_forward(psi, H, n, m, terminal_dz if term else dz, "n" if term else "m")
+                if j != last:
+                    self._site_backward(psi, H, m, dz)
+
+    def _bond_forward(self, psi, H, n, m, dz, center_on):
+        theta = two_site_tensor(psi, n, m)
+        h2 = eff_h2(self.cache, psi, H, n, m, self.precision)
+        theta, _ = h2.exponentiate(dz, theta, self.krylovdim, self.tol)
+        h2.close()
+        self.cache.invalidate_edge(n, m)
+        split_two_site(psi, theta, n, m, self.trunc, center_on)
+
+    def _site_backward(self, psi, H, m, dz):
+        assert psi.center == m
+        h1 = eff_h1(self.cache, psi, H, m, self.precision)
+        A, _ = h1.exponentiate(-dz, psi.tensors[m], self.krylovdim, self.tol)
+        h1.close()
+        psi.tensors[m] = A
+        self.cache.invalidate_node(m)
+
+
+def evolve(ev, psi: TTNS, H: TTNO, dz, nsteps):
     """(Evolution.jl:86-93)"""
     for _ in range(nsteps):
         ev.step(psi, H, dz)

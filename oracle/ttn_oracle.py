@@ -931,6 +931,27 @@ def dmrg2(psi, Ws, maxdim=None, nsweeps=10, tol=1e-10, krylovdim=20, atol=0.0, l
     return psi, energies
 
 
+def dmrg1(psi, Ws, nsweeps=10, tol=1e-10, krylovdim=20, lanczos_tol=1e-12):
+    """Single-site DMRG with fixed bond dimensions (GroundState.jl:51-84): postorder then
+    reverse postorder, the local ground state of eff_h1 at every node."""
+    t = psi.topo
+    cache = EnvCache(t)
+    energies = []
+    order = t.postorder()
+    for sweep in range(nsweeps):
+        E = float("nan")
+        for n in list(order) + list(reversed(order)):
+            move_center(psi, n, cache.invalidate_edge)
+            h1 = eff_h1(cache, psi, Ws, n)
+            E, v, _ = lanczos_min(h1, psi.tensors[n], krylovdim=krylovdim, tol=lanczos_tol)
+            psi.tensors[n] = v
+            cache.invalidate_node(n)
+        energies.append(float(E))
+        if len(energies) >= 2 and abs(energies[-1] - energies[-2]) < tol:
+            break
+    return psi, energies
+
+
 def tdvp1_step(psi, Ws, dz, cache=None, krylovdim=30, tol=1e-12):
     """Order-2 TDVP1 step (tdvp.jl:171-195): forward half sweep with the turning site
     evolved by the full dz, then the reverse half sweep skipping that site."""
@@ -987,6 +1008,59 @@ def _evolve_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol):
         psi.tensors[v] = np.tensordot(psi.tensors[v], C, axes=([psi.tensors[v].ndim - 1], [0]))
     psi.center = v
     cache.invalidate_node(v)
+
+
+def tdvp2_step(psi, Ws, dz, cache=None, maxdim=None, atol=0.0, krylovdim=30, tol=1e-12):
+    """Order-2 TDVP2 step with the fused turning bond (tdvp.jl:307-329): forward half sweep
+    whose last bond is evolved by the full dz and split onto the child, then the reverse
+    half sweep that skips that bond."""
+    cache = cache or EnvCache(psi.topo)
+    opts = dict(maxdim=maxdim, atol=atol, krylovdim=krylovdim, tol=tol)
+    _tdvp2_sweep(psi, Ws, dz / 2, cache, rev=False, terminal_dz=dz, opts=opts)
+    _tdvp2_sweep(psi, Ws, dz / 2, cache, rev=True, skip_initial=True, opts=opts)
+    return cache
+
+
+def _tdvp2_sweep(psi, Ws, dz, cache, rev, terminal_dz=None, skip_initial=False, opts=None):
+    """(tdvp.jl:340-388) Two-site forward evolution of every bond (postorder child nodes);
+    a backward one-site evolution of the parent between consecutive bonds, before the
+    bond in reverse, after it forward; none at the turning bond."""
+    t = psi.topo
+    bonds = [n for n in t.postorder() if t.parent[n] >= 0]
+    last = len(bonds) - 1
+    idx = range(last, -1, -1) if rev else range(last + 1)
+    for j in idx:
+        if rev and skip_initial and j == last:
+            continue
+        n = bonds[j]
+        m = t.parent[n]
+        move_center(psi, m, cache.invalidate_edge)
+        if rev:
+            if j != last:
+                _tdvp2_site_backward(psi, Ws, m, dz, cache, opts)
+            _tdvp2_bond_forward(psi, Ws, n, m, dz, "n", cache, opts)
+        else:
+            term = terminal_dz is not None and j == last
+            _tdvp2_bond_forward(psi, Ws, n, m, terminal_dz if term else dz, "n" if term else "m", cache, opts)
+            if j != last:
+                _tdvp2_site_backward(psi, Ws, m, dz, cache, opts)
+
+
+def _tdvp2_bond_forward(psi, Ws, n, m, dz, center_on, cache, opts):
+    """(tdvp.jl:390-410)"""
+    theta = two_site_tensor(psi, n, m)
+    h2 = eff_h2(cache, psi, Ws, n, m)
+    theta = krylov_expm(h2, dz, theta, krylovdim=opts["krylovdim"], tol=opts["tol"])
+    cache.invalidate_edge(n, m)
+    split_two_site(psi, theta, n, m, maxdim=opts["maxdim"], atol=opts["atol"], center_on=center_on)
+
+
+def _tdvp2_site_backward(psi, Ws, m, dz, cache, opts):
+    """(tdvp.jl:412-431)"""
+    assert psi.center == m
+    h1 = eff_h1(cache, psi, Ws, m)
+    psi.tensors[m] = krylov_expm(h1, -dz, psi.tensors[m], krylovdim=opts["krylovdim"], tol=opts["tol"])
+    cache.invalidate_node(m)
 
 
 # ---------------------------------------------------------------------------

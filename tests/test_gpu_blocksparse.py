@@ -8,11 +8,11 @@ from u1_cases import dense_reference, h2_u1_case
 
 pytestmark = pytest.mark.gpu
 
-RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 1e-5, "bf16x3": 1e-3}
+RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 1e-5, "bf16x3": 1e-3, "fp16x3": 1e-5}
 
 
 @pytest.mark.parametrize("group", [True, False])
-@pytest.mark.parametrize("prec", ["fp64", "bf16x6", "bf16x3", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "bf16x6", "bf16x3", "fp32", "fp16x3"])
 @pytest.mark.parametrize("depth,node,D", [(3, "n2_2", 16), (4, "n3_1", 64)])
 def test_block_map_matches_dense(ctx, prec, depth, node, D, group):
     xs, labels, order, statics, x = h2_u1_case(depth, node, D)
@@ -25,7 +25,7 @@ def test_block_map_matches_dense(ctx, prec, depth, node, D, group):
     bm.close()
 
 
-@pytest.mark.parametrize("prec", ["fp64", "bf16x6"])
+@pytest.mark.parametrize("prec", ["fp64", "bf16x6", "fp16x3"])
 def test_block_map_d128_skinny_and_tc(ctx, prec):
     """Depth-5 binary tree at D = 128: coupled-charge problems of every kind (tcgen05,
     skinny N < 16, narrow K < 16 block moves) in one map."""

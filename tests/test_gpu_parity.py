@@ -151,3 +151,46 @@ def test_tdvp1_full_rank_vs_exact(ctx):
     v1 = O.to_dense(oracle_state(psi))
     assert abs(1 - abs(np.vdot(v1, vex))) < 1e-10
     assert abs(np.linalg.norm(v1) - 1) < 1e-10
+
+
+def test_tdvp2_full_rank_vs_exact(ctx):
+    topo = G.star_topology(3, 2)
+    W = G.TTNO.from_hamiltonian(G.tfi(topo, g=0.9), ctx)
+    psi = G.random_ttns(np.random.default_rng(13), topo, 2, 8, ctx=ctx)
+    Hd = O.dense_hamiltonian(O.tfi(O.star_topology(3, 2), g=0.9))
+    v0 = O.to_dense(oracle_state(psi))
+    vex = O.exact_evolve(Hd, v0, -1j * 0.05 * 4)
+    ev = G.TDVP2(order=2, trunc=G.TruncationScheme(maxdim=64))
+    for _ in range(4):
+        ev.step(psi, W, -1j * 0.05)
+    assert abs(1 - abs(np.vdot(O.to_dense(oracle_state(psi)), vex))) < 1e-10
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("bf16x6", 1e-8)])
+def test_tdvp2_truncated_matches_oracle_trajectory(ctx, precision, tol):
+    # bond growth from a product state under truncation: the same bond dimensions and the
+    # same state as the oracle's TDVP2 after every step
+    topo = G.star_topology(3, 2)
+    W = G.TTNO.from_hamiltonian(G.tfi(topo, g=0.9), ctx)
+    Ws = O.ttno_nn(O.tfi(O.star_topology(3, 2), g=0.9))
+    psi = G.random_ttns(np.random.default_rng(14), topo, 2, 1, ctx=ctx)
+    o = oracle_state(psi)
+    ev = G.TDVP2(order=2, trunc=G.TruncationScheme(maxdim=4, atol=1e-12), precision=precision)
+    cache = None
+    for _ in range(3):
+        ev.step(psi, W, -1j * 0.02)
+        cache = O.tdvp2_step(o, Ws, -1j * 0.02, cache, maxdim=4, atol=1e-12)
+        assert psi.bond_dims() == O.bond_dims(o)
+    assert abs(1 - abs(np.vdot(O.to_dense(oracle_state(psi)), O.to_dense(o)))) < tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "bf16x6"])
+def test_dmrg1_full_bonds_vs_ed(ctx, precision):
+    topo = G.star_topology(3, 2)
+    W = G.TTNO.from_hamiltonian(G.tfi(topo, g=0.9), ctx)
+    E0, _ = O.exact_groundstate(O.dense_hamiltonian(O.tfi(O.star_topology(3, 2), g=0.9)))
+    psi = G.random_ttns(np.random.default_rng(15), topo, 2, 8, ctx=ctx)
+    dims = psi.bond_dims()
+    _, Es = G.dmrg1(psi, W, nsweeps=10, precision=precision)
+    assert psi.bond_dims() == dims
+    assert abs(Es[-1] - E0) / abs(E0) < 1e-10

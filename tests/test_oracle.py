@@ -89,6 +89,47 @@ def test_tdvp1_full_rank_vs_exact():
     assert abs(O.expect(psi, Ws) - np.vdot(vex, Hd @ vex)) < 1e-8
 
 
+def test_dmrg1_full_bonds_vs_ed():
+    # GroundState.jl:51-84 with full bond spaces: the variational space is complete
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo, g=0.9)
+    E0, _ = O.exact_groundstate(O.dense_hamiltonian(H))
+    psi = O.random_ttns(np.random.default_rng(5), topo, 2, 8)
+    _, Es = O.dmrg1(psi, O.ttno_nn(H), nsweeps=10)
+    assert abs(Es[-1] - E0) < 1e-10
+
+
+def test_tdvp2_full_rank_vs_exact():
+    # full bond dimension: every two-site and one-site projector is the identity, so the
+    # order-2 TDVP2 step equals exact evolution (tdvp.jl:307-431)
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo, g=0.9)
+    Ws = O.ttno_nn(H)
+    psi = O.random_ttns(np.random.default_rng(3), topo, 2, 8)
+    Hd = O.dense_hamiltonian(H)
+    vex = O.exact_evolve(Hd, O.to_dense(psi), -1j * 0.05 * 4)
+    cache = None
+    for _ in range(4):
+        cache = O.tdvp2_step(psi, Ws, -1j * 0.05, cache, maxdim=64)
+    assert abs(1 - abs(np.vdot(O.to_dense(psi), vex))) < 1e-10
+
+
+def test_tdvp2_grows_bonds_from_product_state():
+    # from bond dimension 1 TDVP2 grows the bonds (bounded by maxdim) and stays close to
+    # exact evolution for a short time
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo, g=0.9)
+    Ws = O.ttno_nn(H)
+    psi = O.random_ttns(np.random.default_rng(4), topo, 2, 1)
+    Hd = O.dense_hamiltonian(H)
+    vex = O.exact_evolve(Hd, O.to_dense(psi), -1j * 0.02 * 5)
+    cache = None
+    for _ in range(5):
+        cache = O.tdvp2_step(psi, Ws, -1j * 0.02, cache, maxdim=4, atol=1e-12)
+    assert max(O.bond_dims(psi)) > 1 and max(O.bond_dims(psi)) <= 4
+    assert abs(1 - abs(np.vdot(O.to_dense(psi), vex))) < 1e-4
+
+
 @pytest.mark.parametrize("which", ["h1", "h2", "env"])
 def test_package_specs_match_oracle(which):
     gt, ot = G.binary_topology(3), O.binary_topology(3)
