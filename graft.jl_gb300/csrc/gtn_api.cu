@@ -204,9 +204,17 @@ int gtn_contract(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* d
                  const int* labels, const int* conj, const int* order,
                  const void* const* operands, void* out, int precision) {
   if (!ctx || !operands || !out) return set_err(ctx, GTN_ERR_INVALID, "null argument");
-  gtn_map map = nullptr;
-  int st = gtn_map_create(ctx, n_operands, ranks, dims, labels, conj, order, operands, precision, &map);
-  if (st != GTN_OK) return st;
+  // a one-shot contraction: no static grouping (a pre-contracted group only pays off when
+  // the map is applied many times)
+  gtn_map map = new (std::nothrow) gtn_map_s();
+  if (!map) return set_err(ctx, GTN_ERR_MEMORY, "host allocation failed");
+  int st = plan_build(ctx, n_operands, ranks, dims, labels, conj, order, operands, precision, map, false);
+  if (st != GTN_OK) {
+    cudaStreamSynchronize(ctx->stream);
+    map_free(map);
+    delete map;
+    return st;
+  }
   st = map_run(map, precision, static_cast<const double2*>(operands[0]), static_cast<double2*>(out));
   gtn_map_destroy(map);
   return st;

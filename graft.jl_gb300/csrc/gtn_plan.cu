@@ -141,6 +141,38 @@ struct ChainOp {
   std::vector<int64_t> D;
 };
 
+// Largest intermediate (elements) of contracting ops[0], ops[1], ... in order.
+double group_peak(const std::vector<ChainOp>& ops) {
+  std::vector<int> LT = ops[0].L;
+  std::vector<int64_t> DT = ops[0].D;
+  double peak = 1;
+  for (auto d : DT) peak *= (double)d;
+  for (size_t j = 1; j < ops.size(); ++j) {
+    std::vector<int> nL;
+    std::vector<int64_t> nD;
+    for (size_t a = 0; a < ops[j].L.size(); ++a) {
+      const int l = ops[j].L[a];
+      if (!(l > 0 && std::find(LT.begin(), LT.end(), l) != LT.end())) {
+        nL.push_back(l);
+        nD.push_back(ops[j].D[a]);
+      }
+    }
+    for (size_t a = 0; a < LT.size(); ++a) {
+      const int l = LT[a];
+      if (!(l > 0 && std::find(ops[j].L.begin(), ops[j].L.end(), l) != ops[j].L.end())) {
+        nL.push_back(l);
+        nD.push_back(DT[a]);
+      }
+    }
+    LT.swap(nL);
+    DT.swap(nD);
+    double sz = 1;
+    for (auto d : DT) sz *= (double)d;
+    peak = std::max(peak, sz);
+  }
+  return peak;
+}
+
 // External legs of a group of operands: labels not paired inside the group, in order.
 ChainOp group_external(const std::vector<ChainOp>& ops) {
   std::map<int, int> cnt;
@@ -285,6 +317,10 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
             double sz = 1;
             for (auto d : g.D) sz *= (double)d;
             if (sz > (double)kMaxCombined) ok = false;
+            // the pre-contraction runs as a chain in member order: every intermediate of it
+            // stays within the same bound (members with no shared leg would form outer
+            // products far larger than the group)
+            if (ok && group_peak(cur) > (double)kMaxCombined) ok = false;
             chain.push_back(g);
           } else {
             chain.push_back(cur[0]);

@@ -9,8 +9,8 @@ M = Na^H * S link T^T * conj(Np) (Na, Np the complements of Q and of the partner
 S, T the two halves of the two-site Hamiltonian sandwich, two_site_factor_frame.jl:308-426).
 Here the complements are never materialised: with G = S link (ext_u x (edge*w)) and the
 partner half T (ext_v x (edge*w)), the core is the product of two tall-skinny factors
-G' = (1 - Q Q^H) G and T' = (1 - P P^H) T, so its left singular pairs are those of
-Q1 K Q1^H with G' = Q1 R1 and K = R1 (T'^T conj(T')) R1^H, a small Hermitian matrix.
+G' = (1 - Q Q^H) G and T' = (1 - P P^H) T.  With G' = Q1 R1 and T' = Q2 R2 (thin QR) it is
+Q1 (R1 R2^T) Q2^T, so its left singular pairs are Q1 times those of the small R1 R2^T.
 Directions with singular value >= spawn_threshold * ||active|| / |dz| are spliced as
 U = [Q E], R = U^H active (exact: U R = active).  Every step is a libgrafttn call (FP64).
 """
@@ -147,19 +147,29 @@ def cbe_split(cache: EnvCache, psi: TTNS, H: TTNO, u, v, dz, maxdim, strategy: P
             # complements: G' = G - Q (Q^H G), T' = T - P (P^H T)
             G = ctx.axpby(-1.0, _matmul(ctx, Q, _matmul(ctx, Q, G, conjA=True, transA=True)), 1.0, G)
             T = ctx.axpby(-1.0, _matmul(ctx, par, _matmul(ctx, par, T, conjA=True, transA=True)), 1.0, T)
+            # M = G' T'^T = Q1 (R1 R2^T) Q2^T with G' = Q1 R1 and T' = Q2 R2: the singular
+            # pairs come from the small factor directly (accurate to eps * sigma_max; the
+            # Gram matrix of M would square the noise floor up to sqrt(eps) * sigma_max)
             Q1, R1 = ctx.qr(G)
-            W2 = ctx.contract([T.contiguous(), T.contiguous()], [[1, -1], [1, -2]], [False, True])  # T^T conj(T)
-            K = ctx.contract([R1.contiguous(), W2, R1.contiguous()], [[-1, 1], [1, 2], [-2, 2]], [False, False, True])
-            Uk, lam, _, _ = ctx.svd_trunc(K, maxdim=budget)
-            sig = np.sqrt(np.maximum(lam, 0.0))
+            _, R2 = ctx.qr(T)
+            Z = ctx.contract([R1.contiguous(), R2.contiguous()], [[-1, 1], [-2, 1]])
+            Uz, sig, _, _ = ctx.svd_trunc(Z, maxdim=budget)
             cutoff = strategy.spawn_threshold * max(ctx.norm(act), 1e-300) / abs(dz)
             keep = int(np.sum(sig >= cutoff))
             if keep > 0:
-                E = _matmul(ctx, Q1, Uk[:, :keep].contiguous())
-                # re-orthogonalise against Q and within E (FP64 QR)
+                E = _matmul(ctx, Q1, Uz[:, :keep].contiguous())
+                # re-orthogonalise against Q; directions left with no weight outside span(Q)
+                # (null columns of a rank-deficient G') are dropped before the QR
                 E = ctx.axpby(-1.0, _matmul(ctx, Q, _matmul(ctx, Q, E, conjA=True, transA=True)), 1.0, E)
-                E, _ = ctx.qr(E)
-                selected = E.shape[1]
+                norms = np.linalg.norm(ctx.download(E), axis=0)
+                good = [j for j in range(keep) if norms[j] > 1e-6]
+                if len(good) < keep:
+                    E = E[:, good].contiguous() if good else None
+                if E is not None:
+                    E, _ = ctx.qr(E)
+                    E = ctx.axpby(-1.0, _matmul(ctx, Q, _matmul(ctx, Q, E, conjA=True, transA=True)), 1.0, E)
+                    E, _ = ctx.qr(E)
+                    selected = E.shape[1]
             if info is not None:
                 info.update(sigmas=sig.tolist(), cutoff=cutoff)
     Unew = ctx.concat_cols(Q, E) if E is not None else Q

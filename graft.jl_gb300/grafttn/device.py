@@ -90,7 +90,7 @@ class Context:
                                    int_array([1 if c else 0 for c in conj]), int_array(order),
                                    ptr_array([t.data_ptr() for t in operands]), C.c_void_p(out.data_ptr()),
                                    precision)
-        check(st, self.h, "contract")
+        check(st, self.h, f"contract {[tuple(t.shape) for t in operands]} labels {labels} order {order}")
         return out
 
     def permute(self, t, perm):
