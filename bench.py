@@ -651,7 +651,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--skip-extra", action="store_true", help="only the headline workload")
-    ap.add_argument("--precision", default="bf16x6", choices=sorted(DTYPES), help="mixed mode of the headline map")
+    ap.add_argument("--precision", default="fp16x3", choices=sorted(DTYPES), help="mixed mode of the headline map")
     ap.add_argument("--dmrg", action="store_true", help="measure DMRG sweeps instead of map applications")
     ap.add_argument("--dmrg-topology", default="mps", choices=["mps", "binary"])
     ap.add_argument("--dmrg-sites", type=int, default=63)
