@@ -86,6 +86,7 @@ int gtn_ctx_destroy(gtn_ctx ctx) {
   cudaStreamSynchronize(ctx->stream);
   linalg_release(ctx);
   if (ctx->ws) cudaFree(ctx->ws);
+  if (ctx->carena) cudaFree(ctx->carena);
   if (ctx->d_red) cudaFree(ctx->d_red);
   if (ctx->h_red) cudaFreeHost(ctx->h_red);
   if (ctx->d_errflag) cudaFree(ctx->d_errflag);
@@ -205,10 +206,24 @@ int gtn_contract(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* d
                  const void* const* operands, void* out, int precision) {
   if (!ctx || !operands || !out) return set_err(ctx, GTN_ERR_INVALID, "null argument");
   // a one-shot contraction: no static grouping (a pre-contracted group only pays off when
-  // the map is applied many times)
+  // the map is applied many times); its buffers come from the context's arena, reused in
+  // stream order by the next contraction, and the arena grows to the largest need seen
+  if (ctx->carena_need > ctx->carena_cap) {
+    if (ctx->carena) cudaFree(ctx->carena);
+    ctx->carena = nullptr;
+    ctx->carena_cap = 0;
+    if (cudaMalloc(&ctx->carena, ctx->carena_need) == cudaSuccess) ctx->carena_cap = ctx->carena_need;
+    else ctx->carena = nullptr;
+  }
   gtn_map map = new (std::nothrow) gtn_map_s();
   if (!map) return set_err(ctx, GTN_ERR_MEMORY, "host allocation failed");
+  map->ctx = ctx;
+  map->oneshot = true;
+  map->arena = ctx->carena;
+  map->arena_cap = ctx->carena_cap;
   int st = plan_build(ctx, n_operands, ranks, dims, labels, conj, order, operands, precision, map, false);
+  const size_t need = map->arena_off + map->arena_spill;
+  if (need > ctx->carena_need && need <= (size_t(8) << 30)) ctx->carena_need = need;
   if (st != GTN_OK) {
     cudaStreamSynchronize(ctx->stream);
     map_free(map);
@@ -216,7 +231,11 @@ int gtn_contract(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* d
     return st;
   }
   st = map_run(map, precision, static_cast<const double2*>(operands[0]), static_cast<double2*>(out));
-  gtn_map_destroy(map);
+  // arena buffers are reused in stream order: only spilled allocations need the stream to
+  // drain before they are freed
+  if (!map->owned.empty()) cudaStreamSynchronize(ctx->stream);
+  map_free(map);
+  delete map;
   return st;
 }
 

@@ -24,7 +24,9 @@ constexpr int BM = 64, BN = 64, BK = 16;
 template <typename T>
 __device__ __forceinline__ void gemm_simt_tile(const T* __restrict__ A, const T* __restrict__ B,
                                                T* __restrict__ C, int64_t M, int64_t N, int64_t K,
-                                               int64_t m0, int64_t n0) {
+                                               int64_t m0, int64_t n0, int64_t kb = 0, int64_t ke = -1) {
+  // k range [kb, ke) of the row pitch K (split-K slices); ke < 0 means K
+  if (ke < 0) ke = K;
   using R = typename CT<T>::R;
   __shared__ T As[BK][BM + 1];
   __shared__ T Bs[BK][BN + 1];
@@ -36,21 +38,21 @@ __device__ __forceinline__ void gemm_simt_tile(const T* __restrict__ A, const T*
 #pragma unroll
     for (int j = 0; j < 4; ++j) { acc_r[i][j] = 0; acc_i[i][j] = 0; }
 
-  for (int64_t k0 = 0; k0 < K; k0 += BK) {
+  for (int64_t k0 = kb; k0 < ke; k0 += BK) {
     // load A tile: BM rows x BK cols = 1024 elements, 4 per thread; lanes walk k.
 #pragma unroll
     for (int l = 0; l < (BM * BK) / 256; ++l) {
       const int e = tid + l * 256;
       const int r = e / BK, c = e % BK;
       const int64_t m = m0 + r, k = k0 + c;
-      As[c][r] = (m < M && k < K) ? A[m * K + k] : CT<T>::zero();
+      As[c][r] = (m < M && k < ke) ? A[m * K + k] : CT<T>::zero();
     }
 #pragma unroll
     for (int l = 0; l < (BN * BK) / 256; ++l) {
       const int e = tid + l * 256;
       const int r = e / BK, c = e % BK;
       const int64_t n = n0 + r, k = k0 + c;
-      Bs[c][r] = (n < N && k < K) ? B[n * K + k] : CT<T>::zero();
+      Bs[c][r] = (n < N && k < ke) ? B[n * K + k] : CT<T>::zero();
     }
     __syncthreads();
 #pragma unroll 4
@@ -244,6 +246,90 @@ cudaError_t launch_skinny(const GemmJob* jobs, int njobs, cudaStream_t s) {
   return cudaSuccess;
 }
 
+// Narrow tile for split-K products with few output columns: 64 x 16, thread (tx, ty) of
+// 16 x 16 owns m = tx + 16 i (i < 4) and n = ty.
+template <typename T>
+__device__ __forceinline__ void gemm_simt_tile_n16(const T* __restrict__ A, const T* __restrict__ B,
+                                                   T* __restrict__ C, int64_t M, int64_t N, int64_t K, int64_t m0,
+                                                   int64_t kb, int64_t ke) {
+  using R = typename CT<T>::R;
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][16 + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  R acc_r[4], acc_i[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) { acc_r[i] = 0; acc_i[i] = 0; }
+  for (int64_t k0 = kb; k0 < ke; k0 += BK) {
+#pragma unroll
+    for (int l = 0; l < (BM * BK) / 256; ++l) {
+      const int e = tid + l * 256;
+      const int r = e / BK, c = e % BK;
+      const int64_t m = m0 + r, k = k0 + c;
+      As[c][r] = (m < M && k < ke) ? A[m * K + k] : CT<T>::zero();
+    }
+    {
+      const int r = tid / BK, c = tid % BK;
+      const int64_t k = k0 + c;
+      Bs[c][r] = (r < N && k < ke) ? B[(int64_t)r * K + k] : CT<T>::zero();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < BK; ++kk) {
+      const T b = Bs[kk][ty];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const T a = As[kk][tx + 16 * i];
+        acc_r[i] = fma(a.x, b.x, acc_r[i]);
+        acc_r[i] = fma(-a.y, b.y, acc_r[i]);
+        acc_i[i] = fma(a.x, b.y, acc_i[i]);
+        acc_i[i] = fma(a.y, b.x, acc_i[i]);
+      }
+    }
+    __syncthreads();
+  }
+  if (ty < N) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t m = m0 + tx + 16 * i;
+      if (m < M) {
+        T v;
+        v.x = acc_r[i];
+        v.y = acc_i[i];
+        C[(int64_t)ty * M + m] = v;
+      }
+    }
+  }
+}
+
+// Split-K: slice z of gridDim.z computes the partial product over its k range into
+// P[z][N][M]; splitk_reduce_kernel sums the slices in order (deterministic).
+template <typename T, bool N16>
+__global__ void __launch_bounds__(256) gemm_simt_splitk_kernel(const T* __restrict__ A, const T* __restrict__ B,
+                                                               T* __restrict__ P, int64_t M, int64_t N, int64_t K,
+                                                               int64_t kchunk) {
+  const int64_t kb = (int64_t)blockIdx.z * kchunk;
+  const int64_t ke = kb + kchunk < K ? kb + kchunk : K;
+  if (N16)
+    gemm_simt_tile_n16<T>(A, B, P + (int64_t)blockIdx.z * M * N, M, N, K, (int64_t)blockIdx.x * BM, kb, ke);
+  else
+    gemm_simt_tile<T>(A, B, P + (int64_t)blockIdx.z * M * N, M, N, K, (int64_t)blockIdx.x * BM,
+                      (int64_t)blockIdx.y * BN, kb, ke);
+}
+
+template <typename T>
+__global__ void splitk_reduce_kernel(const T* __restrict__ P, int S, int64_t MN, T* __restrict__ C) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < MN; i += (int64_t)gridDim.x * blockDim.x) {
+    T acc = P[i];
+    for (int z = 1; z < S; ++z) {
+      const T v = P[(int64_t)z * MN + i];
+      acc.x += v.x;
+      acc.y += v.y;
+    }
+    C[i] = acc;
+  }
+}
+
 template <typename T>
 cudaError_t launch(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, cudaStream_t s) {
   if (M <= 0 || N <= 0) return cudaSuccess;
@@ -253,11 +339,51 @@ cudaError_t launch(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_splitk(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int S, T* P,
+                          cudaStream_t s) {
+  if (M <= 0 || N <= 0) return cudaSuccess;
+  const int64_t gx = (M + BM - 1) / BM, gy = (N + BN - 1) / BN;
+  if (gy > 65535 || S < 1 || S > 65535) return cudaErrorInvalidConfiguration;
+  int64_t kchunk = (K + S - 1) / S;
+  kchunk = (kchunk + BK - 1) / BK * BK;
+  const int Se = (int)((K + kchunk - 1) / kchunk);
+  if (N <= 16)
+    gemm_simt_splitk_kernel<T, true><<<dim3((unsigned)gx, 1u, (unsigned)Se), 256, 0, s>>>(A, B, P, M, N, K, kchunk);
+  else
+    gemm_simt_splitk_kernel<T, false><<<dim3((unsigned)gx, (unsigned)gy, (unsigned)Se), 256, 0, s>>>(A, B, P, M, N, K,
+                                                                                                   kchunk);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int64_t MN = M * N;
+  int64_t blocks = (MN + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  splitk_reduce_kernel<T><<<(unsigned)(blocks < 1 ? 1 : blocks), 256, 0, s>>>(P, Se, MN, C);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_zgemm_simt(const double2* A, const double2* B, double2* C, int64_t M, int64_t N,
                               int64_t K, cudaStream_t s) {
   return launch(A, B, C, M, N, K, s);
+}
+int gemm_splitk_slices(int64_t M, int64_t N, int64_t K) {
+  const int64_t tiles = ((M + BM - 1) / BM) * (N <= 16 ? 1 : (N + BN - 1) / BN);
+  if (tiles >= 2 * 152 || K < 8 * BK * 16) return 1;
+  int64_t S = (2 * 152) / tiles;
+  const int64_t kmax = K / (BK * 16);  // at least 256 k per slice
+  if (S > kmax) S = kmax;
+  if (S > 256) S = 256;
+  return S < 2 ? 1 : (int)S;
+}
+cudaError_t launch_zgemm_simt_splitk(const double2* A, const double2* B, double2* C, int64_t M, int64_t N, int64_t K,
+                                     int S, double2* P, cudaStream_t s) {
+  return launch_splitk(A, B, C, M, N, K, S, P, s);
+}
+cudaError_t launch_cgemm_simt_splitk(const float2* A, const float2* B, float2* C, int64_t M, int64_t N, int64_t K,
+                                     int S, float2* P, cudaStream_t s) {
+  return launch_splitk(A, B, C, M, N, K, S, P, s);
 }
 cudaError_t launch_gemm_simt_grouped(const GemmJob* jobs, int njobs, int is64, cudaStream_t s) {
   return is64 ? launch_grouped<double2>(jobs, njobs, s) : launch_grouped<float2>(jobs, njobs, s);

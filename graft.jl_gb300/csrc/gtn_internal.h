@@ -43,6 +43,9 @@ struct gtn_ctx_s {
   // transient workspace for one-shot contractions / factorisations
   void* ws = nullptr;
   size_t ws_bytes = 0;
+  // bump arena of one-shot contractions (stream-ordered reuse, grown to the largest need)
+  char* carena = nullptr;
+  size_t carena_cap = 0, carena_need = 0;
   void* cusolver = nullptr;
 };
 
@@ -180,6 +183,13 @@ struct GemmJob {
   int64_t M, N, K;
 };
 cudaError_t launch_gemm_simt_grouped(const GemmJob* jobs, int njobs, int is64, cudaStream_t s);
+// Split-K for GEMMs with few output tiles and a long K: the number of K slices (1 = no
+// split), and the launchers with a partial-sum workspace P of slices * M * N elements.
+int gemm_splitk_slices(int64_t M, int64_t N, int64_t K);
+cudaError_t launch_zgemm_simt_splitk(const double2* A, const double2* B, double2* C, int64_t M, int64_t N, int64_t K,
+                                     int S, double2* P, cudaStream_t s);
+cudaError_t launch_cgemm_simt_splitk(const float2* A, const float2* B, float2* C, int64_t M, int64_t N, int64_t K,
+                                     int S, float2* P, cudaStream_t s);
 // Skinny grouped GEMM (same contraction) for N <= 32; every job must pass gemm_skinny_fits.
 constexpr int kSkinnyMaxSmem = 96 * 1024;
 cudaError_t launch_gemm_skinny_grouped(const GemmJob* jobs, int njobs, int is64, cudaStream_t s);
@@ -262,6 +272,7 @@ struct PlanStep {
   int bfp16 = 0;                   // planes hold fp16 slices scaled per complex row by bmax
   float* bmax = nullptr;           // [N] row maxima of the static (fp16 planes)
   GatherTab tab;                   // offset tables of the running tensor's [M, K] view (tc steps)
+  int splitk = 1;                  // K slices of the SIMT GEMM (few output tiles, long K)
   double macs = 0;
 };
 
@@ -283,6 +294,11 @@ struct gtn_map_s {
   int64_t max_a = 0;       // largest A operand (elements, for permuted / split staging)
   int64_t max_apl = 0;     // largest split-plane staging (bf16 elements per plane * planes)
   int64_t max_mtc = 0;     // largest M of a tensor-core step (fp16 row maxima)
+  int64_t max_splitk = 0;  // largest split-K partial-sum workspace (complex elements)
+  bool oneshot = false;    // a one-shot contraction (gtn_contract): arena allocations, no tables
+  char* arena = nullptr;   // allocations come from here first (one-shot contractions)
+  size_t arena_cap = 0, arena_off = 0, arena_spill = 0;
+  void* skbuf = nullptr;   // that workspace
   float* amax = nullptr;   // [max_mtc] row maxima of the running operand (fp16 planes)
   // device workspace owned by the map
   void* buf0 = nullptr; void* buf1 = nullptr; void* abuf = nullptr;

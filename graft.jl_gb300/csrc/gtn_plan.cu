@@ -56,6 +56,16 @@ int64_t prod(const std::vector<int64_t>& d, const std::vector<int>& legs) {
 }
 
 template <typename T> cudaError_t dalloc(gtn_map map, T** p, size_t bytes) {
+  const size_t sz = ((bytes < 256 ? 256 : bytes) + 255) / 256 * 256;
+  if (map->oneshot) {
+    if (map->arena && map->arena_off + sz <= map->arena_cap) {
+      *p = reinterpret_cast<T*>(map->arena + map->arena_off);
+      map->arena_off += sz;
+      map->bytes += (int64_t)bytes;
+      return cudaSuccess;
+    }
+    map->arena_spill += sz;
+  }
   void* q = nullptr;
   cudaError_t e = cudaMalloc(&q, bytes < 256 ? 256 : bytes);
   if (e == cudaSuccess) {
@@ -90,7 +100,10 @@ cudaError_t upload_offsets(gtn_map map, const GroupSpec& g, int64_t n, const int
   }
   int64_t* d = nullptr;
   cudaError_t e = dalloc(map, &d, h.size() * sizeof(int64_t));
-  if (e == cudaSuccess) e = cudaMemcpy(d, h.data(), h.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  // stream-ordered: the buffer may be arena memory that earlier work on the stream reads
+  // (pageable source: the call returns once the data is staged, so h may go out of scope)
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d, h.data(), h.size() * sizeof(int64_t), cudaMemcpyHostToDevice, map->ctx->stream);
   *out = d;
   return e;
 }
@@ -435,6 +448,8 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
       map->max_a = std::max(map->max_a, st.M * st.K);
       if (st.tc) map->max_apl = std::max(map->max_apl, (int64_t)P * st.M * 2 * st.Kp);
       if (st.tc) map->max_mtc = std::max(map->max_mtc, st.M);
+      st.splitk = gemm_splitk_slices(st.M, st.N, st.K);
+      if (st.splitk > 1) map->max_splitk = std::max(map->max_splitk, (int64_t)st.splitk * st.M * st.N);
     }
 
     // ---- pack the static: B[n][k] = S[freeS(n), shared(k)] (conj applied) -------------
@@ -451,7 +466,8 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
         e = launch_conj_inplace(st.b64, st.N * st.K, ctx->stream);
         ctx->launches++;
       }
-      if (e == cudaSuccess) {
+      // (a one-shot FP64 contraction never reads the complex FP32 copy)
+      if (e == cudaSuccess && !(map->oneshot && precision == GTN_PREC_FP64)) {
         e = dalloc(map, &st.b32, (size_t)st.N * st.K * sizeof(float2));
         if (e == cudaSuccess) {
           const int64_t ne = st.N * st.K;
@@ -478,7 +494,7 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
       }
       if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("static packing: ") + cudaGetErrorString(e));
     }
-    if (statics && st.tc) {
+    if (statics && st.tc && !map->oneshot) {
       cudaError_t e = make_tab(map, st.mg, st.kg, st.M, st.K, &st.tab);
       if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("offset tables: ") + cudaGetErrorString(e));
     }
@@ -510,7 +526,7 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   bool ident = true;
   for (int a = 0; a < R; ++a) ident = ident && ypos[a] == a;
   map->fin_identity = ident;
-  if (statics) {
+  if (statics && !map->oneshot) {  // one-shot contractions skip the tables
     cudaError_t e = make_tab(map, map->fin_mg, map->fin_kg, map->fin_M, map->fin_K, &map->fin_tab);
     if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, std::string("offset tables: ") + cudaGetErrorString(e));
   }
@@ -532,16 +548,18 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   if (!alloc_ws) return GTN_OK;
 
   // ---- workspace admission, then allocation ------------------------------------------
-  int64_t max_t = map->max_t, max_a = map->max_a;
+  int64_t max_t = map->max_t, max_a = map->max_a, max_sk = map->max_splitk;
   if (map->fp64_alt) {
     max_t = std::max(max_t, map->fp64_alt->max_t);
     max_a = std::max(max_a, map->fp64_alt->max_a);
+    max_sk = std::max(max_sk, map->fp64_alt->max_splitk);
   }
   const size_t tbytes = (size_t)max_t * sizeof(double2);
   const size_t abytes = std::max<size_t>((size_t)max_a * sizeof(double2),
                                          (size_t)map->max_apl * sizeof(__nv_bfloat16));
   size_t freeb = 0, totalb = 0;
-  cudaMemGetInfo(&freeb, &totalb);
+  if (map->oneshot) freeb = SIZE_MAX;  // one-shot contraction: the arena or a failing cudaMalloc decides
+  else cudaMemGetInfo(&freeb, &totalb);
   const size_t need = 2 * tbytes + abytes + (size_t)(1u << 30);
   if (need > freeb)
     return set_err(ctx, GTN_ERR_MEMORY, "memory admission refused: map workspace " +
@@ -553,10 +571,14 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   if (is_fp16(precision) && map->max_mtc > 0 &&
       dalloc(map, &map->amax, (size_t)map->max_mtc * sizeof(float)) != cudaSuccess)
     return set_err(ctx, GTN_ERR_MEMORY, "map workspace allocation failed");
+  if (max_sk > 0 && dalloc(map, reinterpret_cast<double2**>(&map->skbuf), (size_t)max_sk * sizeof(double2)) !=
+                        cudaSuccess)
+    return set_err(ctx, GTN_ERR_MEMORY, "map workspace allocation failed");
   if (map->fp64_alt) {
     map->fp64_alt->buf0 = map->buf0;
     map->fp64_alt->buf1 = map->buf1;
     map->fp64_alt->abuf = map->abuf;
+    map->fp64_alt->skbuf = map->skbuf;
   }
   return GTN_OK;
 }
@@ -634,7 +656,11 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
         e = launch_gather_c128_to_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.K, A, s);
         prof_end(s, GTN_KERNEL_GATHER, 0.0);
         prof_begin(s);
-        if (e == cudaSuccess) e = launch_zgemm_simt(A, st.b64, static_cast<double2*>(out), st.M, st.N, st.K, s);
+        if (e == cudaSuccess && st.splitk > 1 && map->skbuf)
+          e = launch_zgemm_simt_splitk(A, st.b64, static_cast<double2*>(out), st.M, st.N, st.K, st.splitk,
+                                       static_cast<double2*>(map->skbuf), s);
+        else if (e == cudaSuccess)
+          e = launch_zgemm_simt(A, st.b64, static_cast<double2*>(out), st.M, st.N, st.K, s);
         prof_end(s, GTN_KERNEL_ZGEMM, 8.0 * st.macs);
         ctx->launches += 2;
       }
@@ -665,7 +691,11 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
         e = launch_gather_c64_to_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.K, A, s);
         prof_end(s, GTN_KERNEL_GATHER, 0.0);
         prof_begin(s);
-        if (e == cudaSuccess) e = launch_cgemm_simt(A, st.b32, static_cast<float2*>(out), st.M, st.N, st.K, s);
+        if (e == cudaSuccess && st.splitk > 1 && map->skbuf)
+          e = launch_cgemm_simt_splitk(A, st.b32, static_cast<float2*>(out), st.M, st.N, st.K, st.splitk,
+                                       static_cast<float2*>(map->skbuf), s);
+        else if (e == cudaSuccess)
+          e = launch_cgemm_simt(A, st.b32, static_cast<float2*>(out), st.M, st.N, st.K, s);
         prof_end(s, GTN_KERNEL_CGEMM, 8.0 * st.macs);
         ctx->launches += 2;
       } else {

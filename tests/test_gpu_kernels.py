@@ -187,3 +187,18 @@ def test_fp16x3_wide_dynamic_range(ctx):
     rows = np.linalg.norm(out - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
     assert np.all(rows[np.arange(M) != 7] < 1e-5)
     assert np.all(out[7] == 0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("N", [5, 16, 40])
+def test_contract_tall_skinny_splitk(ctx, prec, N):
+    # few output tiles, long K: the SIMT GEMM splits K over CTAs and sums the slices
+    # (64 x 16 tiles for N <= 16, 64 x 64 above)
+    rng = np.random.default_rng(13)
+    K, M = 70001, 48
+    a, b = crandn(rng, (K, M)), crandn(rng, (K, N))
+    from grafttn import _lib
+    out = ctx.download(ctx.contract([ctx.upload(a), ctx.upload(b)], [[1, -1], [1, -2]], [False, True], None,
+                                    _lib.PRECISIONS[prec]))
+    ref = a.T @ b.conj()
+    assert rel(out, ref) < (1e-12 if prec == "fp64" else 2e-5)
