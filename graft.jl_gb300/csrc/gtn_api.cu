@@ -327,3 +327,10 @@ int gtn_diag_scale(gtn_ctx ctx, int64_t rows, int64_t cols, const double* d_host
 }
 
 }  // extern "C"
+
+extern "C" int gtn_selftest_wait(gtn_ctx ctx, int64_t timeout_us) {
+  if (!ctx || timeout_us < 1 || timeout_us > 2000000) return set_err(ctx, GTN_ERR_INVALID, "gtn_selftest_wait: bad argument");
+  GTN_CUDA_TRY(ctx, launch_wait_selftest(ctx->d_errflag, (uint64_t)timeout_us * 1000ull, ctx->stream));
+  ctx->launches++;
+  return GTN_OK;
+}

@@ -64,7 +64,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 // Bounded wait on a phase parity.  Returns false on timeout or when another role of the
 // CTA has already aborted.
-__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                          uint64_t timeout_ns = kTimeoutNs) {
   uint64_t t0 = 0;
   for (uint32_t it = 0;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
@@ -72,9 +73,19 @@ __device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_fl
       if (*abort_flag) return false;
       const uint64_t now = globaltimer();
       if (t0 == 0) t0 = now;
-      else if (now - t0 > kTimeoutNs) return false;
+      else if (now - t0 > timeout_ns) return false;
     }
   }
+}
+
+// A wait that runs out: an mbarrier expecting one arrival that never comes.
+__global__ void wait_selftest_kernel(int* __restrict__ errflag, uint64_t timeout_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ volatile int no_abort;
+  mbar_init(&bar, 1);
+  no_abort = 0;
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  if (!mbar_wait(&bar, 0u, &no_abort, timeout_ns)) atomicCAS(errflag, 0, DEVERR_SELFTEST_TIMEOUT);
 }
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* tm, uint64_t* bar, int x,
@@ -916,4 +927,9 @@ cudaError_t launch_tc_gemm(const TcGemmArgs& a, int* errflag, cudaStream_t s, st
   if (n2 <= 64) return launch_bn<64>(a, errflag, s, why);
   if (n2 <= 128) return launch_bn<128>(a, errflag, s, why);
   return launch_bn<256>(a, errflag, s, why);
+}
+
+cudaError_t launch_wait_selftest(int* errflag, uint64_t timeout_ns, cudaStream_t s) {
+  wait_selftest_kernel<<<1, 1, 0, s>>>(errflag, timeout_ns);
+  return cudaGetLastError();
 }

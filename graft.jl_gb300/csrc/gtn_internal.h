@@ -24,7 +24,9 @@ struct GroupSpec {
 };
 
 // Device error codes written to the context's error flag by bounded waits.
-enum : int { DEVERR_NONE = 0, DEVERR_TMA_TIMEOUT = 1, DEVERR_MMA_TIMEOUT = 2, DEVERR_EPI_TIMEOUT = 3 };
+enum : int { DEVERR_NONE = 0, DEVERR_TMA_TIMEOUT = 1, DEVERR_MMA_TIMEOUT = 2, DEVERR_EPI_TIMEOUT = 3,
+             DEVERR_SELFTEST_TIMEOUT = 4 };
+cudaError_t launch_wait_selftest(int* errflag, uint64_t timeout_ns, cudaStream_t s);
 
 struct gtn_ctx_s {
   int device = 0;

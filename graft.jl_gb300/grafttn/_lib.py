@@ -75,6 +75,7 @@ SIGNATURES = {
     "gtn_diag_scale": (_i, [_p, _i64, _i64, _pd, _i, _p]),
     "gtn_copy2d": (_i, [_p, _i64, _i64, _p, _i64, _p, _i64]),
     "gtn_multidot_noalloc": (_i, [_p, _i64, _i, _p, _i64, _p, _p]),
+    "gtn_selftest_wait": (_i, [_p, _i64]),
 }
 
 

@@ -234,6 +234,13 @@ int gtn_copy2d(gtn_ctx ctx, int64_t rows, int64_t cols, const void* src, int64_t
  * side 0 scales column j by d[j] (U * diag(S)), side 1 scales row i by d[i] (diag(S) * Vh). */
 int gtn_diag_scale(gtn_ctx ctx, int64_t rows, int64_t cols, const double* d_host, int side, void* A);
 
+/* Failure-path self-test: one device thread waits on an mbarrier that nothing arrives at,
+ * with the same bounded-wait code as the tensor-core kernels but a limit of `timeout_us`
+ * microseconds (1..2000000); it then records a timeout in the context's error flag and
+ * returns.  The next gtn_ctx_sync reports GTN_ERR_TIMEOUT and clears the flag; the context
+ * stays usable.  No counterpart in the reference (its device-free code has no waits). */
+int gtn_selftest_wait(gtn_ctx ctx, int64_t timeout_us);
+
 #ifdef __cplusplus
 }
 #endif

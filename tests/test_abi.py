@@ -38,3 +38,14 @@ def test_host_metadata_without_gpu():
     assert len(G.kary_topology(4, 3).ids) == 85
     W = G.ttno_tensors(G.heisenberg(t))
     assert W[1].shape == (5, 5, 2, 2, 5) and W[0].shape == (5, 5, 2, 2, 1)
+
+
+def test_null_handles_are_rejected_without_a_gpu():
+    # argument checks run before any device call: the reference's ArgumentError surfaces
+    # as GTN_ERR_INVALID through the ABI
+    from grafttn import _lib
+    lib = _lib.lib()
+    assert lib.gtn_ctx_sync(None) == _lib.GTN_ERR_INVALID
+    assert lib.gtn_map_apply(None, None, None) == _lib.GTN_ERR_INVALID
+    assert lib.gtn_map_destroy(None) == _lib.GTN_ERR_INVALID
+    assert lib.gtn_selftest_wait(None, 1000) == _lib.GTN_ERR_INVALID
