@@ -113,10 +113,7 @@ def _unmat(ctx, M, shape, k):
 
 
 def _matmul(ctx, A, B, conjA=False, transA=False):
-    """op(A) @ B for device matrices via the contraction engine (FP64); B starts the chain
-    so that the conjugated operand is a static one."""
-    la = [1, -1] if transA else [-1, 1]
-    return ctx.contract([B.contiguous(), A.contiguous()], [[1, -2], la], [False, conjA])
+    return ctx.matmul(A, B, conjA, transA)
 
 
 def cbe_split(cache: EnvCache, psi: TTNS, H: TTNO, u, v, dz, maxdim, strategy: PredictorCBE, info=None):

@@ -135,6 +135,12 @@ class Context:
               "diag_scale")
         return A2
 
+    def matmul(self, A, B, conjA=False, transA=False):
+        """op(A) @ B for row-major device matrices, op = conj and / or transpose (FP64
+        contraction; B starts the chain so that the conjugated operand is a static)."""
+        la = [1, -1] if transA else [-1, 1]
+        return self.contract([B.contiguous(), A.contiguous()], [[1, -2], la], [False, conjA])
+
     def concat_cols(self, A, B):
         """[A B] for row-major matrices with equal row counts."""
         rows = A.shape[0]

@@ -104,6 +104,91 @@ def dmrg1(psi: TTNS, H: TTNO, nsweeps=10, tol=1e-10, krylovdim=20, precision="fp
     return psi, energies
 
 
+def expand_exact(cache: EnvCache, psi: TTNS, H: TTNO, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10,
+                 enr_atol=1e-12, precision="fp64"):
+    """3S subspace expansion of the bond n -> m with the exact predictor
+    (lib/GraftContractions/src/Contractions/expansion.jl:40-131, 240-272, 488-512): P = the
+    leading left singular vectors of mixing * H2 Theta (n-side legs x rest, at most
+    cap = min(maxdim, D + max_add)); its directions outside range(A_n) (left singular vectors
+    of P - Q Q^H P with Q spanning A_n, at most cap - D, enrichment tolerances atol / rtol)
+    are appended to A_n; the factor U of [A_n E] (at most cap columns) replaces A_n and
+    R = U^H A_n is absorbed into A_m (the state is unchanged: U U^H A_n = A_n)."""
+    ctx, t = psi.ctx, psi.topo
+    olddim = psi.tensors[n].shape[-1]
+    cap = min(maxdim, olddim + max_add)
+    if cap <= olddim or mixing == 0:
+        return False
+    move_center(psi, n, cache)
+    A = psi.tensors[n].contiguous()
+    sh = tuple(A.shape)
+    Am = A.reshape(-1, sh[-1])
+    theta = two_site_tensor(psi, n, m)
+    prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
+    h2 = eff_h2(cache, psi, H, n, m, prec)
+    Pt = h2(theta)
+    h2.close()
+    if mixing != 1:
+        Pt = ctx.scale(Pt, mixing)
+    P, _, _, _ = ctx.svd_trunc(Pt.reshape(Am.shape[0], -1).contiguous(), maxdim=cap)
+    room = min(max_add, cap - olddim)
+    expanded = Am
+    if room > 0 and Am.shape[0] > Am.shape[1]:
+        Q, _ = ctx.qr(Am)
+        Pc = ctx.axpby(-1.0, ctx.matmul(Q, ctx.matmul(Q, P, conjA=True, transA=True)), 1.0, P.contiguous())
+        E, sig, _, _ = ctx.svd_trunc(Pc, maxdim=room, atol=enr_atol, rtol=enr_rtol)
+        if E.shape[1] > 0:
+            E = ctx.axpby(-1.0, ctx.matmul(Q, ctx.matmul(Q, E, conjA=True, transA=True)), 1.0, E.contiguous())
+            expanded = ctx.concat_cols(Am, E)
+    U, _, _, _ = ctx.svd_trunc(expanded.contiguous(), maxdim=cap)
+    if U.shape[1] == olddim:
+        return False
+    R = ctx.matmul(U, Am, conjA=True, transA=True)
+    psi.tensors[n] = U.contiguous().reshape(sh[:-1] + (U.shape[1],))
+    psi.tensors[m] = absorb_on_leg(ctx, psi.tensors[m], R, t.childslot(m, n))
+    psi.center = m
+    cache.invalidate_edge(n, m)
+    return True
+
+
+def dmrg1_3s(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10, tol=1e-10, krylovdim=20,
+             mixing=1.0, max_add=8, enr_rtol=1e-10, enr_atol=1e-12, precision="fp64", rq_fp64=None,
+             lanczos_tol=1e-12, maxiter=100):
+    """Single-site DMRG with subspace expansion between sweeps (GroundState.jl:166-248,
+    exact predictor): dmrg1's local ground states, then expand_exact on every bond in
+    postorder with mixing(sweep) (a number or a function of the sweep); bonds grow by at
+    most max_add per sweep up to trunc.maxdim.  Returns (psi, energies per sweep)."""
+    if not H.ishermitian:
+        raise ValueError("dmrg1_3s: DMRG requires ishermitian(H) == true")
+    trunc = trunc or TruncationScheme(maxdim=100)
+    prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
+    if rq_fp64 is None:
+        rq_fp64 = prec != _lib.PREC_FP64
+    t = psi.topo
+    cache = EnvCache(t)
+    order = t.postorder()
+    bonds = [n for n in order if t.parent[n] >= 0]
+    energies = []
+    for sweep in range(nsweeps):
+        E = float("nan")
+        for n in list(order) + list(reversed(order)):
+            move_center(psi, n, cache)
+            h1 = eff_h1(cache, psi, H, n, prec)
+            E, v, _ = h1.lanczos_min(psi.tensors[n], krylovdim=krylovdim, tol=lanczos_tol, maxiter=maxiter,
+                                     rq_fp64=rq_fp64)
+            h1.close()
+            psi.tensors[n] = v
+            cache.invalidate_node(n)
+        alpha = mixing(sweep + 1) if callable(mixing) else mixing
+        if alpha != 0:
+            for n in bonds:
+                expand_exact(cache, psi, H, n, t.parent[n], trunc.maxdim or (1 << 30), max_add, alpha,
+                             enr_rtol, enr_atol, prec)
+        energies.append(float(E))
+        if len(energies) >= 2 and abs(energies[-1] - energies[-2]) < tol:
+            break
+    return psi, energies
+
+
 class TDVP1:
     """One-site TDVP with order-2 splitting (tdvp.jl:31-44, 171-301)."""
 

@@ -952,6 +952,79 @@ def dmrg1(psi, Ws, nsweeps=10, tol=1e-10, krylovdim=20, lanczos_tol=1e-12):
     return psi, energies
 
 
+def _svd_keep(M, maxdim=None, atol=0.0, rtol=0.0):
+    """Left singular vectors kept by TruncationScheme(maxdim, atol, rtol)."""
+    U, S, _ = np.linalg.svd(M, full_matrices=False)
+    r = truncation_rank(S, maxdim, atol, rtol)
+    return U[:, :r], S[:r]
+
+
+def expand_exact(psi, Ws, cache, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10, enr_atol=1e-12):
+    """3S subspace expansion of the bond n -> m with the exact predictor (expansion.jl:40-131,
+    240-272, 488-512): the leading left singular vectors P of mixing * H2 Theta (n-side
+    legs x rest, at most cap = min(maxdim, D + max_add) of them); the directions of P
+    outside range(A_n) (left singular vectors of N^H P with N the complement of range(A_n),
+    at most cap - D, atol / rtol enrichment tolerances) are appended to A_n; the factor U of
+    [A_n E] (at most cap columns) replaces A_n and R = U^H A_n is absorbed into A_m."""
+    t = psi.topo
+    olddim = psi.tensors[n].shape[-1]
+    cap = min(maxdim, olddim + max_add)
+    if cap <= olddim or mixing == 0:
+        return
+    move_center(psi, n, cache.invalidate_edge)
+    A = psi.tensors[n]
+    sh = A.shape
+    Am = A.reshape(-1, sh[-1])
+    theta = two_site_tensor(psi, n, m)
+    P = (mixing * eff_h2(cache, psi, Ws, n, m)(theta)).reshape(Am.shape[0], -1)
+    P, _ = _svd_keep(P, cap)
+    room = min(max_add, cap - olddim)
+    expanded = Am
+    if room > 0 and Am.shape[0] > Am.shape[1]:
+        U, S, _ = np.linalg.svd(Am, full_matrices=True)
+        rank = int(np.sum(S > 1e-14 * max(S[0], 1e-300))) if S.size else 0
+        N = U[:, rank:]
+        if N.shape[1] > 0:
+            Um, _ = _svd_keep(N.conj().T @ P, room, enr_atol, enr_rtol)
+            if Um.shape[1] > 0:
+                expanded = np.concatenate([Am, N @ Um], axis=1)
+    U, _ = _svd_keep(expanded, cap)
+    if U.shape[1] == olddim:
+        return
+    R = U.conj().T @ Am
+    psi.tensors[n] = U.reshape(sh[:-1] + (U.shape[1],))
+    psi.tensors[m] = absorb_on_leg(psi.tensors[m], R, t.childslot(m, n))
+    psi.center = m
+    cache.invalidate_edge(n, m)
+
+
+def dmrg1_3s(psi, Ws, maxdim=100, nsweeps=10, tol=1e-10, krylovdim=20, mixing=1.0, max_add=8,
+             enr_rtol=1e-10, enr_atol=1e-12, lanczos_tol=1e-12):
+    """Single-site DMRG with subspace expansion after every sweep (GroundState.jl:166-248,
+    exact predictor): dmrg1's local updates, then expand_exact on every bond in postorder."""
+    t = psi.topo
+    cache = EnvCache(t)
+    energies = []
+    order = t.postorder()
+    bonds = [n for n in order if t.parent[n] >= 0]
+    for sweep in range(nsweeps):
+        E = float("nan")
+        for n in list(order) + list(reversed(order)):
+            move_center(psi, n, cache.invalidate_edge)
+            h1 = eff_h1(cache, psi, Ws, n)
+            E, v, _ = lanczos_min(h1, psi.tensors[n], krylovdim=krylovdim, tol=lanczos_tol)
+            psi.tensors[n] = v
+            cache.invalidate_node(n)
+        alpha = mixing(sweep + 1) if callable(mixing) else mixing
+        if alpha != 0:
+            for n in bonds:
+                expand_exact(psi, Ws, cache, n, t.parent[n], maxdim, max_add, alpha, enr_rtol, enr_atol)
+        energies.append(float(E))
+        if len(energies) >= 2 and abs(energies[-1] - energies[-2]) < tol:
+            break
+    return psi, energies
+
+
 def tdvp1_step(psi, Ws, dz, cache=None, krylovdim=30, tol=1e-12):
     """Order-2 TDVP1 step (tdvp.jl:171-195): forward half sweep with the turning site
     evolved by the full dz, then the reverse half sweep skipping that site."""

@@ -194,3 +194,22 @@ def test_dmrg1_full_bonds_vs_ed(ctx, precision):
     _, Es = G.dmrg1(psi, W, nsweeps=10, precision=precision)
     assert psi.bond_dims() == dims
     assert abs(Es[-1] - E0) / abs(E0) < 1e-10
+
+
+def test_dmrg1_3s_matches_oracle_and_ed(ctx):
+    # one-site DMRG with exact subspace expansion from bond 1: the same bond growth as the
+    # oracle after every sweep, and the exact ground-state energy at the end
+    topo = G.star_topology(3, 2)
+    W = G.TTNO.from_hamiltonian(G.tfi(topo, g=0.9), ctx)
+    Hd = O.dense_hamiltonian(O.tfi(O.star_topology(3, 2), g=0.9))
+    E0, _ = O.exact_groundstate(Hd)
+    psi = G.random_ttns(np.random.default_rng(16), topo, 2, 1, ctx=ctx)
+    o = oracle_state(psi)
+    _, Es = G.dmrg1_3s(psi, W, G.TruncationScheme(maxdim=8), nsweeps=3, max_add=4)
+    _, Eo = O.dmrg1_3s(o, O.ttno_nn(O.tfi(O.star_topology(3, 2), g=0.9)), maxdim=8, nsweeps=3, max_add=4)
+    assert psi.bond_dims() == O.bond_dims(o), (psi.bond_dims(), O.bond_dims(o))
+    # the first sweep precedes any expansion; later sweeps may differ by which of several
+    # equally weighted predictor directions each side kept
+    assert abs(Es[0] - Eo[0]) < 1e-9 * abs(Eo[0]), (Es, Eo)
+    _, Es = G.dmrg1_3s(psi, W, G.TruncationScheme(maxdim=8), nsweeps=10, max_add=4)
+    assert abs(Es[-1] - E0) / abs(E0) < 1e-10

@@ -99,6 +99,18 @@ def test_dmrg1_full_bonds_vs_ed():
     assert abs(Es[-1] - E0) < 1e-10
 
 
+def test_dmrg1_3s_grows_bonds_to_ed():
+    # GroundState.jl:166-248: from bond 1, expansion between one-site sweeps reaches the
+    # exact ground state of the 7-site star once the bonds have grown
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo, g=0.9)
+    E0, _ = O.exact_groundstate(O.dense_hamiltonian(H))
+    psi = O.random_ttns(np.random.default_rng(6), topo, 2, 1)
+    _, Es = O.dmrg1_3s(psi, O.ttno_nn(H), maxdim=8, nsweeps=12, max_add=4)
+    assert max(O.bond_dims(psi)) > 1
+    assert abs(Es[-1] - E0) < 1e-9
+
+
 def test_tdvp2_full_rank_vs_exact():
     # full bond dimension: every two-site and one-site projector is the identity, so the
     # order-2 TDVP2 step equals exact evolution (tdvp.jl:307-431)
