@@ -513,7 +513,7 @@ def run_dmrg(args):
            "model": "Heisenberg XX+YY+ZZ (Pauli), dense ComplexF64", "krylovdim": 20, "runs": {}}
     for prec in args.dmrg_precisions.split(","):
         psi = psi0.copy()
-        stats = {}
+        stats = {"timing": True}
         times, energies = [], []
         for sweep in range(args.dmrg_sweeps):
             torch.cuda.synchronize()
@@ -524,7 +524,8 @@ def run_dmrg(args):
             times.append(time.perf_counter() - t0)
             energies.append(Es[-1])
         out["runs"][prec] = {"sweep_s": times, "energies": energies, "matvecs": stats.get("matvecs"),
-                             "steps": stats.get("steps")}
+                             "steps": stats.get("steps"),
+                             "phase_s": {k[2:]: round(v, 3) for k, v in stats.items() if k.startswith("t_")}}
     runs = out["runs"]
     if "fp64" in runs and len(runs) > 1:
         e64 = runs["fp64"]["energies"][-1]

@@ -141,41 +141,45 @@ __device__ __forceinline__ void gather_tile(const Tin* __restrict__ T, const Gro
 // before the transpose (the gathers are latency-bound at 32 x 32).
 constexpr int kTabRows = 64;
 
-template <typename Tin, class Writer>
+// TM x TK tile of 2048 elements (8 loads in flight per thread).  64 x 32 in general; 256 x 8
+// when the rows are the unit-stride index, so that every k reads a 4 KB contiguous run
+// (a 32-wide tile over far-apart k legs touches 32 pages per tile).
+template <typename Tin, class Writer, int TM, int TK>
 __global__ void __launch_bounds__(256) gather_tab_kernel(const Tin* __restrict__ T, TabOff off, int64_t M,
                                                          int64_t K, int64_t Kw, int m_fast, Writer w) {
-  __shared__ int64_t offM[kTabRows];
-  __shared__ int64_t offK[32];
-  __shared__ Tin tile[kTabRows][33];
+  static_assert(TM * TK == 2048, "2048 elements per tile");
+  __shared__ int64_t offM[TM];
+  __shared__ int64_t offK[TK];
+  __shared__ Tin tile[TM][TK + 1];
   const int tid = threadIdx.x + 32 * threadIdx.y;
-  const int64_t m0 = (int64_t)blockIdx.x * kTabRows, k0 = (int64_t)blockIdx.y * 32;
-  if (tid < kTabRows) {
-    offM[tid] = m0 + tid < M ? off.m(m0 + tid) : 0;
-  } else if (tid < kTabRows + 32) {
-    const int j = tid - kTabRows;
-    offK[j] = k0 + j < K ? off.k(k0 + j) : 0;
+  const int64_t m0 = (int64_t)blockIdx.x * TM, k0 = (int64_t)blockIdx.y * TK;
+  for (int i = tid; i < TM + TK; i += 256) {
+    if (i < TM)
+      offM[i] = m0 + i < M ? off.m(m0 + i) : 0;
+    else
+      offK[i - TM] = k0 + (i - TM) < K ? off.k(k0 + (i - TM)) : 0;
   }
   __syncthreads();
-  Tin v[kTabRows / 8];
+  Tin v[8];
 #pragma unroll
-  for (int it = 0; it < kTabRows / 8; ++it) {
+  for (int it = 0; it < 8; ++it) {
     const int e = it * 256 + tid;
-    const int im = m_fast ? (e % kTabRows) : (e >> 5);
-    const int ik = m_fast ? (e / kTabRows) : (e & 31);
+    const int im = m_fast ? (e % TM) : (e / TK);
+    const int ik = m_fast ? (e / TM) : (e % TK);
     v[it] = (m0 + im < M && k0 + ik < K) ? T[offM[im] + offK[ik]] : Zero<Tin>::v();
   }
 #pragma unroll
-  for (int it = 0; it < kTabRows / 8; ++it) {
+  for (int it = 0; it < 8; ++it) {
     const int e = it * 256 + tid;
-    const int im = m_fast ? (e % kTabRows) : (e >> 5);
-    const int ik = m_fast ? (e / kTabRows) : (e & 31);
+    const int im = m_fast ? (e % TM) : (e / TK);
+    const int ik = m_fast ? (e / TM) : (e % TK);
     tile[im][ik] = v[it];
   }
   __syncthreads();
 #pragma unroll
-  for (int it = 0; it < kTabRows / 8; ++it) {
+  for (int it = 0; it < 8; ++it) {
     const int e = it * 256 + tid;
-    const int r = e >> 5, c = e & 31;
+    const int r = e / TK, c = e % TK;
     if (m0 + r < M && k0 + c < Kw) w(m0 + r, k0 + c, tile[r][c]);
   }
 }
@@ -184,10 +188,17 @@ template <typename Tin, class Writer>
 cudaError_t launch_gather_tab(const Tin* T, const int64_t* om, const int64_t* ok, int64_t M, int64_t K, int64_t Kw,
                               int m_fast, const Writer& w, cudaStream_t s) {
   if (M <= 0 || Kw <= 0) return cudaSuccess;
-  const int64_t gy = (Kw + 31) / 32, gx = (M + kTabRows - 1) / kTabRows;
-  if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
-  gather_tab_kernel<Tin, Writer><<<dim3((unsigned)gx, (unsigned)gy), dim3(32, 8), 0, s>>>(T, TabOff{om, ok}, M, K, Kw,
-                                                                                         m_fast, w);
+  if (m_fast) {
+    const int64_t gy = (Kw + 7) / 8, gx = (M + 255) / 256;
+    if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
+    gather_tab_kernel<Tin, Writer, 256, 8><<<dim3((unsigned)gx, (unsigned)gy), dim3(32, 8), 0, s>>>(
+        T, TabOff{om, ok}, M, K, Kw, m_fast, w);
+  } else {
+    const int64_t gy = (Kw + 31) / 32, gx = (M + 63) / 64;
+    if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
+    gather_tab_kernel<Tin, Writer, 64, 32><<<dim3((unsigned)gx, (unsigned)gy), dim3(32, 8), 0, s>>>(
+        T, TabOff{om, ok}, M, K, Kw, m_fast, w);
+  }
   return cudaGetLastError();
 }
 
@@ -275,43 +286,49 @@ struct Split16Writer {
 
 // amax[m] = max over k of max(|re|, |im|) of the K-major gather (atomic max of the
 // non-negative float bits; amax zeroed before the launch).
-template <typename Tin, class Off>
+template <typename Tin, class Off, int TM, int TK>
 __global__ void __launch_bounds__(256) rowmax_kernel(const Tin* __restrict__ T, Off off, int64_t M, int64_t K,
                                                      int m_fast, float* __restrict__ amax) {
-  constexpr int R = 64;  // rows per tile; every thread keeps R / 8 loads in flight
-  __shared__ int64_t offM[R];
-  __shared__ int64_t offK[32];
-  __shared__ float tile[R][33];
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + 32 * ty;
-  const int64_t m0 = (int64_t)blockIdx.x * R, k0 = (int64_t)blockIdx.y * 32;
-  if (tid < R) {
-    offM[tid] = m0 + tid < M ? off.m(m0 + tid) : 0;
-  } else if (tid < R + 32) {
-    const int j = tid - R;
-    offK[j] = k0 + j < K ? off.k(k0 + j) : 0;
+  // TM x TK = 2048 elements per tile (8 loads in flight per thread); 256 x 8 when the rows
+  // are the unit-stride index (long contiguous runs per k), else 64 x 32
+  static_assert(TM * TK == 2048 && TK <= 32, "tile shape");
+  __shared__ int64_t offM[TM];
+  __shared__ int64_t offK[TK];
+  __shared__ float tile[TM][TK + 1];
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  const int64_t m0 = (int64_t)blockIdx.x * TM, k0 = (int64_t)blockIdx.y * TK;
+  for (int i = tid; i < TM + TK; i += 256) {
+    if (i < TM)
+      offM[i] = m0 + i < M ? off.m(m0 + i) : 0;
+    else
+      offK[i - TM] = k0 + (i - TM) < K ? off.k(k0 + (i - TM)) : 0;
   }
   __syncthreads();
-  float v[R / 8];
+  float v[8];
 #pragma unroll
-  for (int it = 0; it < R / 8; ++it) {
+  for (int it = 0; it < 8; ++it) {
     const int e = it * 256 + tid;
-    const int im = m_fast ? (e % R) : (e >> 5);
-    const int ik = m_fast ? (e / R) : (e & 31);
+    const int im = m_fast ? (e % TM) : (e / TK);
+    const int ik = m_fast ? (e / TM) : (e % TK);
     v[it] = (m0 + im < M && k0 + ik < K) ? absmax2(T[offM[im] + offK[ik]]) : 0.f;
   }
 #pragma unroll
-  for (int it = 0; it < R / 8; ++it) {
+  for (int it = 0; it < 8; ++it) {
     const int e = it * 256 + tid;
-    const int im = m_fast ? (e % R) : (e >> 5);
-    const int ik = m_fast ? (e / R) : (e & 31);
+    const int im = m_fast ? (e % TM) : (e / TK);
+    const int ik = m_fast ? (e / TM) : (e % TK);
     tile[im][ik] = v[it];
   }
   __syncthreads();
-  for (int r = ty; r < R; r += 8) {
-    float x = tile[r][tx];
+  // row r's TK values sit on TK consecutive lanes: segmented max, one atomic per row
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
-    if (tx == 0 && m0 + r < M && x > 0.f) atomicMax(reinterpret_cast<unsigned int*>(amax) + m0 + r, __float_as_uint(x));
+  for (int it = 0; it < 8; ++it) {
+    const int e = it * 256 + tid;
+    const int r = e / TK, c = e % TK;
+    float x = tile[r][c];
+#pragma unroll
+    for (int o = TK / 2; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (c == 0 && m0 + r < M && x > 0.f) atomicMax(reinterpret_cast<unsigned int*>(amax) + m0 + r, __float_as_uint(x));
   }
 }
 
@@ -758,9 +775,17 @@ static cudaError_t launch_rowmax(const Tin* T, const Off& off, int m_fast, int64
   if (M <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(amax, 0, (size_t)M * sizeof(float), s);
   if (e != cudaSuccess || K <= 0) return e;
-  const int64_t gx = (M + 63) / 64, gy = (K + 31) / 32;
-  if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
-  rowmax_kernel<Tin, Off><<<dim3((unsigned)gx, (unsigned)gy), dim3(32, 8), 0, s>>>(T, off, M, K, m_fast, amax);
+  if (m_fast) {
+    const int64_t gx = (M + 255) / 256, gy = (K + 7) / 8;
+    if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
+    rowmax_kernel<Tin, Off, 256, 8><<<dim3((unsigned)gx, (unsigned)gy), dim3(32, 8), 0, s>>>(T, off, M, K, m_fast,
+                                                                                           amax);
+  } else {
+    const int64_t gx = (M + 63) / 64, gy = (K + 31) / 32;
+    if (gy > 65535 || gx > 2147483647LL) return cudaErrorInvalidConfiguration;
+    rowmax_kernel<Tin, Off, 64, 32><<<dim3((unsigned)gx, (unsigned)gy), dim3(32, 8), 0, s>>>(T, off, M, K, m_fast,
+                                                                                           amax);
+  }
   return cudaGetLastError();
 }
 cudaError_t launch_rowmax_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,

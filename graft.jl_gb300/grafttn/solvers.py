@@ -19,8 +19,10 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
           krylovdim=20, precision="fp64", rq_fp64=None, lanczos_tol=1e-12, maxiter=100,
           verbose=False, stats=None):
     """Two-site DMRG; returns (psi, energies per sweep).  ``precision`` selects the map
-    arithmetic; with a mixed mode the energy of every local solve is the FP64 Rayleigh
-    quotient of its eigenvector (``rq_fp64`` defaults to True for mixed modes)."""
+    arithmetic.  With a mixed mode the energy that closes each sweep (the one returned and
+    used for the convergence test) is the FP64 Rayleigh quotient of the last local
+    eigenvector (``rq_fp64`` defaults to True for mixed modes); the other local solves keep
+    their mixed-precision Ritz values, which nothing downstream reads."""
     if not H.ishermitian:
         raise ValueError("dmrg2: DMRG requires ishermitian(H) == true")
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
@@ -53,8 +55,10 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
             tt = mark("t_merge", tt)
             h2 = eff_h2(cache, psi, H, n, m, prec)
             tt = mark("t_env_and_map", tt)
+            last = step == len(sched) - 1 or (stats is not None and stats.get("max_steps") is not None
+                                               and step == stats["max_steps"] - 1)
             E, v, info = h2.lanczos_min(theta, krylovdim=krylovdim, tol=lanczos_tol, maxiter=maxiter,
-                                        rq_fp64=rq_fp64)
+                                        rq_fp64=rq_fp64 and last)
             tt = mark("t_lanczos", tt)
             if stats is not None:
                 stats["matvecs"] = stats.get("matvecs", 0) + info["matvecs"]
@@ -88,11 +92,12 @@ def dmrg1(psi: TTNS, H: TTNO, nsweeps=10, tol=1e-10, krylovdim=20, precision="fp
     energies = []
     for sweep in range(nsweeps):
         E = float("nan")
-        for n in list(order) + list(reversed(order)):
+        seq = list(order) + list(reversed(order))
+        for i, n in enumerate(seq):
             move_center(psi, n, cache)
             h1 = eff_h1(cache, psi, H, n, prec)
             E, v, info = h1.lanczos_min(psi.tensors[n], krylovdim=krylovdim, tol=lanczos_tol, maxiter=maxiter,
-                                        rq_fp64=rq_fp64)
+                                        rq_fp64=rq_fp64 and i == len(seq) - 1)
             h1.close()
             if stats is not None:
                 stats["matvecs"] = stats.get("matvecs", 0) + info["matvecs"]
@@ -170,11 +175,12 @@ def dmrg1_3s(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=
     energies = []
     for sweep in range(nsweeps):
         E = float("nan")
-        for n in list(order) + list(reversed(order)):
+        seq = list(order) + list(reversed(order))
+        for i, n in enumerate(seq):
             move_center(psi, n, cache)
             h1 = eff_h1(cache, psi, H, n, prec)
             E, v, _ = h1.lanczos_min(psi.tensors[n], krylovdim=krylovdim, tol=lanczos_tol, maxiter=maxiter,
-                                     rq_fp64=rq_fp64)
+                                     rq_fp64=rq_fp64 and i == len(seq) - 1)
             h1.close()
             psi.tensors[n] = v
             cache.invalidate_node(n)
