@@ -205,6 +205,35 @@ __global__ void row_phase_conj_kernel(double2* __restrict__ A, int64_t rows, int
   }
 }
 
+// Thick-restart basis rotation, in place.  A block stages its kRotRows rows of all m basis
+// vectors in shared memory before it writes any of them, and blocks own disjoint rows, so the
+// kept combinations can overwrite the leading columns directly.
+constexpr int kRotRows = 32;
+constexpr int kRotThreads = 128;
+
+__global__ void __launch_bounds__(kRotThreads) basis_rotate_kernel(double2* __restrict__ V, int64_t ldv, int m,
+                                                                   int k, const double* __restrict__ Q,
+                                                                   int64_t n) {
+  __shared__ double2 tile[kMaxJ][kRotRows];
+  const int64_t row0 = (int64_t)blockIdx.x * kRotRows;
+  const int r = threadIdx.x % kRotRows, g = threadIdx.x / kRotRows;
+  constexpr int kGroups = kRotThreads / kRotRows;
+  const bool live = row0 + r < n;
+  for (int i = g; i < m; i += kGroups)
+    tile[i][r] = live ? V[(int64_t)i * ldv + row0 + r] : make_double2(0.0, 0.0);
+  __syncthreads();
+  if (!live) return;
+  for (int j = g; j < k; j += kGroups) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int i = 0; i < m; ++i) {
+      const double q = __ldg(Q + (int64_t)i * k + j);
+      acc.x += q * tile[i][r].x;
+      acc.y += q * tile[i][r].y;
+    }
+    V[(int64_t)j * ldv + row0 + r] = acc;
+  }
+}
+
 inline unsigned grid_for(int64_t n) {
   int64_t b = (n + 255) / 256;
   if (b > 152 * 8) b = 152 * 8;
@@ -231,6 +260,16 @@ cudaError_t launch_lincomb(double2* w, double2 beta, const double2* V, int64_t l
                            const double2* coef, double2 cscale, int64_t n, cudaStream_t s) {
   if (J > kMaxJ) return cudaErrorInvalidValue;
   lincomb_kernel<<<grid_for(n), 256, 0, s>>>(w, beta, V, ldv, J, coef, cscale, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_basis_rotate(double2* V, int64_t ldv, int m, int k, const double* Q, int64_t n,
+                                cudaStream_t s) {
+  if (m > kMaxJ || k > m || k < 0) return cudaErrorInvalidValue;
+  if (k == 0 || n <= 0) return cudaSuccess;
+  const int64_t blocks = (n + kRotRows - 1) / kRotRows;
+  if (blocks > 0x7fffffff) return cudaErrorInvalidValue;
+  basis_rotate_kernel<<<(unsigned)blocks, kRotThreads, 0, s>>>(V, ldv, m, k, Q, n);
   return cudaGetLastError();
 }
 

@@ -244,6 +244,9 @@ cudaError_t launch_lincomb(double2* w, double2 beta, const double2* V, int64_t l
                            cudaStream_t s);
 cudaError_t launch_axpby(int64_t n, double2 a, const double2* x, double2 b, double2* y,
                          cudaStream_t s);
+// In place: V_j <- sum_{i<m} Q[i * k + j] V_i for j < k (k <= m <= 64, Q real, device).
+cudaError_t launch_basis_rotate(double2* V, int64_t ldv, int m, int k, const double* Q, int64_t n,
+                                cudaStream_t s);
 cudaError_t launch_c64_to_c128(const float2* x, double2* y, int64_t n, cudaStream_t s);
 cudaError_t launch_fill_c128(double2* x, double2 v, int64_t n, cudaStream_t s);
 cudaError_t launch_conj_inplace(double2* x, int64_t n, cudaStream_t s);

@@ -6,7 +6,9 @@
 // precision mode), then runs two passes of classical Gram-Schmidt against the whole basis
 // in FP64 (batched projections h = V^H w and one linear combination per pass), then
 // normalises.  Only the tridiagonal coefficients cross to the host; the small symmetric
-// eigenproblem is solved there by cyclic Jacobi rotations.
+// eigenproblem is solved there by cyclic Jacobi rotations.  The eigensolver restarts thick:
+// the lowest Ritz vectors are rotated in place at the front of the basis and the expansion
+// continues from the residual direction.
 #include "gtn_internal.h"
 
 #include <algorithm>
@@ -71,7 +73,8 @@ struct Krylov {
   gtn_ctx ctx;
   int64_t n;
   double2* V;       // (kd+1) x n
-  double2* coef;    // device coefficient area: [0,64) h1, [64,128) h2, [128] norm^2, [192,256) lincomb
+  double2* coef;    // device coefficient area: [0,64) h1, [64,128) h2, [128] norm^2, [192,256) lincomb,
+                    // [256, 2304) kept-Ritz rotation matrix (doubles)
   double2* part;    // multidot partials
   int nblk;
 };
@@ -98,7 +101,8 @@ int krylov_setup(gtn_map map, int kd, Krylov* K) {
     map->kv_cap = kd + 1;
   }
   if (!map->kcoef) {
-    if (cudaMalloc(&map->kcoef, 256 * sizeof(double2)) != cudaSuccess)
+    // [0, 256): coefficient slots; [256, 256 + 2048): kept-Ritz rotation (kMaxKrylov^2 doubles)
+    if (cudaMalloc(&map->kcoef, (256 + 2048) * sizeof(double2)) != cudaSuccess)
       return set_err(ctx, GTN_ERR_MEMORY, "Krylov coefficient allocation failed");
     map->owned.push_back(map->kcoef);
   }
@@ -154,18 +158,21 @@ int normalize(Krylov& K, double2* x, double* nrm) {
   return GTN_OK;
 }
 
-// One Lanczos expansion from V[0] (unit norm).  Fills a[0..m), b[0..m) and returns m (the
-// number of basis vectors).  Stops early at an invariant subspace, or when `stop` says so.
+// Lanczos expansion of the basis from column j0 (V[j0] unit norm and orthogonal to V[0..j0))
+// up to kd columns.  Fills a[j0..m), b[j0..m) and returns m (the number of basis vectors);
+// V[m] then holds the normalised residual direction and b[m-1] its norm.  Stops early at an
+// invariant subspace, or when `stop` says so.
 template <class Stop>
-int lanczos_expand(Krylov& K, int kd, int precision, std::vector<double>& a, std::vector<double>& b,
+int lanczos_expand(Krylov& K, int j0, int kd, int precision, std::vector<double>& a, std::vector<double>& b,
                    int* m_out, int* matvecs, bool* breakdown, Stop stop) {
   gtn_ctx ctx = K.ctx;
   cudaStream_t s = ctx->stream;
-  a.assign(kd, 0.0);
-  b.assign(kd, 0.0);
+  a.resize(kd, 0.0);
+  b.resize(kd, 0.0);
+  for (int j = j0; j < kd; ++j) a[j] = b[j] = 0.0;
   *breakdown = false;
   int m = kd;
-  for (int j = 0; j < kd; ++j) {
+  for (int j = j0; j < kd; ++j) {
     double2* vj = K.V + (int64_t)j * K.n;
     double2* w = K.V + (int64_t)(j + 1) * K.n;
     int st = map_run(K.map, precision, vj, w);
@@ -201,18 +208,36 @@ int lanczos_expand(Krylov& K, int kd, int precision, std::vector<double>& a, std
   return GTN_OK;
 }
 
-void tridiag_eig(int m, const std::vector<double>& a, const std::vector<double>& b, std::vector<double>& w,
-                 std::vector<double>& Q) {
+// Eigen-decomposition of the projected matrix of a thick-restarted Lanczos basis: the first k
+// columns are kept Ritz vectors (diagonal a[i], coupled to column k by the arrow entries
+// s[i]), the rest a Lanczos tridiagonal (diagonal a, off-diagonal b).  k = 0 is the plain
+// tridiagonal case.
+void projected_eig(int m, int k, const std::vector<double>& a, const std::vector<double>& b,
+                   const std::vector<double>& s, std::vector<double>& w, std::vector<double>& Q) {
   std::vector<double> T((size_t)m * m, 0.0);
   for (int i = 0; i < m; ++i) {
     T[(size_t)i * m + i] = a[i];
-    if (i + 1 < m) {
+    if (i >= k && i + 1 < m) {
       T[(size_t)i * m + i + 1] = b[i];
       T[(size_t)(i + 1) * m + i] = b[i];
     }
   }
+  if (k < m)
+    for (int i = 0; i < k; ++i) {
+      T[(size_t)i * m + k] = s[i];
+      T[(size_t)k * m + i] = s[i];
+    }
   jacobi_eig(m, T, w, Q);
 }
+
+void tridiag_eig(int m, const std::vector<double>& a, const std::vector<double>& b, std::vector<double>& w,
+                 std::vector<double>& Q) {
+  projected_eig(m, 0, a, b, {}, w, Q);
+}
+
+// Kept Ritz vectors per restart: about three fifths of the Krylov dimension, as KrylovKit
+// (0.10) keeps in its restarted Lanczos eigsolve, the solver behind the reference's hook.
+int thick_keep(int kd, int m) { return std::max(0, std::min((3 * kd + 2) / 5, m - 1)); }
 
 }  // namespace
 
@@ -240,35 +265,62 @@ extern "C" int gtn_lanczos_min(gtn_map map, void* xv, int krylovdim, double tol,
   st = normalize(K, K.V, &nrm);
   if (st != GTN_OK) return st;
   if (nrm == 0) return set_err(ctx, GTN_ERR_INVALID, "zero start vector");
-  std::vector<double> a, b, w, Q;
-  for (int it = 0; it < std::max(1, maxiter); ++it) {
+  // Thick-restarted Lanczos (Wu and Simon, 2000): a restart keeps the lowest Ritz vectors
+  // (rotated in place at the front of the basis) and the residual direction, so that each
+  // restart adds kd - keep matvecs instead of rebuilding the basis from one vector.
+  std::vector<double> a, b, s, w, Q;
+  int k = 0;  // kept Ritz vectors at the front of V
+  const int maxit = std::max(1, maxiter);
+  for (int it = 0; it < maxit; ++it) {
     restarts = it + 1;
     int m = 0;
     bool brk = false;
     auto stop = [&](int mm, const std::vector<double>& aa, const std::vector<double>& bb) {
       if (mm < 2 && kd > 1) return false;
       std::vector<double> ww, QQ;
-      tridiag_eig(mm, aa, bb, ww, QQ);
+      projected_eig(mm, k, aa, bb, s, ww, QQ);
       const double r = std::fabs(bb[mm - 1] * QQ[(size_t)(mm - 1) * mm + 0]);
       return r <= tol * std::max(1.0, std::fabs(ww[0]));
     };
-    st = lanczos_expand(K, kd, map->precision, a, b, &m, &matvecs, &brk, stop);
+    st = lanczos_expand(K, k, kd, map->precision, a, b, &m, &matvecs, &brk, stop);
     if (st != GTN_OK) return st;
-    tridiag_eig(m, a, b, w, Q);
+    projected_eig(m, k, a, b, s, w, Q);
     theta = w[0];
     res = brk ? 0.0 : std::fabs(b[m - 1] * Q[(size_t)(m - 1) * m + 0]);
-    // Ritz vector x = sum_i Q[i,0] V_i
-    std::vector<double2> c(m);
-    for (int i = 0; i < m; ++i) c[i] = make_double2(Q[(size_t)i * m + 0], 0.0);
-    st = push(K, c, K.coef + 192);
-    if (st != GTN_OK) return st;
-    GTN_CUDA_TRY(ctx, launch_lincomb(x, make_double2(0.0, 0.0), K.V, K.n, m, K.coef + 192, make_double2(1.0, 0.0), K.n, ctx->stream));
-    ctx->launches++;
-    st = normalize(K, x, &nrm);
-    if (st != GTN_OK) return st;
     converged = brk || res <= tol * std::max(1.0, std::fabs(theta)) || m == K.n;
-    if (converged) break;
-    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(K.V, x, K.n * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
+    const int keep = thick_keep(kd, m);
+    if (converged || it + 1 == maxit || keep == 0) {
+      // Ritz vector x = sum_i Q[i,0] V_i
+      std::vector<double2> c(m);
+      for (int i = 0; i < m; ++i) c[i] = make_double2(Q[(size_t)i * m + 0], 0.0);
+      st = push(K, c, K.coef + 192);
+      if (st != GTN_OK) return st;
+      GTN_CUDA_TRY(ctx, launch_lincomb(x, make_double2(0.0, 0.0), K.V, K.n, m, K.coef + 192, make_double2(1.0, 0.0), K.n, ctx->stream));
+      ctx->launches++;
+      st = normalize(K, x, &nrm);
+      if (st != GTN_OK) return st;
+      if (converged || it + 1 == maxit) break;
+      GTN_CUDA_TRY(ctx, cudaMemcpyAsync(K.V, x, K.n * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
+      k = 0;
+      continue;
+    }
+    // V[:, :keep] <- V[:, :m] Q[:, :keep]; the residual direction V[m] becomes column keep.
+    std::vector<double> qk((size_t)m * keep);
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < keep; ++j) qk[(size_t)i * keep + j] = Q[(size_t)i * m + j];
+    double* dq = reinterpret_cast<double*>(K.coef + 256);
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(dq, qk.data(), qk.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    GTN_CUDA_TRY(ctx, launch_basis_rotate(K.V, K.n, m, keep, dq, K.n, ctx->stream));
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(K.V + (int64_t)keep * K.n, K.V + (int64_t)m * K.n, K.n * sizeof(double2),
+                                      cudaMemcpyDeviceToDevice, ctx->stream));
+    GTN_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // qk is pageable host memory
+    ctx->launches++;
+    s.assign(keep, 0.0);
+    for (int i = 0; i < keep; ++i) {
+      a[i] = w[i];
+      s[i] = b[m - 1] * Q[(size_t)(m - 1) * m + i];
+    }
+    k = keep;
   }
   double E = theta;
   if (rq_fp64) {
@@ -314,7 +366,7 @@ extern "C" int gtn_expm_apply(gtn_map map, double dz_re, double dz_im, void* xv,
     if (beta0 == 0) break;
     int m = 0;
     bool brk = false;
-    st = lanczos_expand(K, kd, map->precision, a, b, &m, &matvecs, &brk,
+    st = lanczos_expand(K, 0, kd, map->precision, a, b, &m, &matvecs, &brk,
                         [](int, const std::vector<double>&, const std::vector<double>&) { return false; });
     if (st != GTN_OK) return st;
     tridiag_eig(m, a, b, w, Q);
