@@ -57,6 +57,81 @@ __global__ void __launch_bounds__(kDotThreads) multidot_partial_kernel(const dou
   }
 }
 
+// The same projections with FP32 products (inputs rounded to float, per-thread sums in
+// float, block sums in double): for reorthogonalisation passes of mixed-precision Krylov
+// bases, whose coefficients only need to be accurate well below the map's own error.  The
+// vector kernels are FP64-ALU bound on this part, not HBM bound.
+template <int JB>
+__global__ void __launch_bounds__(kDotThreads) multidot_f32_partial_kernel(const double2* __restrict__ V,
+                                                                           int64_t ldv, int J, int j0,
+                                                                           const double2* __restrict__ w,
+                                                                           int64_t n,
+                                                                           double2* __restrict__ part) {
+  float2 acc[JB];
+#pragma unroll
+  for (int j = 0; j < JB; ++j) acc[j] = make_float2(0.f, 0.f);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 wd = w[i];
+    const float wx = __double2float_rn(wd.x), wy = __double2float_rn(wd.y);
+#pragma unroll
+    for (int j = 0; j < JB; ++j) {
+      if (j0 + j < J) {
+        const double2 vd = V[(int64_t)(j0 + j) * ldv + i];
+        const float vx = __double2float_rn(vd.x), vy = __double2float_rn(vd.y);
+        acc[j].x = fmaf(vx, wx, fmaf(vy, wy, acc[j].x));
+        acc[j].y = fmaf(vx, wy, fmaf(-vy, wx, acc[j].y));
+      }
+    }
+  }
+  __shared__ double2 red[kDotThreads / 32][JB];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < JB; ++j) {
+    double x = acc[j].x, y = acc[j].y;
+    for (int o = 16; o > 0; o >>= 1) {
+      x += __shfl_down_sync(0xffffffffu, x, o);
+      y += __shfl_down_sync(0xffffffffu, y, o);
+    }
+    if (lane == 0) red[wid][j] = make_double2(x, y);
+  }
+  __syncthreads();
+  if (threadIdx.x < JB && j0 + (int)threadIdx.x < J) {
+    double x = 0, y = 0;
+    for (int q = 0; q < kDotThreads / 32; ++q) {
+      x += red[q][threadIdx.x].x;
+      y += red[q][threadIdx.x].y;
+    }
+    part[(int64_t)blockIdx.x * J + j0 + threadIdx.x] = make_double2(x, y);
+  }
+}
+
+// w -= sum_j coef[j] V_j with FP32 products and one FP64 subtraction per element: the
+// update of a reorthogonalisation pass, whose coefficients are small next to |w|.
+__global__ void reorth_update_f32_kernel(double2* __restrict__ w, const double2* __restrict__ V, int64_t ldv,
+                                         int J, const double2* __restrict__ coef, int64_t n) {
+  __shared__ float2 c[kMaxJ];
+  if ((int)threadIdx.x < J) {
+    const double2 a = coef[threadIdx.x];
+    c[threadIdx.x] = make_float2((float)a.x, (float)a.y);
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float ax = 0.f, ay = 0.f;
+    for (int j = 0; j < J; ++j) {
+      const double2 vd = V[(int64_t)j * ldv + i];
+      const float vx = __double2float_rn(vd.x), vy = __double2float_rn(vd.y);
+      ax = fmaf(c[j].x, vx, fmaf(-c[j].y, vy, ax));
+      ay = fmaf(c[j].x, vy, fmaf(c[j].y, vx, ay));
+    }
+    double2 wi = w[i];
+    wi.x -= (double)ax;
+    wi.y -= (double)ay;
+    w[i] = wi;
+  }
+}
+
 // out[j] = sum over blocks of part[b * J + j] (fixed order: deterministic).
 __global__ void multidot_final_kernel(const double2* __restrict__ part, int nblk, int J,
                                       double2* __restrict__ out) {
@@ -253,6 +328,25 @@ cudaError_t launch_multidot(const double2* V, int64_t ldv, int J, const double2*
     multidot_partial_kernel<8><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
   }
   multidot_final_kernel<<<J, 256, 0, s>>>(scratch, nblk, J, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_multidot_f32(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
+                                double2* out, double2* scratch, int nblk, cudaStream_t s) {
+  if (J <= 0) return cudaSuccess;
+  if (J > kMaxJ) return cudaErrorInvalidValue;
+  for (int j0 = 0; j0 < J; j0 += 8) {
+    multidot_f32_partial_kernel<8><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+  }
+  multidot_final_kernel<<<J, 256, 0, s>>>(scratch, nblk, J, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reorth_update_f32(double2* w, const double2* V, int64_t ldv, int J, const double2* coef,
+                                     int64_t n, cudaStream_t s) {
+  if (J > kMaxJ) return cudaErrorInvalidValue;
+  if (J <= 0) return cudaSuccess;
+  reorth_update_f32_kernel<<<grid_for(n), 256, 0, s>>>(w, V, ldv, J, coef, n);
   return cudaGetLastError();
 }
 

@@ -244,6 +244,11 @@ cudaError_t launch_lincomb(double2* w, double2 beta, const double2* V, int64_t l
                            cudaStream_t s);
 cudaError_t launch_axpby(int64_t n, double2 a, const double2* x, double2 b, double2* y,
                          cudaStream_t s);
+// FP32-product variants for reorthogonalisation passes of mixed-precision bases.
+cudaError_t launch_multidot_f32(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
+                                double2* out /*[J]*/, double2* scratch, int nblk, cudaStream_t s);
+cudaError_t launch_reorth_update_f32(double2* w, const double2* V, int64_t ldv, int J,
+                                     const double2* coef /*device [J]*/, int64_t n, cudaStream_t s);
 // In place: V_j <- sum_{i<m} Q[i * k + j] V_i for j < k (k <= m <= 64, Q real, device).
 cudaError_t launch_basis_rotate(double2* V, int64_t ldv, int m, int k, const double* Q, int64_t n,
                                 cudaStream_t s);

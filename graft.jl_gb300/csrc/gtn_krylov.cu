@@ -171,6 +171,7 @@ int lanczos_expand(Krylov& K, int j0, int kd, int precision, std::vector<double>
   b.resize(kd, 0.0);
   for (int j = j0; j < kd; ++j) a[j] = b[j] = 0.0;
   *breakdown = false;
+  const bool fast_reorth = precision != GTN_PREC_FP64;
   int m = kd;
   for (int j = j0; j < kd; ++j) {
     double2* vj = K.V + (int64_t)j * K.n;
@@ -178,19 +179,55 @@ int lanczos_expand(Krylov& K, int j0, int kd, int precision, std::vector<double>
     int st = map_run(K.map, precision, vj, w);
     if (st != GTN_OK) return st;
     (*matvecs)++;
-    // two classical Gram-Schmidt passes against V[0..j]
-    GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef, K.part, K.nblk, s));
-    GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef, make_double2(-1.0, 0.0), K.n, s));
-    GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
-    GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
-    GTN_CUDA_TRY(ctx, norm2_dev(K, w, K.coef + 128));
-    ctx->launches += 2 * ((j + 8) / 8 + 1) + 2;
     double2 hbuf[130];
-    st = fetch(K, K.coef, 130, hbuf);  // h (0..63), h2 (64..127), |w|^2 (128)
-    if (st != GTN_OK) return st;
-    const double2 nn = hbuf[128];
-    a[j] = hbuf[j].x + hbuf[64 + j].x;
-    const double beta = std::sqrt(std::max(nn.x, 0.0));
+    double hh = 0.0;  // squared norm of the full-pass coefficients (local steps only)
+    if (j == j0) {
+      // first vector of an expansion (couples to every kept Ritz vector): two classical
+      // Gram-Schmidt passes against V[0..j] in FP64
+      GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef, K.part, K.nblk, s));
+      GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef, make_double2(-1.0, 0.0), K.n, s));
+      GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
+      GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
+      ctx->launches += 2 * ((j + 8) / 8 + 1) + 2;
+    } else {
+      // local three-term step against V[j-1], V[j] in FP64, then one full reorthogonalisation
+      // pass (FP32 products for mixed-precision maps, whose error sits far above the
+      // coefficients this pass removes)
+      const double2* vprev = K.V + (int64_t)(j - 1) * K.n;
+      GTN_CUDA_TRY(ctx, launch_multidot(vprev, K.n, 2, w, K.n, K.coef, K.part, K.nblk, s));
+      GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), vprev, K.n, 2, K.coef, make_double2(-1.0, 0.0), K.n, s));
+      if (fast_reorth) {
+        GTN_CUDA_TRY(ctx, launch_multidot_f32(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
+        GTN_CUDA_TRY(ctx, launch_reorth_update_f32(w, K.V, K.n, j + 1, K.coef + 64, K.n, s));
+      } else {
+        GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
+        GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
+      }
+      ctx->launches += (j + 8) / 8 + 5;
+    }
+    GTN_CUDA_TRY(ctx, norm2_dev(K, w, K.coef + 128));
+    int st2 = fetch(K, K.coef, 130, hbuf);  // h (0..63), h2 (64..127), |w|^2 (128)
+    if (st2 != GTN_OK) return st2;
+    double nn = hbuf[128].x;
+    if (j == j0) {
+      a[j] = hbuf[j].x + hbuf[64 + j].x;
+    } else {
+      a[j] = hbuf[1].x + hbuf[64 + j].x;
+      for (int i = 0; i <= j; ++i) hh += hbuf[64 + i].x * hbuf[64 + i].x + hbuf[64 + i].y * hbuf[64 + i].y;
+      if (nn < hh) {
+        // DGKS criterion: the pass removed more than half of |w|^2, so V[0..j] and w were far
+        // from orthogonal; repeat it in FP64
+        GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
+        GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
+        GTN_CUDA_TRY(ctx, norm2_dev(K, w, K.coef + 128));
+        ctx->launches += (j + 8) / 8 + 2;
+        st2 = fetch(K, K.coef + 64, 65, hbuf + 64);
+        if (st2 != GTN_OK) return st2;
+        a[j] += hbuf[64 + j].x;
+        nn = hbuf[128].x;
+      }
+    }
+    const double beta = std::sqrt(std::max(nn, 0.0));
     b[j] = beta;
     if (beta <= 1e-13 * std::max(1.0, std::fabs(a[j]))) {
       m = j + 1;
