@@ -536,6 +536,61 @@ def run_dmrg(args):
     print(json.dumps(out), flush=True)
 
 
+def run_lanczos(args):
+    """One Lanczos solve in the middle of the dense Heisenberg chain mps_topology(63) at bond
+    dimension --dmrg-D (Θ = [D,2,2,D]): the time of one map application against the time of
+    one Lanczos iteration (application + Gram-Schmidt + coefficient read-back), krylovdim 20,
+    two restarts (28 matvecs), from a seeded random start.  The solve runs inside the NVTX
+    range "lanczos" so that a profiler can select its launches."""
+    import torch
+    import grafttn as G
+    from grafttn.contractions import EnvCache, eff_h2
+    from grafttn.networks import move_center, two_site_tensor
+    ctx = G.default_context(0)
+    L, D = 63, args.dmrg_D
+    topo = G.mps_topology(L)
+    H = G.TTNO.from_hamiltonian(G.heisenberg(topo), ctx)
+    bond = {}
+    for c in range(topo.nnodes):
+        if topo.parent[c] >= 0:
+            below = len(topo.subtree_nodes(c, topo.parent[c]))
+            bond[c] = int(min(D, 2 ** min(below, 40), 2 ** min(L - below, 40)))
+    psi = G.random_ttns(np.random.default_rng(7), topo, 2, bond, ctx=ctx)
+    n = L // 2
+    m = topo.parent[n]
+    cache = EnvCache(topo)
+    move_center(psi, n, cache)
+    theta = two_site_tensor(psi, n, m)
+    rng = np.random.default_rng(3)
+    x0 = ctx.upload((rng.standard_normal(theta.shape) + 1j * rng.standard_normal(theta.shape)).astype(np.complex128))
+    torch.cuda.synchronize()
+    out = {"metric": "Lanczos iteration time", "unit": "ms", "topology": f"mps{L}", "bond_dim": D,
+           "theta_shape": list(theta.shape), "krylovdim": 20, "runs": {}}
+    for prec in args.dmrg_precisions.split(","):
+        h2 = eff_h2(cache, psi, H, n, m, G._lib.PRECISIONS[prec])
+        y = h2(theta)
+        for _ in range(3):
+            h2.apply_into(theta, y)
+        ctx.sync()
+        t0 = time.perf_counter()
+        for _ in range(20):
+            h2.apply_into(theta, y)
+        ctx.sync()
+        apply_ms = (time.perf_counter() - t0) / 20 * 1e3
+        h2.lanczos_min(x0, krylovdim=20, tol=1e-14, maxiter=1)  # warm the basis allocation
+        ctx.sync()
+        torch.cuda.nvtx.range_push("lanczos")
+        t0 = time.perf_counter()
+        _, _, info = h2.lanczos_min(x0, krylovdim=20, tol=1e-14, maxiter=2)
+        ctx.sync()
+        torch.cuda.nvtx.range_pop()
+        solve_s = time.perf_counter() - t0
+        out["runs"][prec] = {"apply_ms": apply_ms, "solve_s": solve_s, "matvecs": info["matvecs"],
+                             "iteration_ms": solve_s / info["matvecs"] * 1e3}
+        h2.close()
+    print(json.dumps(out), flush=True)
+
+
 def run_grad(args):
     """Gradient workload: XXZ (Delta = 0.7) on binary_topology(4) (31 sites) at bond
     dimension --grad-D with per-edge couplings theta_e ~ U(0.5, 1.5): wall time of the
@@ -659,6 +714,8 @@ def main():
     ap.add_argument("--dmrg-D", type=int, default=256)
     ap.add_argument("--dmrg-sweeps", type=int, default=2)
     ap.add_argument("--dmrg-precisions", default="bf16x6,fp64")
+    ap.add_argument("--lanczos", action="store_true",
+                    help="time one mid-chain Lanczos solve of mps63 at --dmrg-D against one map application")
     ap.add_argument("--grad", action="store_true", help="measure the gradient workload (bin31 XXZ)")
     ap.add_argument("--grad-D", type=int, default=128)
     ap.add_argument("--grad-precisions", default="fp64,bf16x6")
@@ -678,9 +735,9 @@ def main():
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
         dist.init_process_group(backend)
     try:
-        if args.dmrg or args.grad or args.cbe:
+        if args.dmrg or args.grad or args.cbe or args.lanczos:
             if rank == 0:
-                (run_dmrg if args.dmrg else run_grad if args.grad else run_cbe)(args)
+                (run_dmrg if args.dmrg else run_lanczos if args.lanczos else run_grad if args.grad else run_cbe)(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:

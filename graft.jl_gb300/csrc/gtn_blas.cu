@@ -12,6 +12,20 @@ __device__ __forceinline__ double2 cmul_conj(double2 a, double2 b) {  // conj(a)
   return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
 }
 
+// double -> float by bit manipulation on the integer pipe: mantissa truncated to 23 bits,
+// magnitudes below float's normal range flushed to signed zero, above it clamped to the
+// largest float.  The hardware F2F conversion runs at the FP64 rate on this part, which
+// would make the FP32-product kernels as slow as FP64 ones.
+__device__ __forceinline__ float dtof_trunc(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d);
+  const unsigned lo = (unsigned)__double2loint(d);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned bits = e <= 0 ? sign : e >= 255 ? (sign | 0x7f7fffffu) : (sign | ((unsigned)e << 23) | mant);
+  return __uint_as_float(bits);
+}
+
 // Per-block partial sums of conj(V_j) . w for j < J, written to part[block * J + j].
 template <int JB>
 __global__ void __launch_bounds__(kDotThreads) multidot_partial_kernel(const double2* __restrict__ V,
@@ -73,12 +87,12 @@ __global__ void __launch_bounds__(kDotThreads) multidot_f32_partial_kernel(const
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double2 wd = w[i];
-    const float wx = __double2float_rn(wd.x), wy = __double2float_rn(wd.y);
+    const float wx = dtof_trunc(wd.x), wy = dtof_trunc(wd.y);
 #pragma unroll
     for (int j = 0; j < JB; ++j) {
       if (j0 + j < J) {
         const double2 vd = V[(int64_t)(j0 + j) * ldv + i];
-        const float vx = __double2float_rn(vd.x), vy = __double2float_rn(vd.y);
+        const float vx = dtof_trunc(vd.x), vy = dtof_trunc(vd.y);
         acc[j].x = fmaf(vx, wx, fmaf(vy, wy, acc[j].x));
         acc[j].y = fmaf(vx, wy, fmaf(-vy, wx, acc[j].y));
       }
@@ -121,7 +135,7 @@ __global__ void reorth_update_f32_kernel(double2* __restrict__ w, const double2*
     float ax = 0.f, ay = 0.f;
     for (int j = 0; j < J; ++j) {
       const double2 vd = V[(int64_t)j * ldv + i];
-      const float vx = __double2float_rn(vd.x), vy = __double2float_rn(vd.y);
+      const float vx = dtof_trunc(vd.x), vy = dtof_trunc(vd.y);
       ax = fmaf(c[j].x, vx, fmaf(-c[j].y, vy, ax));
       ay = fmaf(c[j].x, vy, fmaf(c[j].y, vx, ay));
     }
@@ -170,6 +184,8 @@ __global__ void lincomb_kernel(double2* __restrict__ w, double2 beta, const doub
     double2 acc;
     if (beta.x == 0.0 && beta.y == 0.0) {
       acc = make_double2(0.0, 0.0);
+    } else if (beta.x == 1.0 && beta.y == 0.0) {  // the Gram-Schmidt update: no FP64 multiply
+      acc = w[i];
     } else {
       const double2 wi = w[i];
       acc = make_double2(beta.x * wi.x - beta.y * wi.y, beta.x * wi.y + beta.y * wi.x);
@@ -188,6 +204,10 @@ __global__ void axpby_kernel(int64_t n, double2 a, const double2* __restrict__ x
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double2 xi = x[i];
+    if (a.y == 0.0 && b.x == 0.0 && b.y == 0.0) {  // real scaling (normalisation): 2 FP64 multiplies
+      y[i] = make_double2(a.x * xi.x, a.x * xi.y);
+      continue;
+    }
     double2 yi = make_double2(0.0, 0.0);
     if (b.x != 0.0 || b.y != 0.0) {
       const double2 t = y[i];
@@ -320,12 +340,28 @@ inline unsigned grid_for(int64_t n) {
 
 int multidot_blocks(gtn_ctx ctx) { return (ctx->sm_count > 0 ? ctx->sm_count : 152) * 2; }
 
+int multidot_launch_count(int J) {
+  int c = J > 0 ? 1 : 0;  // the final reduction
+  for (int j0 = 0; j0 < J;) {
+    const int rem = J - j0;
+    j0 += rem >= 8 ? 8 : rem >= 4 ? 4 : rem >= 2 ? 2 : 1;
+    ++c;
+  }
+  return c;
+}
+
 cudaError_t launch_multidot(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
                             double2* out, double2* scratch, int nblk, cudaStream_t s) {
   if (J <= 0) return cudaSuccess;
   if (J > kMaxJ) return cudaErrorInvalidValue;
-  for (int j0 = 0; j0 < J; j0 += 8) {
-    multidot_partial_kernel<8><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+  // vectors in groups of 8, 4, 2, 1: a guarded slot of a wider kernel still costs its FP64 work
+  for (int j0 = 0; j0 < J;) {
+    const int rem = J - j0;
+    if (rem >= 8) multidot_partial_kernel<8><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+    else if (rem >= 4) multidot_partial_kernel<4><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+    else if (rem >= 2) multidot_partial_kernel<2><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+    else multidot_partial_kernel<1><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+    j0 += rem >= 8 ? 8 : rem >= 4 ? 4 : rem >= 2 ? 2 : 1;
   }
   multidot_final_kernel<<<J, 256, 0, s>>>(scratch, nblk, J, out);
   return cudaGetLastError();
@@ -335,8 +371,13 @@ cudaError_t launch_multidot_f32(const double2* V, int64_t ldv, int J, const doub
                                 double2* out, double2* scratch, int nblk, cudaStream_t s) {
   if (J <= 0) return cudaSuccess;
   if (J > kMaxJ) return cudaErrorInvalidValue;
-  for (int j0 = 0; j0 < J; j0 += 8) {
-    multidot_f32_partial_kernel<8><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+  for (int j0 = 0; j0 < J;) {
+    const int rem = J - j0;
+    if (rem >= 8) multidot_f32_partial_kernel<8><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+    else if (rem >= 4) multidot_f32_partial_kernel<4><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+    else if (rem >= 2) multidot_f32_partial_kernel<2><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+    else multidot_f32_partial_kernel<1><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);
+    j0 += rem >= 8 ? 8 : rem >= 4 ? 4 : rem >= 2 ? 2 : 1;
   }
   multidot_final_kernel<<<J, 256, 0, s>>>(scratch, nblk, J, out);
   return cudaGetLastError();

@@ -244,6 +244,7 @@ cudaError_t launch_lincomb(double2* w, double2 beta, const double2* V, int64_t l
                            cudaStream_t s);
 cudaError_t launch_axpby(int64_t n, double2 a, const double2* x, double2 b, double2* y,
                          cudaStream_t s);
+int multidot_launch_count(int J);  // kernels one launch_multidot[_f32] of J vectors issues
 // FP32-product variants for reorthogonalisation passes of mixed-precision bases.
 cudaError_t launch_multidot_f32(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
                                 double2* out /*[J]*/, double2* scratch, int nblk, cudaStream_t s);

@@ -188,7 +188,7 @@ int lanczos_expand(Krylov& K, int j0, int kd, int precision, std::vector<double>
       GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef, make_double2(-1.0, 0.0), K.n, s));
       GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
       GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
-      ctx->launches += 2 * ((j + 8) / 8 + 1) + 2;
+      ctx->launches += 2 * (multidot_launch_count(j + 1) + 1);
     } else {
       // local three-term step against V[j-1], V[j] in FP64, then one full reorthogonalisation
       // pass (FP32 products for mixed-precision maps, whose error sits far above the
@@ -203,7 +203,7 @@ int lanczos_expand(Krylov& K, int j0, int kd, int precision, std::vector<double>
         GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
         GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
       }
-      ctx->launches += (j + 8) / 8 + 5;
+      ctx->launches += multidot_launch_count(2) + multidot_launch_count(j + 1) + 2;
     }
     GTN_CUDA_TRY(ctx, norm2_dev(K, w, K.coef + 128));
     int st2 = fetch(K, K.coef, 130, hbuf);  // h (0..63), h2 (64..127), |w|^2 (128)
@@ -220,7 +220,7 @@ int lanczos_expand(Krylov& K, int j0, int kd, int precision, std::vector<double>
         GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
         GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
         GTN_CUDA_TRY(ctx, norm2_dev(K, w, K.coef + 128));
-        ctx->launches += (j + 8) / 8 + 2;
+        ctx->launches += multidot_launch_count(j + 1) + 1;
         st2 = fetch(K, K.coef + 64, 65, hbuf + 64);
         if (st2 != GTN_OK) return st2;
         a[j] += hbuf[64 + j].x;
