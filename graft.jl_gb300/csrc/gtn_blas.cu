@@ -350,10 +350,21 @@ int multidot_launch_count(int J) {
   return c;
 }
 
+// Grid widening for latency-bound projections: the FP32 kernels and the 1-2 vector FP64 ones
+// keep too few loads in flight with 2 CTAs per SM.  The partials need nb * J entries, so the
+// grid only widens as far as the caller's scratch capacity allows (0: exactly nblk * J).
+int widened_blocks(int nblk, int J, int64_t scratch_cap, bool f32) {
+  if (scratch_cap <= 0 || (!f32 && J > 2)) return nblk;
+  for (int f : {4, 2})
+    if ((int64_t)nblk * f * J <= scratch_cap) return nblk * f;
+  return nblk;
+}
+
 cudaError_t launch_multidot(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
-                            double2* out, double2* scratch, int nblk, cudaStream_t s) {
+                            double2* out, double2* scratch, int nblk, cudaStream_t s, int64_t scratch_cap) {
   if (J <= 0) return cudaSuccess;
   if (J > kMaxJ) return cudaErrorInvalidValue;
+  nblk = widened_blocks(nblk, J, scratch_cap, false);
   // vectors in groups of 8, 4, 2, 1: a guarded slot of a wider kernel still costs its FP64 work
   for (int j0 = 0; j0 < J;) {
     const int rem = J - j0;
@@ -368,9 +379,10 @@ cudaError_t launch_multidot(const double2* V, int64_t ldv, int J, const double2*
 }
 
 cudaError_t launch_multidot_f32(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
-                                double2* out, double2* scratch, int nblk, cudaStream_t s) {
+                                double2* out, double2* scratch, int nblk, cudaStream_t s, int64_t scratch_cap) {
   if (J <= 0) return cudaSuccess;
   if (J > kMaxJ) return cudaErrorInvalidValue;
+  nblk = widened_blocks(nblk, J, scratch_cap, true);
   for (int j0 = 0; j0 < J;) {
     const int rem = J - j0;
     if (rem >= 8) multidot_f32_partial_kernel<8><<<nblk, kDotThreads, 0, s>>>(V, ldv, J, j0, w, n, scratch);

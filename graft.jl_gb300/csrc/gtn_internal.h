@@ -237,8 +237,11 @@ cudaError_t launch_tc_gemm_grouped(const TcGemmArgs* probs, int nprob, int* errf
                                    std::string* why);
 
 // ---- vector kernels (gtn_blas.cu) --------------------------------------------------
+// scratch holds nblk * J partials; with scratch_cap > 0 (its capacity in entries) the grid
+// may widen up to 4 * nblk CTAs where that helps.
 cudaError_t launch_multidot(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
-                            double2* out /*[J]*/, double2* scratch, int nblk, cudaStream_t s);
+                            double2* out /*[J]*/, double2* scratch, int nblk, cudaStream_t s,
+                            int64_t scratch_cap = 0);
 cudaError_t launch_lincomb(double2* w, double2 beta, const double2* V, int64_t ldv, int J,
                            const double2* coef /*device [J]*/, double2 cscale, int64_t n,
                            cudaStream_t s);
@@ -247,7 +250,8 @@ cudaError_t launch_axpby(int64_t n, double2 a, const double2* x, double2 b, doub
 int multidot_launch_count(int J);  // kernels one launch_multidot[_f32] of J vectors issues
 // FP32-product variants for reorthogonalisation passes of mixed-precision bases.
 cudaError_t launch_multidot_f32(const double2* V, int64_t ldv, int J, const double2* w, int64_t n,
-                                double2* out /*[J]*/, double2* scratch, int nblk, cudaStream_t s);
+                                double2* out /*[J]*/, double2* scratch, int nblk, cudaStream_t s,
+                                int64_t scratch_cap = 0);
 cudaError_t launch_reorth_update_f32(double2* w, const double2* V, int64_t ldv, int J,
                                      const double2* coef /*device [J]*/, int64_t n, cudaStream_t s);
 // In place: V_j <- sum_{i<m} Q[i * k + j] V_i for j < k (k <= m <= 64, Q real, device).

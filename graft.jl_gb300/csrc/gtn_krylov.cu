@@ -77,6 +77,7 @@ struct Krylov {
                     // [256, 2304) kept-Ritz rotation matrix (doubles)
   double2* part;    // multidot partials
   int nblk;
+  int64_t part_cap;  // entries in part (nblk * 64)
 };
 
 int krylov_setup(gtn_map map, int kd, Krylov* K) {
@@ -115,6 +116,7 @@ int krylov_setup(gtn_map map, int kd, Krylov* K) {
   K->V = map->kv;
   K->coef = map->kcoef;
   K->part = map->kscratch;
+  K->part_cap = map->kscratch_cap;
   GTN_CUDA_TRY(ctx, ctx_red(ctx, 64));
   return GTN_OK;
 }
@@ -122,7 +124,7 @@ int krylov_setup(gtn_map map, int kd, Krylov* K) {
 // ||x||^2 into coef[slot] (device)
 cudaError_t norm2_dev(Krylov& K, const double2* x, double2* dst) {
   K.ctx->launches += 2;
-  return launch_multidot(x, 0, 1, x, K.n, dst, K.part, K.nblk, K.ctx->stream);
+  return launch_multidot(x, 0, 1, x, K.n, dst, K.part, K.nblk, K.ctx->stream, K.part_cap);
 }
 
 // Copy `cnt` double2 from device to host and wait; reports device-side wait timeouts.
@@ -184,9 +186,9 @@ int lanczos_expand(Krylov& K, int j0, int kd, int precision, std::vector<double>
     if (j == j0) {
       // first vector of an expansion (couples to every kept Ritz vector): two classical
       // Gram-Schmidt passes against V[0..j] in FP64
-      GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef, K.part, K.nblk, s));
+      GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef, K.part, K.nblk, s, K.part_cap));
       GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef, make_double2(-1.0, 0.0), K.n, s));
-      GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
+      GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s, K.part_cap));
       GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
       ctx->launches += 2 * (multidot_launch_count(j + 1) + 1);
     } else {
@@ -194,13 +196,13 @@ int lanczos_expand(Krylov& K, int j0, int kd, int precision, std::vector<double>
       // pass (FP32 products for mixed-precision maps, whose error sits far above the
       // coefficients this pass removes)
       const double2* vprev = K.V + (int64_t)(j - 1) * K.n;
-      GTN_CUDA_TRY(ctx, launch_multidot(vprev, K.n, 2, w, K.n, K.coef, K.part, K.nblk, s));
+      GTN_CUDA_TRY(ctx, launch_multidot(vprev, K.n, 2, w, K.n, K.coef, K.part, K.nblk, s, K.part_cap));
       GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), vprev, K.n, 2, K.coef, make_double2(-1.0, 0.0), K.n, s));
       if (fast_reorth) {
-        GTN_CUDA_TRY(ctx, launch_multidot_f32(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
+        GTN_CUDA_TRY(ctx, launch_multidot_f32(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s, K.part_cap));
         GTN_CUDA_TRY(ctx, launch_reorth_update_f32(w, K.V, K.n, j + 1, K.coef + 64, K.n, s));
       } else {
-        GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
+        GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s, K.part_cap));
         GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
       }
       ctx->launches += multidot_launch_count(2) + multidot_launch_count(j + 1) + 2;
@@ -217,7 +219,7 @@ int lanczos_expand(Krylov& K, int j0, int kd, int precision, std::vector<double>
       if (nn < hh) {
         // DGKS criterion: the pass removed more than half of |w|^2, so V[0..j] and w were far
         // from orthogonal; repeat it in FP64
-        GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s));
+        GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s, K.part_cap));
         GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
         GTN_CUDA_TRY(ctx, norm2_dev(K, w, K.coef + 128));
         ctx->launches += multidot_launch_count(j + 1) + 1;
