@@ -523,6 +523,8 @@ def run_dmrg(args):
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
             energies.append(Es[-1])
+            print(f"dmrg {prec} sweep {sweep + 1}: {times[-1]:.3f} s, E = {Es[-1]:.12f}, "
+                  f"matvecs so far {stats.get('matvecs')}", file=sys.stderr, flush=True)
         out["runs"][prec] = {"sweep_s": times, "energies": energies, "matvecs": stats.get("matvecs"),
                              "steps": stats.get("steps"),
                              "phase_s": {k[2:]: round(v, 3) for k, v in stats.items() if k.startswith("t_")}}
