@@ -329,6 +329,21 @@ __global__ void __launch_bounds__(kRotThreads) basis_rotate_kernel(double2* __re
   }
 }
 
+// Counter-based uniform fill in [-1, 1) for both parts: the SplitMix64 finaliser (Steele,
+// Lea and Flood, 2014) of seed + index, top 53 bits as a double.  Deterministic for a seed.
+__device__ __forceinline__ double splitmix_unit(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+__global__ void fill_uniform_kernel(double2* __restrict__ x, int64_t n, uint64_t seed) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = make_double2(splitmix_unit(seed + 2 * (uint64_t)i), splitmix_unit(seed + 2 * (uint64_t)i + 1));
+}
+
 inline unsigned grid_for(int64_t n) {
   int64_t b = (n + 255) / 256;
   if (b > 152 * 8) b = 152 * 8;
@@ -428,6 +443,12 @@ cudaError_t launch_c64_to_c128(const float2* x, double2* y, int64_t n, cudaStrea
   c64_to_c128_kernel<<<grid_for(n), 256, 0, s>>>(x, y, n);
   return cudaGetLastError();
 }
+cudaError_t launch_fill_uniform_c128(double2* x, int64_t n, uint64_t seed, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  fill_uniform_kernel<<<grid_for(n), 256, 0, s>>>(x, n, seed);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fill_c128(double2* x, double2 v, int64_t n, cudaStream_t s) {
   fill_kernel<<<grid_for(n), 256, 0, s>>>(x, v, n);
   return cudaGetLastError();

@@ -259,6 +259,8 @@ cudaError_t launch_basis_rotate(double2* V, int64_t ldv, int m, int k, const dou
                                 cudaStream_t s);
 cudaError_t launch_c64_to_c128(const float2* x, double2* y, int64_t n, cudaStream_t s);
 cudaError_t launch_fill_c128(double2* x, double2 v, int64_t n, cudaStream_t s);
+// x[i] = (u, v), u and v uniform in [-1, 1), a fixed function of (seed, i).
+cudaError_t launch_fill_uniform_c128(double2* x, int64_t n, uint64_t seed, cudaStream_t s);
 cudaError_t launch_conj_inplace(double2* x, int64_t n, cudaStream_t s);
 cudaError_t launch_transpose_c128(const double2* in, int64_t rows, int64_t cols, double2* out,
                                   cudaStream_t s);  // out[c][r] = in[r][c]

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 namespace {
@@ -88,8 +89,11 @@ void linalg_release(gtn_ctx ctx) {
 namespace {
 
 // Truncation rank (truncrank & trunctol & truncerror, Backend.jl:466-483) from singular
-// values sorted descending.
-int64_t trunc_rank(const std::vector<double>& hs, int64_t maxdim, double atol, double rtol, double dw) {
+// values sorted descending.  tot_sq >= 0 gives the squared Frobenius norm of the whole
+// matrix when hs holds only the leading part of its spectrum; the discarded weight of a
+// cut at i is then tot_sq minus the kept weight.
+int64_t trunc_rank(const std::vector<double>& hs, int64_t maxdim, double atol, double rtol, double dw,
+                   double tot_sq = -1.0) {
   const int64_t k = (int64_t)hs.size();
   int64_t r = k;
   if (maxdim > 0) r = std::min(r, maxdim);
@@ -99,7 +103,16 @@ int64_t trunc_rank(const std::vector<double>& hs, int64_t maxdim, double atol, d
     for (int64_t i = 0; i < k; ++i) c += hs[i] > thr ? 1 : 0;
     r = std::min(r, c);
   }
-  if (dw > 0) {
+  if (dw > 0 && tot_sq >= 0) {
+    std::vector<double> prefix(k + 1, 0.0);
+    for (int64_t i = 0; i < k; ++i) prefix[i + 1] = prefix[i] + hs[i] * hs[i];
+    int64_t rr = k;
+    for (int64_t i = k - 1; i >= 0; --i) {
+      if (std::sqrt(std::max(tot_sq - prefix[i], 0.0)) <= dw * std::sqrt(tot_sq)) rr = i;
+      else break;
+    }
+    r = std::min(r, rr);
+  } else if (dw > 0) {
     double tot = 0;
     for (double v : hs) tot += v * v;
     double tail = 0;
@@ -197,6 +210,201 @@ int svd_gram(gtn_ctx ctx, cusolverDnHandle_t h, int64_t m, int64_t n, const doub
   return gtn_ctx_sync(ctx);
 }
 
+// Device buffers of one call, freed (after the stream drains) on every return path.
+struct CallBuffers {
+  cudaStream_t s;
+  std::vector<void*> ptrs;
+  explicit CallBuffers(cudaStream_t st) : s(st) {}
+  ~CallBuffers() {
+    cudaStreamSynchronize(s);
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <class T>
+  T* get(size_t count) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return static_cast<T*>(p);
+  }
+};
+
+// Subspace dimension of the subspace-iteration route for a wide m x n matrix (m <= n)
+// truncated to maxdim, or 0 when the Gram route is the better choice: the route pays off
+// when maxdim plus its oversampling is small next to m.  GTN_SVD_SUBSPACE=0 switches it off.
+int64_t subspace_dim(int64_t m, int64_t maxdim) {
+  const char* env = std::getenv("GTN_SVD_SUBSPACE");
+  if (env && env[0] == '0') return 0;
+  if (maxdim <= 0) return 0;
+  const int64_t kk = maxdim + std::max<int64_t>(32, maxdim / 2);
+  return 4 * kk <= m ? kk : 0;
+}
+
+// Truncated SVD of a wide row-major m x n matrix (m <= n) by subspace iteration: the
+// randomised range finder with power iterations (Halko, Martinsson and Tropp, SIAM Review
+// 2011, algorithm 4.4) on a kk-dimensional subspace, iterated until the leading maxdim
+// Rayleigh-Ritz singular values stop moving (1e-13 of the largest).  Their vectors have
+// then converged to ~1e-7 in angle; the split is the exact orthogonal projection of A on
+// the kept left vectors whatever the angle.  Every product is an FP64 SIMT GEMM of
+// m x n x kk (two per iteration) instead of the m x m x n Gram product and an m x m
+// eigenproblem.  *done is false when the values have not settled within the iteration
+// cap, or when the truncation would keep the whole subspace; the caller then takes the
+// Gram route.  Outputs and conventions as svd_gram.
+int svd_subspace(gtn_ctx ctx, cusolverDnHandle_t h, int64_t m, int64_t n, const double2* A, int64_t maxdim,
+                 int64_t kk, double atol, double rtol, double dw, double2* U, double* S, double2* Vh,
+                 int64_t* rank, double* discarded, bool* done) {
+  *done = false;
+  Solver& sv = solver();
+  cudaStream_t s = ctx->stream;
+  const int ik = (int)kk;
+  const int max_it = (int)std::max<int64_t>(4, std::min<int64_t>(40, m / (4 * kk)));
+  // squared Frobenius norm of A
+  const int nblk = multidot_blocks(ctx);
+  GTN_CUDA_TRY(ctx, ctx_red(ctx, (size_t)nblk + 8));
+  GTN_CUDA_TRY(ctx, launch_multidot(A, 0, 1, A, m * n, ctx->d_red, ctx->d_red + 8, nblk, s));
+  double2 tot2;
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(&tot2, ctx->d_red, sizeof(double2), cudaMemcpyDeviceToHost, s));
+  GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  const double tot = tot2.x;
+  const int sk1 = gemm_splitk_slices(m, kk, n), sk2 = gemm_splitk_slices(n, kk, m);
+  const size_t pcap = (size_t)std::max(sk1 > 1 ? sk1 : 0, sk2 > 1 ? sk2 : 0) * std::max(m, n) * kk;
+  CallBuffers buf(s);
+  double2* Ah = buf.get<double2>(m * n);     // conj(A)^T, n x m
+  double2* Qt = buf.get<double2>(kk * m);    // basis of the range, rows of length m
+  double2* Zt = buf.get<double2>(kk * n);    // Z = A^H Q, rows of length n
+  double2* Zc = buf.get<double2>(kk * n);    // conj(Z) rows, later Z^T
+  double2* Gc = buf.get<double2>(kk * kk);   // Z^H Z (column-major), then its eigenvectors
+  double2* Wr = buf.get<double2>(kk * kk);
+  double2* Qr = buf.get<double2>(m * kk);    // Q row-major m x kk
+  double* w = buf.get<double>(kk);
+  double* dnorm = buf.get<double>(kk);
+  double2* tau = buf.get<double2>(kk);
+  double2* P = pcap ? buf.get<double2>(pcap) : nullptr;
+  int* dinfo = buf.get<int>(1);
+  if (!Ah || !Qt || !Zt || !Zc || !Gc || !Wr || !Qr || !w || !dnorm || !tau || !dinfo || (pcap && !P))
+    return set_err(ctx, GTN_ERR_MEMORY, "svd subspace: staging allocation failed");
+  int lq = 0, lq2 = 0, lu = 0, lu2 = 0, le = 0;
+  if (sv.geqrf_bs(h, (int)m, ik, reinterpret_cast<cuDoubleComplex*>(Qt), (int)m, &lq) != CUSOLVER_STATUS_SUCCESS ||
+      sv.geqrf_bs(h, (int)n, ik, reinterpret_cast<cuDoubleComplex*>(Zt), (int)n, &lq2) != CUSOLVER_STATUS_SUCCESS ||
+      sv.ungqr_bs(h, (int)m, ik, ik, reinterpret_cast<cuDoubleComplex*>(Qt), (int)m,
+                  reinterpret_cast<cuDoubleComplex*>(tau), &lu) != CUSOLVER_STATUS_SUCCESS ||
+      sv.ungqr_bs(h, (int)n, ik, ik, reinterpret_cast<cuDoubleComplex*>(Zt), (int)n,
+                  reinterpret_cast<cuDoubleComplex*>(tau), &lu2) != CUSOLVER_STATUS_SUCCESS ||
+      sv.heevd_bs(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ik, reinterpret_cast<cuDoubleComplex*>(Gc), ik,
+                  w, &le) != CUSOLVER_STATUS_SUCCESS)
+    return set_err(ctx, GTN_ERR_CUDA, "svd subspace: bufferSize failed");
+  const int lwork = std::max({lq, lq2, lu, lu2, le, 1});
+  double2* work = buf.get<double2>(lwork);
+  if (!work) return set_err(ctx, GTN_ERR_MEMORY, "svd subspace: workspace allocation failed");
+  auto gemm = [&](const double2* X, const double2* Y, double2* C, int64_t M, int64_t N, int64_t K) {
+    const int sl = gemm_splitk_slices(M, N, K);
+    ctx->launches += sl > 1 ? 2 : 1;
+    if (sl > 1 && P && (size_t)sl * M * N <= pcap) return launch_zgemm_simt_splitk(X, Y, C, M, N, K, sl, P, s);
+    return launch_zgemm_simt(X, Y, C, M, N, K, s);
+  };
+  // Householder QR of a column-major rows x kk block (a row-major kk x rows one), in place: Q
+  auto orth = [&](double2* Y, int64_t rows) -> int {
+    if (sv.geqrf(h, (int)rows, ik, reinterpret_cast<cuDoubleComplex*>(Y), (int)rows,
+                 reinterpret_cast<cuDoubleComplex*>(tau), reinterpret_cast<cuDoubleComplex*>(work), lwork,
+                 dinfo) != CUSOLVER_STATUS_SUCCESS ||
+        sv.ungqr(h, (int)rows, ik, ik, reinterpret_cast<cuDoubleComplex*>(Y), (int)rows,
+                 reinterpret_cast<cuDoubleComplex*>(tau), reinterpret_cast<cuDoubleComplex*>(work), lwork,
+                 dinfo) != CUSOLVER_STATUS_SUCCESS)
+      return set_err(ctx, GTN_ERR_CUDA, "svd subspace: QR failed");
+    return GTN_OK;
+  };
+  GTN_CUDA_TRY(ctx, launch_transpose_c128(A, m, n, Ah, s));
+  GTN_CUDA_TRY(ctx, launch_conj_inplace(Ah, m * n, s));
+  GTN_CUDA_TRY(ctx, launch_fill_uniform_c128(Zt, kk * n, 0x5eed5eedull + (uint64_t)m * 131 + (uint64_t)n, s));
+  ctx->launches += 3;
+  GTN_CUDA_TRY(ctx, gemm(A, Zt, Qt, m, kk, n));  // Y = A Omega
+  int st = orth(Qt, m);
+  if (st != GTN_OK) return st;
+  std::vector<double> hw(kk), sig(kk), prev;
+  const int64_t rchk = std::min(maxdim, kk);
+  bool settled = false;
+  for (int it = 0; it <= max_it; ++it) {
+    GTN_CUDA_TRY(ctx, gemm(Ah, Qt, Zt, n, kk, m));  // Z = A^H Q
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(Zc, Zt, kk * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    GTN_CUDA_TRY(ctx, launch_conj_inplace(Zc, kk * n, s));
+    GTN_CUDA_TRY(ctx, gemm(Zc, Zt, Gc, kk, kk, n));  // Z^H Z, column-major
+    ctx->launches++;
+    if (sv.heevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ik, reinterpret_cast<cuDoubleComplex*>(Gc), ik, w,
+                 reinterpret_cast<cuDoubleComplex*>(work), lwork, dinfo) != CUSOLVER_STATUS_SUCCESS)
+      return set_err(ctx, GTN_ERR_CUDA, "svd subspace: heevd failed");
+    int hinfo = 0;
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(hw.data(), w, kk * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    if (hinfo != 0) return set_err(ctx, GTN_ERR_CUDA, "svd subspace: info = " + std::to_string(hinfo));
+    for (int64_t i = 0; i < kk; ++i) sig[i] = std::sqrt(std::max(hw[kk - 1 - i], 0.0));
+    if (!prev.empty()) {
+      double dmax = 0;
+      for (int64_t i = 0; i < rchk; ++i) dmax = std::max(dmax, std::fabs(sig[i] - prev[i]));
+      if (dmax <= 1e-13 * sig[0]) {
+        settled = true;
+        break;
+      }
+    }
+    if (it == max_it) break;
+    prev = sig;
+    st = orth(Zt, n);  // P = orth(Z)
+    if (st != GTN_OK) return st;
+    GTN_CUDA_TRY(ctx, gemm(A, Zt, Qt, m, kk, n));  // Y = A P
+    st = orth(Qt, m);
+    if (st != GTN_OK) return st;
+  }
+  if (!settled) return GTN_OK;
+  const int64_t r = trunc_rank(sig, maxdim, atol, rtol, dw, tot);
+  if (r >= kk) return GTN_OK;
+  double kept = 0;
+  for (int64_t i = 0; i < r; ++i) kept += sig[i] * sig[i];
+  *rank = r;
+  if (discarded) *discarded = std::sqrt(std::max(tot - kept, 0.0));
+  // Wr[c][j] = W[j][kk-1-c]: eigenvectors in descending order, one per row
+  GroupSpec mg, kg;
+  std::memset(&mg, 0, sizeof(mg));
+  std::memset(&kg, 0, sizeof(kg));
+  mg.n = 1; mg.dim[0] = r; mg.str[0] = -kk;
+  kg.n = 1; kg.dim[0] = kk; kg.str[0] = 1;
+  GTN_CUDA_TRY(ctx, launch_gather_c128_to_c128(Gc + (kk - 1) * kk, mg, kg, r, kk, kk, Wr, s));
+  // U = Q W (m x r)
+  GTN_CUDA_TRY(ctx, launch_transpose_c128(Qt, kk, m, Qr, s));
+  GTN_CUDA_TRY(ctx, gemm(Wr, Qr, U, r, m, kk));
+  // Vh = S^-1 W^H Q^H A = S^-1 conj(W^T Z^T): C[c][l] = sum_j Z^T[l][j] Wr[c][j], conjugated
+  GTN_CUDA_TRY(ctx, launch_transpose_c128(Zt, kk, n, Zc, s));
+  GTN_CUDA_TRY(ctx, gemm(Zc, Wr, Vh, n, r, kk));
+  GTN_CUDA_TRY(ctx, launch_conj_inplace(Vh, r * n, s));
+  GTN_CUDA_TRY(ctx, launch_row_norms(Vh, r, n, dnorm, s));
+  ctx->launches += 5;
+  std::vector<double> inv(r);
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(inv.data(), dnorm, r * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  for (int64_t i = 0; i < r; ++i) {
+    S[i] = inv[i];
+    inv[i] = inv[i] > 0 ? 1.0 / inv[i] : 0.0;
+  }
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(dnorm, inv.data(), r * sizeof(double), cudaMemcpyHostToDevice, s));
+  GTN_CUDA_TRY(ctx, launch_diag_scale(Vh, r, n, dnorm, 1, s));
+  ctx->launches++;
+  st = gtn_ctx_sync(ctx);
+  if (st == GTN_OK) *done = true;
+  return st;
+}
+
+// Thin truncated SVD of a wide row-major m x n matrix (m <= n): the subspace-iteration
+// route where maxdim is small next to m and its values settle, else the Gram route.
+int svd_wide(gtn_ctx ctx, cusolverDnHandle_t h, int64_t m, int64_t n, const double2* A, int64_t maxdim,
+             double atol, double rtol, double dw, double2* U, double* S, double2* Vh, int64_t* rank,
+             double* discarded) {
+  const int64_t kk = subspace_dim(m, maxdim);
+  if (kk > 0) {
+    bool done = false;
+    const int st = svd_subspace(ctx, h, m, n, A, maxdim, kk, atol, rtol, dw, U, S, Vh, rank, discarded, &done);
+    if (st != GTN_OK || done) return st;
+  }
+  return svd_gram(ctx, h, m, n, A, maxdim, atol, rtol, dw, U, S, Vh, rank, discarded);
+}
+
 constexpr int64_t kGramMin = 384;
 
 }  // namespace
@@ -264,7 +472,7 @@ extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, i
   const int64_t k = std::min(m, n);
   if (k >= kGramMin) {
     if (m <= n) {
-      st = svd_gram(ctx, h, m, n, static_cast<const double2*>(A), maxdim, atol, rtol, discarded_weight,
+      st = svd_wide(ctx, h, m, n, static_cast<const double2*>(A), maxdim, atol, rtol, discarded_weight,
                     static_cast<double2*>(U), S, static_cast<double2*>(Vh), rank, discarded);
       return st == GTN_OK ? orthonormalize_rows(ctx, *rank, n, static_cast<double2*>(Vh)) : st;
     }
@@ -279,7 +487,7 @@ extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, i
     }
     st = GTN_OK;
     cudaError_t e = launch_transpose_c128(static_cast<const double2*>(A), m, n, B, s);
-    if (e == cudaSuccess) st = svd_gram(ctx, h, n, m, B, maxdim, atol, rtol, discarded_weight, UB, S, VB, rank, discarded);
+    if (e == cudaSuccess) st = svd_wide(ctx, h, n, m, B, maxdim, atol, rtol, discarded_weight, UB, S, VB, rank, discarded);
     else st = set_err(ctx, GTN_ERR_CUDA, cudaGetErrorString(e));
     if (st == GTN_OK) st = orthonormalize_rows(ctx, *rank, m, VB);
     if (st == GTN_OK) {

@@ -157,6 +157,50 @@ def test_svd_gram_path_large(ctx, m, n):
     assert abs(disc - np.sqrt(np.sum(s0[300:] ** 2))) < 1e-8
 
 
+@pytest.mark.parametrize("m,n", [(1536, 2048), (2048, 1536)])
+def test_svd_subspace_route(ctx, m, n, monkeypatch):
+    # maxdim 64 of 1536: subspace iteration on 96 vectors instead of the Gram matrix; a
+    # geometric spectrum (0.85^i: sigma_97 / sigma_64 = 5e-3) settles in three iterations
+    rng = np.random.default_rng(21)
+    k = min(m, n)
+    U0, _ = np.linalg.qr(crandn(rng, (m, k)))
+    V0, _ = np.linalg.qr(crandn(rng, (n, k)))
+    s0 = 0.85 ** np.arange(k)
+    a = (U0 * s0) @ V0.conj().T
+    U, S, Vh, disc = ctx.svd_trunc(ctx.upload(a), maxdim=64)
+    U, Vh = ctx.download(U), ctx.download(Vh)
+    assert len(S) == 64
+    assert np.allclose(S, s0[:64], rtol=1e-10, atol=1e-14)
+    assert np.allclose(U.conj().T @ U, np.eye(64), atol=1e-12)
+    assert np.allclose(Vh @ Vh.conj().T, np.eye(64), atol=1e-12)
+    ref = (U0[:, :64] * s0[:64]) @ V0[:, :64].conj().T
+    assert np.linalg.norm((U * S) @ Vh - ref) < 1e-8 * np.linalg.norm(ref)
+    # discarded 2-norm from |A|_F^2 minus the kept weight: absolute accuracy ~ eps |A|_F^2 / disc
+    assert abs(disc - np.sqrt(np.sum(s0[64:] ** 2))) < 1e-9
+    # the Gram route (switched off subspace iteration) gives the same truncation
+    monkeypatch.setenv("GTN_SVD_SUBSPACE", "0")
+    U2, S2, Vh2, disc2 = ctx.svd_trunc(ctx.upload(a), maxdim=64)
+    assert np.allclose(S2, S, rtol=1e-9)
+    assert np.linalg.norm((ctx.download(U2) * S2) @ ctx.download(Vh2) - (U * S) @ Vh) < 1e-8 * np.linalg.norm(ref)
+    assert abs(disc2 - disc) < 1e-9
+
+
+def test_svd_subspace_flat_spectrum_falls_back(ctx):
+    # a nearly flat spectrum does not settle within the iteration cap: the Gram route runs
+    rng = np.random.default_rng(22)
+    m, n = 1536, 1600
+    U0, _ = np.linalg.qr(crandn(rng, (m, m)))
+    V0, _ = np.linalg.qr(crandn(rng, (n, m)))
+    s0 = np.linspace(1.0, 0.9, m)
+    a = (U0 * s0) @ V0.conj().T
+    U, S, Vh, disc = ctx.svd_trunc(ctx.upload(a), maxdim=64)
+    U, Vh = ctx.download(U), ctx.download(Vh)
+    assert np.allclose(S, s0[:64], rtol=1e-9)
+    assert np.allclose(U.conj().T @ U, np.eye(64), atol=1e-10)
+    assert np.allclose(Vh @ Vh.conj().T, np.eye(64), atol=1e-10)
+    assert abs(disc - np.sqrt(np.sum(s0[64:] ** 2))) < 1e-8
+
+
 @pytest.mark.parametrize("m,n", [(512, 768), (768, 512)])
 def test_svd_gram_rank_deficient(ctx, m, n):
     # rank 200 < maxdim: the kept directions beyond the rank still form isometries, so a
