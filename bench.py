@@ -593,6 +593,43 @@ def run_lanczos(args):
     print(json.dumps(out), flush=True)
 
 
+def run_svd(args):
+    """Truncated SVD of one 8192 x 8192 complex matrix at maxdim 64, the shape of a two-site
+    split on a depth-2 edge of the 63-site binary tree at D = 64: the subspace-iteration
+    route against the Gram route (GTN_SVD_SUBSPACE=0).  The matrix is X Y with X = 8192 x 512
+    Gaussian columns scaled by 0.9^i and Y = 512 x 8192 Gaussian (seeded, built on the
+    device), so its spectrum decays like a DMRG two-site block's."""
+    import torch
+    import grafttn as G
+    ctx = G.default_context(0)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    n, r = 8192, 512
+    sc = 0.9 ** torch.arange(r, device="cuda", dtype=torch.float64)
+    A = ((torch.randn(n, r, dtype=torch.complex128, device="cuda", generator=g) * sc)
+         @ torch.randn(r, n, dtype=torch.complex128, device="cuda", generator=g)).contiguous()
+    torch.cuda.synchronize()
+    out = {"metric": "truncated SVD time", "unit": "s", "shape": [n, n], "maxdim": 64, "routes": {}}
+    old = os.environ.get("GTN_SVD_SUBSPACE")
+    try:
+        for route, flag in (("subspace", "1"), ("gram", "0")):
+            os.environ["GTN_SVD_SUBSPACE"] = flag
+            ts = []
+            for _ in range(3):
+                ctx.sync()
+                t0 = time.perf_counter()
+                _, S, _, disc = ctx.svd_trunc(A, maxdim=64)
+                ctx.sync()
+                ts.append(time.perf_counter() - t0)
+            out["routes"][route] = {"s": ts, "best_s": min(ts[1:]), "sigma_0": float(S[0]),
+                                    "sigma_63": float(S[63]), "discarded": disc}
+    finally:
+        if old is None:
+            os.environ.pop("GTN_SVD_SUBSPACE", None)
+        else:
+            os.environ["GTN_SVD_SUBSPACE"] = old
+    print(json.dumps(out), flush=True)
+
+
 def run_grad(args):
     """Gradient workload: XXZ (Delta = 0.7) on binary_topology(4) (31 sites) at bond
     dimension --grad-D with per-edge couplings theta_e ~ U(0.5, 1.5): wall time of the
@@ -716,6 +753,8 @@ def main():
     ap.add_argument("--dmrg-D", type=int, default=256)
     ap.add_argument("--dmrg-sweeps", type=int, default=2)
     ap.add_argument("--dmrg-precisions", default="bf16x6,fp64")
+    ap.add_argument("--svd", action="store_true",
+                    help="time one 8192 x 8192 truncated SVD at maxdim 64, subspace route against Gram route")
     ap.add_argument("--lanczos", action="store_true",
                     help="time one mid-chain Lanczos solve of mps63 at --dmrg-D against one map application")
     ap.add_argument("--grad", action="store_true", help="measure the gradient workload (bin31 XXZ)")
@@ -737,9 +776,10 @@ def main():
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
         dist.init_process_group(backend)
     try:
-        if args.dmrg or args.grad or args.cbe or args.lanczos:
+        if args.dmrg or args.grad or args.cbe or args.lanczos or args.svd:
             if rank == 0:
-                (run_dmrg if args.dmrg else run_lanczos if args.lanczos else run_grad if args.grad else run_cbe)(args)
+                (run_dmrg if args.dmrg else run_lanczos if args.lanczos else run_svd if args.svd
+                 else run_grad if args.grad else run_cbe)(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:
