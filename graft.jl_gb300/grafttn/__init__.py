@@ -19,7 +19,7 @@ __all__ = [
 
 
 _DEVICE_MODULES = ("device", "networks", "contractions", "solvers", "cbe", "gradients", "blocksparse", "parallel",
-                   "observables")
+                   "observables", "expansion")
 
 
 def __getattr__(name):

@@ -10,6 +10,7 @@ from __future__ import annotations
 import time
 
 from . import _lib
+from .expansion import check_scheme, predictor_basis
 from .contractions import EnvCache, eff_h0, eff_h1, eff_h2
 from .networks import (TTNO, TTNS, TruncationScheme, absorb_on_leg, left_orth, move_center,
                        orth_factor_leg, split_two_site, two_site_tensor)
@@ -111,13 +112,22 @@ def dmrg1(psi: TTNS, H: TTNO, nsweeps=10, tol=1e-10, krylovdim=20, precision="fp
 
 def expand_exact(cache: EnvCache, psi: TTNS, H: TTNO, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10,
                  enr_atol=1e-12, precision="fp64"):
-    """3S subspace expansion of the bond n -> m with the exact predictor
-    (lib/GraftContractions/src/Contractions/expansion.jl:40-131, 240-272, 488-512): P = the
-    leading left singular vectors of mixing * H2 Theta (n-side legs x rest, at most
-    cap = min(maxdim, D + max_add)); its directions outside range(A_n) (left singular vectors
-    of P - Q Q^H P with Q spanning A_n, at most cap - D, enrichment tolerances atol / rtol)
-    are appended to A_n; the factor U of [A_n E] (at most cap columns) replaces A_n and
-    R = U^H A_n is absorbed into A_m (the state is unchanged: U U^H A_n = A_n)."""
+    """expand with the exact predictor scheme."""
+    return expand(cache, psi, H, n, m, maxdim, max_add, mixing, enr_rtol, enr_atol, precision, scheme="exact")
+
+
+def expand(cache: EnvCache, psi: TTNS, H: TTNO, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10,
+           enr_atol=1e-12, precision="fp64", scheme="exact", rng=None, rsvd_oversample=8, rsvd_poweriter=0):
+    """3S subspace expansion of the bond n -> m (expand!, unfactorised branch,
+    lib/GraftContractions/src/Contractions/expansion.jl:40-131, 240-370, 488-512): P = the
+    predictor basis of mixing * H2 Theta (n-side legs x rest; expansion.predictor_basis with
+    cap = min(maxdim, D + max_add) and the scheme exact / directqr / rsvd / rangefinder); its
+    directions outside range(A_n) (left singular vectors of P - Q Q^H P with Q spanning A_n,
+    at most cap - D, enrichment tolerances atol / rtol) are appended to A_n; the factor U of
+    [A_n E] (at most cap columns) replaces A_n and R = U^H A_n is absorbed into A_m (the
+    state is unchanged: U U^H A_n = A_n).  The randomised schemes draw their probe block
+    from rng, a numpy Generator.  Returns True when the bond grew."""
+    check_scheme(scheme, rng)
     ctx, t = psi.ctx, psi.topo
     olddim = psi.tensors[n].shape[-1]
     cap = min(maxdim, olddim + max_add)
@@ -134,7 +144,7 @@ def expand_exact(cache: EnvCache, psi: TTNS, H: TTNO, n, m, maxdim, max_add=8, m
     h2.close()
     if mixing != 1:
         Pt = ctx.scale(Pt, mixing)
-    P, _, _, _ = ctx.svd_trunc(Pt.reshape(Am.shape[0], -1).contiguous(), maxdim=cap)
+    P = predictor_basis(ctx, Pt.reshape(Am.shape[0], -1), cap, scheme, rng, rsvd_oversample, rsvd_poweriter)
     room = min(max_add, cap - olddim)
     expanded = Am
     if room > 0 and Am.shape[0] > Am.shape[1]:
@@ -157,13 +167,18 @@ def expand_exact(cache: EnvCache, psi: TTNS, H: TTNO, n, m, maxdim, max_add=8, m
 
 def dmrg1_3s(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10, tol=1e-10, krylovdim=20,
              mixing=1.0, max_add=8, enr_rtol=1e-10, enr_atol=1e-12, precision="fp64", rq_fp64=None,
-             lanczos_tol=1e-12, maxiter=100):
-    """Single-site DMRG with subspace expansion between sweeps (GroundState.jl:166-248,
-    exact predictor): dmrg1's local ground states, then expand_exact on every bond in
-    postorder with mixing(sweep) (a number or a function of the sweep); bonds grow by at
-    most max_add per sweep up to trunc.maxdim.  Returns (psi, energies per sweep)."""
+             lanczos_tol=1e-12, maxiter=100, expand_scheme="exact", rng=None, rsvd_oversample=8,
+             rsvd_poweriter=0):
+    """Single-site DMRG with subspace expansion between sweeps (GroundState.jl:166-248):
+    dmrg1's local ground states, then expand with expand_scheme on every bond in postorder
+    with mixing(sweep) (a number or a function of the sweep); bonds grow by at most max_add
+    per sweep up to trunc.maxdim.  The randomised schemes (rsvd, rangefinder) draw their
+    probes from rng, a numpy Generator, bond by bond.  Returns (psi, energies per sweep)."""
     if not H.ishermitian:
         raise ValueError("dmrg1_3s: DMRG requires ishermitian(H) == true")
+    check_scheme(expand_scheme, rng, "dmrg1_3s")
+    if rsvd_oversample < 0 or rsvd_poweriter < 0:
+        raise ValueError("dmrg1_3s: rsvd_oversample and rsvd_poweriter must be nonnegative")
     trunc = trunc or TruncationScheme(maxdim=100)
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
     if rq_fp64 is None:
@@ -187,8 +202,8 @@ def dmrg1_3s(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=
         alpha = mixing(sweep + 1) if callable(mixing) else mixing
         if alpha != 0:
             for n in bonds:
-                expand_exact(cache, psi, H, n, t.parent[n], trunc.maxdim or (1 << 30), max_add, alpha,
-                             enr_rtol, enr_atol, prec)
+                expand(cache, psi, H, n, t.parent[n], trunc.maxdim or (1 << 30), max_add, alpha, enr_rtol,
+                       enr_atol, prec, expand_scheme, rng, rsvd_oversample, rsvd_poweriter)
         energies.append(float(E))
         if len(energies) >= 2 and abs(energies[-1] - energies[-2]) < tol:
             break

@@ -959,13 +959,66 @@ def _svd_keep(M, maxdim=None, atol=0.0, rtol=0.0):
     return U[:, :r], S[:r]
 
 
+EXPAND_SCHEMES = ("exact", "directqr", "rsvd", "rangefinder")
+
+
+def predictor_probe(rng, rest, budget):
+    """Gaussian probe block (rest x budget, complex, unit variance) for the randomised
+    predictor schemes (expansion.jl:372-446).  The reference draws it from a caller-owned
+    Xoshiro stream, which cannot be reproduced here; this restatement draws the real parts,
+    then the imaginary parts, from a numpy Generator, the convention the device path shares."""
+    return (rng.standard_normal((rest, budget)) + 1j * rng.standard_normal((rest, budget))) / np.sqrt(2.0)
+
+
+def predictor_basis(P, cap, scheme="exact", rng=None, oversample=8, poweriter=0):
+    """Child predictor basis of the (n-side legs) x (rest) matrix P (_child_predictor_basis,
+    expansion.jl:240-370): exact = its leading cap left singular vectors; directqr = Q of its
+    compact QR; rsvd = the leading cap left singular vectors of Y = (P P^H)^q P Omega;
+    rangefinder = Q of QR(P Omega) after q QR-stabilised power steps.  Omega has
+    min(rest, cap + oversample) columns."""
+    if scheme == "exact":
+        U, _ = _svd_keep(P, cap)
+        return U
+    if scheme == "directqr":
+        Q, _ = np.linalg.qr(P, mode="reduced")
+        return Q
+    if scheme not in ("rsvd", "rangefinder"):
+        raise ValueError(f"expand: scheme must be one of {EXPAND_SCHEMES}")
+    if rng is None:
+        raise ValueError(f"expand: scheme={scheme} requires an explicit rng")
+    budget = min(P.shape[1], cap + oversample)
+    Om = predictor_probe(rng, P.shape[1], budget)
+    if scheme == "rsvd":
+        Y = P @ Om
+        for _ in range(poweriter):
+            Y = P @ (P.conj().T @ Y)
+        U, _ = _svd_keep(Y, cap)
+        return U
+    Q, _ = np.linalg.qr(P @ Om, mode="reduced")
+    for _ in range(poweriter):
+        Z, _ = np.linalg.qr(P.conj().T @ Q, mode="reduced")
+        Q, _ = np.linalg.qr(P @ Z, mode="reduced")
+    return Q
+
+
 def expand_exact(psi, Ws, cache, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10, enr_atol=1e-12):
-    """3S subspace expansion of the bond n -> m with the exact predictor (expansion.jl:40-131,
-    240-272, 488-512): the leading left singular vectors P of mixing * H2 Theta (n-side
-    legs x rest, at most cap = min(maxdim, D + max_add) of them); the directions of P
-    outside range(A_n) (left singular vectors of N^H P with N the complement of range(A_n),
-    at most cap - D, atol / rtol enrichment tolerances) are appended to A_n; the factor U of
-    [A_n E] (at most cap columns) replaces A_n and R = U^H A_n is absorbed into A_m."""
+    """expand with the exact predictor scheme."""
+    return expand(psi, Ws, cache, n, m, maxdim, max_add, mixing, enr_rtol, enr_atol, scheme="exact")
+
+
+def expand(psi, Ws, cache, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10, enr_atol=1e-12,
+           scheme="exact", rng=None, oversample=8, poweriter=0):
+    """3S subspace expansion of the bond n -> m (expand!, unfactorised branch,
+    expansion.jl:40-131, 240-370, 488-512): the predictor basis P of mixing * H2 Theta
+    (n-side legs x rest, predictor_basis with cap = min(maxdim, D + max_add)); the
+    directions of P outside range(A_n) (left singular vectors of N^H P with N the
+    complement of range(A_n), at most cap - D, atol / rtol enrichment tolerances) are
+    appended to A_n; the factor U of [A_n E] (at most cap columns) replaces A_n and
+    R = U^H A_n is absorbed into A_m."""
+    if scheme not in EXPAND_SCHEMES:
+        raise ValueError(f"expand: scheme must be one of {EXPAND_SCHEMES}")
+    if scheme in ("rsvd", "rangefinder") and rng is None:
+        raise ValueError(f"expand: scheme={scheme} requires an explicit rng")
     t = psi.topo
     olddim = psi.tensors[n].shape[-1]
     cap = min(maxdim, olddim + max_add)
@@ -977,7 +1030,7 @@ def expand_exact(psi, Ws, cache, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1
     Am = A.reshape(-1, sh[-1])
     theta = two_site_tensor(psi, n, m)
     P = (mixing * eff_h2(cache, psi, Ws, n, m)(theta)).reshape(Am.shape[0], -1)
-    P, _ = _svd_keep(P, cap)
+    P = predictor_basis(P, cap, scheme, rng, oversample, poweriter)
     room = min(max_add, cap - olddim)
     expanded = Am
     if room > 0 and Am.shape[0] > Am.shape[1]:
@@ -999,9 +1052,15 @@ def expand_exact(psi, Ws, cache, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1
 
 
 def dmrg1_3s(psi, Ws, maxdim=100, nsweeps=10, tol=1e-10, krylovdim=20, mixing=1.0, max_add=8,
-             enr_rtol=1e-10, enr_atol=1e-12, lanczos_tol=1e-12):
-    """Single-site DMRG with subspace expansion after every sweep (GroundState.jl:166-248,
-    exact predictor): dmrg1's local updates, then expand_exact on every bond in postorder."""
+             enr_rtol=1e-10, enr_atol=1e-12, lanczos_tol=1e-12, expand_scheme="exact", rng=None,
+             rsvd_oversample=8, rsvd_poweriter=0):
+    """Single-site DMRG with subspace expansion after every sweep (GroundState.jl:166-248):
+    dmrg1's local updates, then expand with expand_scheme on every bond in postorder (the
+    randomised schemes draw their probes from rng, bond by bond)."""
+    if expand_scheme not in EXPAND_SCHEMES:
+        raise ValueError(f"dmrg1_3s: expand_scheme must be one of {EXPAND_SCHEMES}")
+    if expand_scheme in ("rsvd", "rangefinder") and rng is None:
+        raise ValueError(f"dmrg1_3s: expand_scheme={expand_scheme} requires an explicit rng")
     t = psi.topo
     cache = EnvCache(t)
     energies = []
@@ -1018,7 +1077,8 @@ def dmrg1_3s(psi, Ws, maxdim=100, nsweeps=10, tol=1e-10, krylovdim=20, mixing=1.
         alpha = mixing(sweep + 1) if callable(mixing) else mixing
         if alpha != 0:
             for n in bonds:
-                expand_exact(psi, Ws, cache, n, t.parent[n], maxdim, max_add, alpha, enr_rtol, enr_atol)
+                expand(psi, Ws, cache, n, t.parent[n], maxdim, max_add, alpha, enr_rtol, enr_atol,
+                       expand_scheme, rng, rsvd_oversample, rsvd_poweriter)
         energies.append(float(E))
         if len(energies) >= 2 and abs(energies[-1] - energies[-2]) < tol:
             break

@@ -213,3 +213,28 @@ def test_dmrg1_3s_matches_oracle_and_ed(ctx):
     assert abs(Es[0] - Eo[0]) < 1e-9 * abs(Eo[0]), (Es, Eo)
     _, Es = G.dmrg1_3s(psi, W, G.TruncationScheme(maxdim=8), nsweeps=10, max_add=4)
     assert abs(Es[-1] - E0) / abs(E0) < 1e-10
+
+
+@pytest.mark.parametrize("scheme", ["directqr", "rsvd", "rangefinder"])
+def test_dmrg1_3s_schemes_match_oracle_and_ed(ctx, scheme):
+    # expand!'s other predictor schemes (expansion.jl:240-370), probes drawn from the same
+    # seeded Generator on both sides: the same bond growth as the oracle, the same energy
+    # after the first sweep, and the exact ground state once the bonds have grown
+    topo = G.star_topology(3, 2)
+    W = G.TTNO.from_hamiltonian(G.tfi(topo, g=0.9), ctx)
+    Hd = O.dense_hamiltonian(O.tfi(O.star_topology(3, 2), g=0.9))
+    E0, _ = O.exact_groundstate(Hd)
+    psi = G.random_ttns(np.random.default_rng(16), topo, 2, 1, ctx=ctx)
+    o = oracle_state(psi)
+    _, Es = G.dmrg1_3s(psi, W, G.TruncationScheme(maxdim=8), nsweeps=3, max_add=4, expand_scheme=scheme,
+                       rng=np.random.default_rng(60))
+    _, Eo = O.dmrg1_3s(o, O.ttno_nn(O.tfi(O.star_topology(3, 2), g=0.9)), maxdim=8, nsweeps=3, max_add=4,
+                       expand_scheme=scheme, rng=np.random.default_rng(60))
+    assert psi.bond_dims() == O.bond_dims(o), (psi.bond_dims(), O.bond_dims(o))
+    assert abs(Es[0] - Eo[0]) < 1e-9 * abs(Eo[0]), (Es, Eo)
+    _, Es = G.dmrg1_3s(psi, W, G.TruncationScheme(maxdim=8), nsweeps=10, max_add=4, expand_scheme=scheme,
+                       rng=np.random.default_rng(61))
+    assert abs(Es[-1] - E0) / abs(E0) < 1e-10
+    with pytest.raises(ValueError):
+        G.dmrg1_3s(psi, W, G.TruncationScheme(maxdim=8), nsweeps=1, expand_scheme=scheme if scheme != "directqr"
+                   else "lanczos")

@@ -111,6 +111,48 @@ def test_dmrg1_3s_grows_bonds_to_ed():
     assert abs(Es[-1] - E0) < 1e-9
 
 
+@pytest.mark.parametrize("scheme", ["directqr", "rsvd", "rangefinder"])
+def test_dmrg1_3s_schemes_grow_bonds_to_ed(scheme):
+    # expand!'s other predictor schemes (expansion.jl:240-370) reach the same exact ground
+    # state of the 7-site star from bond 1
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo, g=0.9)
+    E0, _ = O.exact_groundstate(O.dense_hamiltonian(H))
+    psi = O.random_ttns(np.random.default_rng(6), topo, 2, 1)
+    _, Es = O.dmrg1_3s(psi, O.ttno_nn(H), maxdim=8, nsweeps=12, max_add=4, expand_scheme=scheme,
+                       rng=np.random.default_rng(40))
+    assert max(O.bond_dims(psi)) > 1
+    assert abs(Es[-1] - E0) < 1e-9
+
+
+def test_predictor_schemes_span_the_exact_predictor():
+    # a rank-12 predictor: rangefinder and rsvd sketches with 12 + oversample columns capture
+    # its whole range, so the exact scheme's leading directions lie inside both; directqr
+    # spans the full column space; the randomised schemes insist on an explicit rng
+    rng = np.random.default_rng(41)
+    P = O.randn_c(rng, (40, 12)) @ O.randn_c(rng, (12, 30))
+    ex = O.predictor_basis(P, 6, "exact")
+    for scheme in ("rsvd", "rangefinder"):
+        B = O.predictor_basis(P, 12, scheme, np.random.default_rng(42), oversample=4)
+        assert np.allclose(B.conj().T @ B, np.eye(B.shape[1]), atol=1e-12)
+        assert np.linalg.norm(ex - B @ (B.conj().T @ ex)) < 1e-10
+    Q = O.predictor_basis(P, 6, "directqr")
+    assert Q.shape == (40, 30)
+    assert np.linalg.norm(P - Q @ (Q.conj().T @ P)) < 1e-10 * np.linalg.norm(P)
+    # power iterations sharpen an rsvd sketch smaller than the rank
+    Pd = (O.randn_c(rng, (40, 40)) * 0.7 ** np.arange(40)) @ O.randn_c(rng, (40, 30))
+    e0 = O.predictor_basis(Pd, 4, "exact")
+    errs = []
+    for q in (0, 2):
+        B = O.predictor_basis(Pd, 4, "rsvd", np.random.default_rng(43), oversample=2, poweriter=q)
+        errs.append(np.linalg.norm(e0 - B @ (B.conj().T @ e0)))
+    assert errs[1] < errs[0]
+    with pytest.raises(ValueError):
+        O.predictor_basis(P, 6, "rsvd")
+    with pytest.raises(ValueError):
+        O.predictor_basis(P, 6, "lanczos")
+
+
 def test_tdvp2_full_rank_vs_exact():
     # full bond dimension: every two-site and one-site projector is the identity, so the
     # order-2 TDVP2 step equals exact evolution (tdvp.jl:307-431)
