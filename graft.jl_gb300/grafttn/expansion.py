@@ -5,8 +5,8 @@ The randomised schemes take their Gaussian probe block from a caller-owned numpy
 in place of the reference's caller-owned Xoshiro stream (whose draws cannot be reproduced
 outside Julia): real parts first, then imaginary parts, scaled to unit complex variance.
 The probe is drawn on the host and uploaded; every product, QR and SVD runs on the device.
-This module only needs a context object with sync / upload / matmul / qr / svd_trunc, so its
-logic is importable without a GPU.
+This module only needs a context object with sync / upload / matmul / qr / svd_trunc / axpby /
+scale, so its logic is importable without a GPU.
 """
 from __future__ import annotations
 
@@ -66,3 +66,40 @@ def predictor_basis(ctx, P, cap, scheme="exact", rng=None, oversample=8, powerit
         Z, _ = ctx.qr(ctx.matmul(P, Q, conjA=True, transA=True).contiguous())
         Q, _ = ctx.qr(ctx.matmul(P, Z).contiguous())
     return Q
+
+
+def factorized_rangefinder_enrichment(ctx, Am, P, room, rng, oversample=8, poweriter=0, enr_atol=1e-12,
+                                      enr_rtol=1e-10):
+    """Enrichment of the factorised range finder (_factorized_rangefinder_enrich_split,
+    expansion.jl:134-216) for the row-major n-side matrix A_n and the predictor
+    P = mixing * H2 Theta (n-side legs x rest), both on the device.
+
+    The reference range-finds N^H P, with N an orthonormal basis of the complement of
+    range(A_n), and appends E = N S L, where S is the range-finder basis and L holds the
+    kept left singular vectors of S^H N^H P (maxdim = room, atol, rtol). Here the complement
+    is the projector 1 - Q Q^H, with Q from the QR of A_n, so that no basis of N is formed:
+    P_c = P - Q (Q^H P) has the same range-finder sketches as N^H P, mapped by N. A QR of
+    P_c Omega that is wider than the complement completes with columns of zero weight, and
+    the rank cut on S^H P_c drops them. Returns (Q, E), with E None when nothing is added."""
+    Q, _ = ctx.qr(Am.contiguous())
+    if room <= 0 or Am.shape[0] <= Q.shape[1]:
+        return Q, None
+    # a copy made on the context's stream (ctx.scale), not by torch on its own stream
+    Pc = ctx.axpby(-1.0, ctx.matmul(Q, ctx.matmul(Q, P, conjA=True, transA=True)), 1.0,
+                   ctx.scale(P.contiguous(), 1.0))
+    rest = int(P.shape[1])
+    sk = min(rest, room + oversample)
+    ctx.sync()  # the upload runs outside the context's stream
+    omega = ctx.upload(probe_block(rng, rest, sk))
+    S, _ = ctx.qr(ctx.matmul(Pc, omega).contiguous())
+    for _ in range(poweriter):
+        Z, _ = ctx.qr(ctx.matmul(Pc, S, conjA=True, transA=True).contiguous())
+        S, _ = ctx.qr(ctx.matmul(Pc, Z).contiguous())
+    L, _, _, _ = ctx.svd_trunc(ctx.matmul(S, Pc, conjA=True, transA=True).contiguous(), maxdim=room,
+                               atol=enr_atol, rtol=enr_rtol)
+    if L.shape[1] == 0:
+        return Q, None
+    E = ctx.matmul(S, L)
+    # keep E orthogonal to range(A_n) to working precision
+    E = ctx.axpby(-1.0, ctx.matmul(Q, ctx.matmul(Q, E, conjA=True, transA=True)), 1.0, E.contiguous())
+    return Q, E

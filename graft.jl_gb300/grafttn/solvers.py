@@ -10,7 +10,7 @@ from __future__ import annotations
 import time
 
 from . import _lib
-from .expansion import check_scheme, predictor_basis
+from .expansion import check_scheme, factorized_rangefinder_enrichment, predictor_basis
 from .contractions import EnvCache, eff_h0, eff_h1, eff_h2
 from .networks import (TTNO, TTNS, TruncationScheme, absorb_on_leg, left_orth, move_center,
                        orth_factor_leg, split_two_site, two_site_tensor)
@@ -117,7 +117,8 @@ def expand_exact(cache: EnvCache, psi: TTNS, H: TTNO, n, m, maxdim, max_add=8, m
 
 
 def expand(cache: EnvCache, psi: TTNS, H: TTNO, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10,
-           enr_atol=1e-12, precision="fp64", scheme="exact", rng=None, rsvd_oversample=8, rsvd_poweriter=0):
+           enr_atol=1e-12, precision="fp64", scheme="exact", rng=None, rsvd_oversample=8, rsvd_poweriter=0,
+           factorized=False):
     """3S subspace expansion of the bond n -> m (expand!, unfactorised branch,
     lib/GraftContractions/src/Contractions/expansion.jl:40-131, 240-370, 488-512): P = the
     predictor basis of mixing * H2 Theta (n-side legs x rest; expansion.predictor_basis with
@@ -126,7 +127,9 @@ def expand(cache: EnvCache, psi: TTNS, H: TTNO, n, m, maxdim, max_add=8, mixing=
     at most cap - D, enrichment tolerances atol / rtol) are appended to A_n; the factor U of
     [A_n E] (at most cap columns) replaces A_n and R = U^H A_n is absorbed into A_m (the
     state is unchanged: U U^H A_n = A_n).  The randomised schemes draw their probe block
-    from rng, a numpy Generator.  Returns True when the bond grew."""
+    from rng, a numpy Generator.  factorized with scheme rangefinder takes the factorised
+    range finder's enrichment (expansion.factorized_rangefinder_enrichment, expansion.jl:
+    134-216) and U = [Q E] with no final SVD.  Returns True when the bond grew."""
     check_scheme(scheme, rng)
     ctx, t = psi.ctx, psi.topo
     olddim = psi.tensors[n].shape[-1]
@@ -144,6 +147,18 @@ def expand(cache: EnvCache, psi: TTNS, H: TTNO, n, m, maxdim, max_add=8, mixing=
     h2.close()
     if mixing != 1:
         Pt = ctx.scale(Pt, mixing)
+    if factorized and scheme == "rangefinder":
+        Q, E = factorized_rangefinder_enrichment(ctx, Am, Pt.reshape(Am.shape[0], -1), cap - olddim, rng,
+                                                 rsvd_oversample, rsvd_poweriter, enr_atol, enr_rtol)
+        if E is None:
+            return False
+        U = ctx.concat_cols(Q, E)
+        R = ctx.matmul(U, Am, conjA=True, transA=True)
+        psi.tensors[n] = U.reshape(sh[:-1] + (U.shape[1],))
+        psi.tensors[m] = absorb_on_leg(ctx, psi.tensors[m], R, t.childslot(m, n))
+        psi.center = m
+        cache.invalidate_edge(n, m)
+        return True
     P = predictor_basis(ctx, Pt.reshape(Am.shape[0], -1), cap, scheme, rng, rsvd_oversample, rsvd_poweriter)
     room = min(max_add, cap - olddim)
     expanded = Am
@@ -171,9 +186,11 @@ def dmrg1_3s(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=
              rsvd_poweriter=0):
     """Single-site DMRG with subspace expansion between sweeps (GroundState.jl:166-248):
     dmrg1's local ground states, then expand with expand_scheme on every bond in postorder
-    with mixing(sweep) (a number or a function of the sweep); bonds grow by at most max_add
-    per sweep up to trunc.maxdim.  The randomised schemes (rsvd, rangefinder) draw their
-    probes from rng, a numpy Generator, bond by bond.  Returns (psi, energies per sweep)."""
+    with mixing(sweep) (a number or a function of the sweep) and factorized=true, as the
+    reference passes it (rangefinder is then the factorised range finder); bonds grow by at
+    most max_add per sweep up to trunc.maxdim.  The randomised schemes (rsvd, rangefinder)
+    draw their probes from rng, a numpy Generator, bond by bond.  Returns (psi, energies per
+    sweep)."""
     if not H.ishermitian:
         raise ValueError("dmrg1_3s: DMRG requires ishermitian(H) == true")
     check_scheme(expand_scheme, rng, "dmrg1_3s")
@@ -203,7 +220,7 @@ def dmrg1_3s(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=
         if alpha != 0:
             for n in bonds:
                 expand(cache, psi, H, n, t.parent[n], trunc.maxdim or (1 << 30), max_add, alpha, enr_rtol,
-                       enr_atol, prec, expand_scheme, rng, rsvd_oversample, rsvd_poweriter)
+                       enr_atol, prec, expand_scheme, rng, rsvd_oversample, rsvd_poweriter, factorized=True)
         energies.append(float(E))
         if len(energies) >= 2 and abs(energies[-1] - energies[-2]) < tol:
             break

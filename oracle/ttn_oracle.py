@@ -1001,20 +1001,47 @@ def predictor_basis(P, cap, scheme="exact", rng=None, oversample=8, poweriter=0)
     return Q
 
 
+def factorized_rangefinder_enrichment(Am, P, room, rng, oversample=8, poweriter=0, enr_atol=1e-12,
+                                      enr_rtol=1e-10):
+    """Enrichment of the factorised range finder (_factorized_rangefinder_enrich_split,
+    expansion.jl:134-216) for the n-side matrix A_n and the predictor P = mixing * H2 Theta:
+    kept Q = QR(A_n); N = orthonormal complement of range(Q); the range finder (:280-326)
+    on the complement-side operator N^H P (probes of min(rest, room + oversample) columns,
+    poweriter QR-stabilised steps) gives S; the left singular vectors of S^H N^H P kept by
+    (maxdim = room, atol, rtol) give L; the enrichment is E = N S L.  Returns (Q, E), E None
+    when nothing is added."""
+    Q, _ = np.linalg.qr(Am, mode="reduced")
+    full, _ = np.linalg.qr(np.concatenate([Q, np.eye(Am.shape[0])], axis=1), mode="reduced")
+    N = full[:, Q.shape[1]:Am.shape[0]]
+    if room <= 0 or N.shape[1] == 0:
+        return Q, None
+    NP = N.conj().T @ P
+    sk = min(P.shape[1], room + oversample)
+    S, _ = np.linalg.qr(NP @ predictor_probe(rng, P.shape[1], sk), mode="reduced")
+    for _ in range(poweriter):
+        Z, _ = np.linalg.qr(NP.conj().T @ S, mode="reduced")
+        S, _ = np.linalg.qr(NP @ Z, mode="reduced")
+    L, _ = _svd_keep(S.conj().T @ NP, room, enr_atol, enr_rtol)
+    if L.shape[1] == 0:
+        return Q, None
+    return Q, N @ (S @ L)
+
+
 def expand_exact(psi, Ws, cache, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10, enr_atol=1e-12):
     """expand with the exact predictor scheme."""
     return expand(psi, Ws, cache, n, m, maxdim, max_add, mixing, enr_rtol, enr_atol, scheme="exact")
 
 
 def expand(psi, Ws, cache, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10, enr_atol=1e-12,
-           scheme="exact", rng=None, oversample=8, poweriter=0):
+           scheme="exact", rng=None, oversample=8, poweriter=0, factorized=False):
     """3S subspace expansion of the bond n -> m (expand!, unfactorised branch,
     expansion.jl:40-131, 240-370, 488-512): the predictor basis P of mixing * H2 Theta
     (n-side legs x rest, predictor_basis with cap = min(maxdim, D + max_add)); the
     directions of P outside range(A_n) (left singular vectors of N^H P with N the
     complement of range(A_n), at most cap - D, atol / rtol enrichment tolerances) are
     appended to A_n; the factor U of [A_n E] (at most cap columns) replaces A_n and
-    R = U^H A_n is absorbed into A_m."""
+    R = U^H A_n is absorbed into A_m.  factorized with scheme rangefinder takes the factorised
+    range finder's enrichment instead, and U = [Q E] with no final SVD."""
     if scheme not in EXPAND_SCHEMES:
         raise ValueError(f"expand: scheme must be one of {EXPAND_SCHEMES}")
     if scheme in ("rsvd", "rangefinder") and rng is None:
@@ -1030,6 +1057,18 @@ def expand(psi, Ws, cache, n, m, maxdim, max_add=8, mixing=1.0, enr_rtol=1e-10, 
     Am = A.reshape(-1, sh[-1])
     theta = two_site_tensor(psi, n, m)
     P = (mixing * eff_h2(cache, psi, Ws, n, m)(theta)).reshape(Am.shape[0], -1)
+    if factorized and scheme == "rangefinder":
+        Q, E = factorized_rangefinder_enrichment(Am, P, cap - olddim, rng, oversample, poweriter, enr_atol,
+                                                 enr_rtol)
+        if E is None:
+            return
+        U = np.concatenate([Q, E], axis=1)
+        R = U.conj().T @ Am
+        psi.tensors[n] = U.reshape(sh[:-1] + (U.shape[1],))
+        psi.tensors[m] = absorb_on_leg(psi.tensors[m], R, t.childslot(m, n))
+        psi.center = m
+        cache.invalidate_edge(n, m)
+        return
     P = predictor_basis(P, cap, scheme, rng, oversample, poweriter)
     room = min(max_add, cap - olddim)
     expanded = Am
@@ -1055,8 +1094,9 @@ def dmrg1_3s(psi, Ws, maxdim=100, nsweeps=10, tol=1e-10, krylovdim=20, mixing=1.
              enr_rtol=1e-10, enr_atol=1e-12, lanczos_tol=1e-12, expand_scheme="exact", rng=None,
              rsvd_oversample=8, rsvd_poweriter=0):
     """Single-site DMRG with subspace expansion after every sweep (GroundState.jl:166-248):
-    dmrg1's local updates, then expand with expand_scheme on every bond in postorder (the
-    randomised schemes draw their probes from rng, bond by bond)."""
+    dmrg1's local updates, then expand with expand_scheme on every bond in postorder, with
+    factorized=true as the reference passes it (so rangefinder is the factorised range
+    finder); the randomised schemes draw their probes from rng, bond by bond."""
     if expand_scheme not in EXPAND_SCHEMES:
         raise ValueError(f"dmrg1_3s: expand_scheme must be one of {EXPAND_SCHEMES}")
     if expand_scheme in ("rsvd", "rangefinder") and rng is None:
@@ -1078,7 +1118,7 @@ def dmrg1_3s(psi, Ws, maxdim=100, nsweeps=10, tol=1e-10, krylovdim=20, mixing=1.
         if alpha != 0:
             for n in bonds:
                 expand(psi, Ws, cache, n, t.parent[n], maxdim, max_add, alpha, enr_rtol, enr_atol,
-                       expand_scheme, rng, rsvd_oversample, rsvd_poweriter)
+                       expand_scheme, rng, rsvd_oversample, rsvd_poweriter, factorized=True)
         energies.append(float(E))
         if len(energies) >= 2 and abs(energies[-1] - energies[-2]) < tol:
             break

@@ -14,7 +14,8 @@ from oracle import ttn_oracle as O
 
 
 class HostContext:
-    """The device context's dense calls on CPU complex128 tensors."""
+    """The device context's dense calls on CPU complex128 tensors (axpby writes y in place, as
+    the device call does)."""
 
     def sync(self):
         pass
@@ -30,6 +31,13 @@ class HostContext:
     def qr(self, A2):
         Q, R = torch.linalg.qr(A2, mode="reduced")
         return Q.contiguous(), R.contiguous()
+
+    def axpby(self, a, x, b, y):
+        y.copy_(a * x + b * y)
+        return y
+
+    def scale(self, x, a):
+        return (a * x).contiguous()
 
     def svd_trunc(self, A2, maxdim=None, atol=0.0, rtol=0.0, discarded_weight=0.0):
         U, S, Vh = np.linalg.svd(A2.numpy(), full_matrices=False)
@@ -74,3 +82,25 @@ def test_scheme_argument_checks():
             X.predictor_basis(ctx, P, 2, scheme, rng=None)
     with pytest.raises(ValueError):
         X.predictor_basis(ctx, P, 2, "rsvd", np.random.default_rng(0), oversample=-1)
+
+
+@pytest.mark.parametrize("rows,D,rest,room,oversample,poweriter", [
+    (32, 4, 24, 6, 8, 0), (32, 4, 24, 6, 2, 2), (12, 4, 40, 6, 8, 1), (10, 10, 8, 3, 8, 0)])
+def test_factorized_rangefinder_matches_oracle(rows, D, rest, room, oversample, poweriter):
+    # the projector form (1 - Q Q^H) P against the oracle's explicit complement N, including a
+    # complement narrower than the sketch (12 rows, D 4, sketch 14) and an empty one
+    rng = np.random.default_rng(53)
+    Am = O.randn_c(rng, (rows, D))
+    P = (O.randn_c(rng, (rows, rows)) * 0.75 ** np.arange(rows)) @ O.randn_c(rng, (rows, rest))
+    Qd, Ed = X.factorized_rangefinder_enrichment(HostContext(), torch.from_numpy(Am), torch.from_numpy(P), room,
+                                                 np.random.default_rng(54), oversample, poweriter)
+    Qo, Eo = O.factorized_rangefinder_enrichment(Am, P, room, np.random.default_rng(54), oversample, poweriter)
+    assert np.allclose(_projector(Qd), _projector(Qo), atol=1e-12)
+    if Eo is None:
+        assert Ed is None
+        return
+    Ed = Ed.numpy()
+    assert Ed.shape == Eo.shape
+    assert np.allclose(_projector(Ed), _projector(Eo), atol=1e-9)
+    U = np.concatenate([Qd.numpy(), Ed], axis=1)
+    assert np.allclose(U.conj().T @ U, np.eye(U.shape[1]), atol=1e-12)
