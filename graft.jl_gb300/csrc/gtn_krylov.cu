@@ -439,3 +439,169 @@ extern "C" int gtn_expm_apply(gtn_map map, double dz_re, double dz_im, void* xv,
   }
   return gtn_ctx_sync(ctx);
 }
+
+namespace {
+
+using cplx = std::complex<double>;
+
+// exp(A) of a small dense complex matrix (row-major m x m) by scaling and squaring with a
+// truncated Taylor series (Moler and Van Loan, SIAM Review 45 (2003), method 3): A is
+// scaled by 2^-s so that its 1-norm is at most 1/2, the series is summed until a term
+// falls below 2^-60 of the partial sum (at most 40 terms), and the result is squared s times.
+void expm_small(int m, const std::vector<cplx>& A, std::vector<cplx>& E) {
+  double nrm = 0;
+  for (int j = 0; j < m; ++j) {
+    double col = 0;
+    for (int i = 0; i < m; ++i) col += std::abs(A[(size_t)i * m + j]);
+    nrm = std::max(nrm, col);
+  }
+  int s = 0;
+  while (nrm > 0.5 && s < 1000) {
+    nrm *= 0.5;
+    ++s;
+  }
+  const double scale = std::ldexp(1.0, -s);
+  std::vector<cplx> As(A.size()), term((size_t)m * m, 0.0), next((size_t)m * m);
+  for (size_t i = 0; i < A.size(); ++i) As[i] = A[i] * scale;
+  E.assign((size_t)m * m, 0.0);
+  for (int i = 0; i < m; ++i) {
+    E[(size_t)i * m + i] = 1.0;
+    term[(size_t)i * m + i] = 1.0;
+  }
+  for (int k = 1; k <= 40; ++k) {
+    double tn = 0, en = 0;
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) {
+        cplx acc = 0;
+        for (int l = 0; l < m; ++l) acc += term[(size_t)i * m + l] * As[(size_t)l * m + j];
+        next[(size_t)i * m + j] = acc / (double)k;
+      }
+    term.swap(next);
+    for (size_t i = 0; i < E.size(); ++i) {
+      E[i] += term[i];
+      tn = std::max(tn, std::abs(term[i]));
+      en = std::max(en, std::abs(E[i]));
+    }
+    if (tn <= std::ldexp(en, -60)) break;
+  }
+  for (int q = 0; q < s; ++q) {
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) {
+        cplx acc = 0;
+        for (int l = 0; l < m; ++l) acc += E[(size_t)i * m + l] * E[(size_t)l * m + j];
+        next[(size_t)i * m + j] = acc;
+      }
+    E.swap(next);
+  }
+}
+
+// Arnoldi expansion from V[0] (unit norm) for a map that is not Hermitian: two FP64
+// classical Gram-Schmidt passes against the whole basis per step.  Hm (row-major
+// (kd+1) x kd) receives the projections H[i][j] = <v_i, A v_j> and the subdiagonal norms.
+int arnoldi_expand(Krylov& K, int kd, int precision, std::vector<cplx>& Hm, int* m_out, int* matvecs,
+                   bool* breakdown) {
+  gtn_ctx ctx = K.ctx;
+  cudaStream_t s = ctx->stream;
+  Hm.assign((size_t)(kd + 1) * kd, 0.0);
+  *breakdown = false;
+  int m = kd;
+  for (int j = 0; j < kd; ++j) {
+    double2* vj = K.V + (int64_t)j * K.n;
+    double2* w = K.V + (int64_t)(j + 1) * K.n;
+    int st = map_run(K.map, precision, vj, w);
+    if (st != GTN_OK) return st;
+    (*matvecs)++;
+    GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef, K.part, K.nblk, s, K.part_cap));
+    GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef, make_double2(-1.0, 0.0), K.n, s));
+    GTN_CUDA_TRY(ctx, launch_multidot(K.V, K.n, j + 1, w, K.n, K.coef + 64, K.part, K.nblk, s, K.part_cap));
+    GTN_CUDA_TRY(ctx, launch_lincomb(w, make_double2(1.0, 0.0), K.V, K.n, j + 1, K.coef + 64, make_double2(-1.0, 0.0), K.n, s));
+    GTN_CUDA_TRY(ctx, norm2_dev(K, w, K.coef + 128));
+    ctx->launches += 2 * (multidot_launch_count(j + 1) + 1);
+    double2 hbuf[130];
+    st = fetch(K, K.coef, 130, hbuf);
+    if (st != GTN_OK) return st;
+    double colmax = 0;
+    for (int i = 0; i <= j; ++i) {
+      Hm[(size_t)i * kd + j] = cplx(hbuf[i].x + hbuf[64 + i].x, hbuf[i].y + hbuf[64 + i].y);
+      colmax = std::max(colmax, std::abs(Hm[(size_t)i * kd + j]));
+    }
+    const double beta = std::sqrt(std::max(hbuf[128].x, 0.0));
+    Hm[(size_t)(j + 1) * kd + j] = beta;
+    if (beta <= 1e-13 * std::max(1.0, colmax)) {
+      m = j + 1;
+      *breakdown = true;
+      break;
+    }
+    GTN_CUDA_TRY(ctx, launch_axpby(K.n, make_double2(1.0 / beta, 0.0), w, make_double2(0.0, 0.0), w, s));
+    ctx->launches++;
+  }
+  *m_out = m;
+  return GTN_OK;
+}
+
+}  // namespace
+
+extern "C" int gtn_expm_small(int m, const double* A, double* E) {
+  if (m < 1 || m > 256 || !A || !E) return GTN_ERR_INVALID;
+  std::vector<cplx> a((size_t)m * m), e;
+  for (size_t i = 0; i < a.size(); ++i) a[i] = cplx(A[2 * i], A[2 * i + 1]);
+  expm_small(m, a, e);
+  for (size_t i = 0; i < e.size(); ++i) {
+    E[2 * i] = e[i].real();
+    E[2 * i + 1] = e[i].imag();
+  }
+  return GTN_OK;
+}
+
+extern "C" int gtn_expm_apply_arnoldi(gtn_map map, double dz_re, double dz_im, void* xv, int krylovdim, double tol,
+                                      int* info) {
+  if (!map || !xv) return GTN_ERR_INVALID;
+  Krylov K;
+  int st = krylov_setup(map, std::min<int64_t>(krylovdim, std::max<int64_t>(map->x_elems, 1)), &K);
+  if (st != GTN_OK) return st;
+  gtn_ctx ctx = K.ctx;
+  double2* x = static_cast<double2*>(xv);
+  const int kd = (int)std::min<int64_t>(krylovdim, K.n);
+  const cplx dz(dz_re, dz_im);
+  double remaining = 1.0, frac = 1.0;
+  int matvecs = 0, substeps = 0;
+  std::vector<cplx> Hm, T, E;
+  while (remaining > 1e-14) {
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(K.V, x, K.n * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
+    double beta0;
+    st = normalize(K, K.V, &beta0);
+    if (st != GTN_OK) return st;
+    if (beta0 == 0) break;
+    int m = 0;
+    bool brk = false;
+    st = arnoldi_expand(K, kd, map->precision, Hm, &m, &matvecs, &brk);
+    if (st != GTN_OK) return st;
+    double step = std::min(frac, remaining);
+    std::vector<cplx> c(m);
+    T.assign((size_t)m * m, 0.0);
+    for (int tries = 0; tries < 60; ++tries) {
+      for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j) T[(size_t)i * m + j] = dz * step * Hm[(size_t)i * kd + j];
+      expm_small(m, T, E);
+      for (int i = 0; i < m; ++i) c[i] = E[(size_t)i * m + 0];
+      const double err = (brk || m < kd) ? 0.0 : beta0 * std::abs(Hm[(size_t)m * kd + m - 1]) * std::abs(c[m - 1]);
+      if (err <= tol || step < 1e-12) break;
+      step *= 0.5;
+    }
+    std::vector<double2> cd(m);
+    for (int i = 0; i < m; ++i) cd[i] = make_double2(beta0 * c[i].real(), beta0 * c[i].imag());
+    st = push(K, cd, K.coef + 192);
+    if (st != GTN_OK) return st;
+    GTN_CUDA_TRY(ctx, launch_lincomb(x, make_double2(0.0, 0.0), K.V, K.n, m, K.coef + 192, make_double2(1.0, 0.0), K.n, ctx->stream));
+    ctx->launches++;
+    remaining -= step;
+    frac = step;
+    substeps++;
+    if (substeps > 4096) return set_err(ctx, GTN_ERR_NOT_CONVERGED, "expm: too many substeps");
+  }
+  if (info) {
+    info[0] = substeps;
+    info[1] = matvecs;
+  }
+  return gtn_ctx_sync(ctx);
+}

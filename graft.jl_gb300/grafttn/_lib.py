@@ -68,6 +68,8 @@ SIGNATURES = {
     "gtn_permute": (_i, [_p, _i, _pi64, _pi, _p, _p]),
     "gtn_lanczos_min": (_i, [_p, _p, _i, _d, _i, _i, _pd, _pi, _pd]),
     "gtn_expm_apply": (_i, [_p, _d, _d, _p, _i, _d, _pi]),
+    "gtn_expm_apply_arnoldi": (_i, [_p, _d, _d, _p, _i, _d, _pi]),
+    "gtn_expm_small": (_i, [_i, _pd, _pd]),
     "gtn_svd_trunc": (_i, [_p, _i64, _i64, _p, _i64, _d, _d, _d, _p, _pd, _p, _pi64, _pd]),
     "gtn_qr": (_i, [_p, _i64, _i64, _p, _p, _p]),
     "gtn_dot": (_i, [_p, _i64, _p, _p, _pd]),

@@ -210,13 +210,13 @@ class TDVP1_CBE:
         b = self._base
         if t.parent[u] == v:
             k0 = eff_h0(cache, psi, H, u, v, b.precision)
-            C, _ = k0.exponentiate(-dz, R, b.krylovdim, b.tol)
+            C, _ = k0.exponentiate(-dz, R, b.krylovdim, b.tol, hermitian=H.ishermitian)
             k0.close()
             psi.tensors[v] = absorb_on_leg(ctx, psi.tensors[v], C, t.childslot(v, u))
         else:
             Ct = ctx.permute(R.contiguous(), [1, 0])
             k0 = eff_h0(cache, psi, H, v, u, b.precision)
-            C, _ = k0.exponentiate(-dz, Ct, b.krylovdim, b.tol)
+            C, _ = k0.exponentiate(-dz, Ct, b.krylovdim, b.tol, hermitian=H.ishermitian)
             k0.close()
             Av = psi.tensors[v]
             rk = Av.dim()

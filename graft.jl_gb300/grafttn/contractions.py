@@ -317,7 +317,7 @@ class EffectiveMap:
 
     def lanczos_min(self, x0, krylovdim=20, tol=1e-12, maxiter=100, rq_fp64=False):
         """Lowest eigenpair (groundstate_eigsolve_backend, GroundState.jl:25-39); x0 untouched."""
-        x = x0.contiguous().clone()
+        x = self.ctx.copy(x0)
         E = C.c_double()
         info = (C.c_int * 3)()
         res = C.c_double()
@@ -327,13 +327,15 @@ class EffectiveMap:
             check(st, self.ctx.h, "lanczos")
         return E.value, x, dict(restarts=info[0], matvecs=info[1], converged=bool(info[2]), resid=res.value)
 
-    def exponentiate(self, dz, x0, krylovdim=30, tol=1e-12):
-        """exp(dz H) x0 (evolution_exponentiate_backend, Evolution.jl:54-68)."""
-        x = x0.contiguous().clone()
+    def exponentiate(self, dz, x0, krylovdim=30, tol=1e-12, hermitian=True):
+        """exp(dz H) x0 (evolution_exponentiate_backend, Evolution.jl:54-68): Lanczos for a
+        Hermitian map, Arnoldi otherwise (KrylovKit's exponentiate with ishermitian, as the
+        TDVP sweeps pass it from the TTNO, tdvp.jl:204-281)."""
+        x = self.ctx.copy(x0)
         info = (C.c_int * 2)()
         dz = complex(dz)
-        check(self.ctx.lib.gtn_expm_apply(self.h, dz.real, dz.imag, C.c_void_p(x.data_ptr()), krylovdim, tol, info),
-              self.ctx.h, "expm")
+        fn = self.ctx.lib.gtn_expm_apply if hermitian else self.ctx.lib.gtn_expm_apply_arnoldi
+        check(fn(self.h, dz.real, dz.imag, C.c_void_p(x.data_ptr()), krylovdim, tol, info), self.ctx.h, "expm")
         return x, dict(substeps=info[0], matvecs=info[1])
 
 

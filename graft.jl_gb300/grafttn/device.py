@@ -59,6 +59,19 @@ class Context:
     def empty(self, shape):
         return torch.empty(tuple(int(s) for s in shape), dtype=CDT, device=f"cuda:{self.device}")
 
+    def copy(self, t):
+        """Copy of a device tensor made on the context's stream, so that it follows the
+        context's pending work (a torch copy would run on torch's stream, unordered with the
+        context's non-blocking one)."""
+        if not t.is_contiguous():
+            self.sync()
+            t = t.contiguous()
+            torch.cuda.current_stream(t.device).synchronize()
+        y = self.empty(t.shape)
+        if t.numel():
+            self.axpby(1.0, t, 0.0, y)
+        return y
+
     def upload(self, arr):
         a = np.ascontiguousarray(np.asarray(arr, dtype=np.complex128))
         return torch.from_numpy(a).to(f"cuda:{self.device}")
@@ -95,7 +108,7 @@ class Context:
 
     def permute(self, t, perm):
         if t.dim() == 0:
-            return t.clone()
+            return self.copy(t)
         out = self.empty([t.shape[p] for p in perm])
         st = self.lib.gtn_permute(self.h, t.dim(), i64_array([int(s) for s in t.shape]), int_array(perm),
                                   C.c_void_p(t.data_ptr()), C.c_void_p(out.data_ptr()))

@@ -54,7 +54,7 @@ class TTNS:
         self.center = center
 
     def copy(self):
-        return TTNS(self.topo, [t.clone() for t in self.tensors], self.center, self.ctx)
+        return TTNS(self.topo, [self.ctx.copy(t) for t in self.tensors], self.center, self.ctx)
 
     def host_tensors(self):
         return [self.ctx.download(t) for t in self.tensors]

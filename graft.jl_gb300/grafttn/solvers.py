@@ -261,7 +261,7 @@ class TDVP1:
             if not (skip_initial and i == 0):
                 sdz = terminal_dz if (terminal_dz is not None and i == len(order) - 1) else dz
                 h1 = eff_h1(cache, psi, H, n, self.precision)
-                A, _ = h1.exponentiate(sdz, psi.tensors[n], self.krylovdim, self.tol)
+                A, _ = h1.exponentiate(sdz, psi.tensors[n], self.krylovdim, self.tol, hermitian=H.ishermitian)
                 h1.close()
                 psi.tensors[n] = A
                 cache.invalidate_node(n)
@@ -283,7 +283,7 @@ class TDVP1:
             psi.tensors[u] = Q
             cache.invalidate_node(u)
             k0 = eff_h0(cache, psi, H, u, v, self.precision)
-            Cl, _ = k0.exponentiate(-dz, Cl, self.krylovdim, self.tol)
+            Cl, _ = k0.exponentiate(-dz, Cl, self.krylovdim, self.tol, hermitian=H.ishermitian)
             k0.close()
             psi.tensors[v] = absorb_on_leg(ctx, psi.tensors[v], Cl, t.childslot(v, u))
         else:
@@ -293,7 +293,7 @@ class TDVP1:
             Cl = ctx.permute(Cd, [1, 0])
             cache.invalidate_node(u)
             k0 = eff_h0(cache, psi, H, v, u, self.precision)
-            Cl, _ = k0.exponentiate(-dz, Cl, self.krylovdim, self.tol)
+            Cl, _ = k0.exponentiate(-dz, Cl, self.krylovdim, self.tol, hermitian=H.ishermitian)
             k0.close()
             Av = psi.tensors[v]
             r = Av.dim()
@@ -357,7 +357,7 @@ class TDVP2:
     def _bond_forward(self, psi, H, n, m, dz, center_on):
         theta = two_site_tensor(psi, n, m)
         h2 = eff_h2(self.cache, psi, H, n, m, self.precision)
-        theta, _ = h2.exponentiate(dz, theta, self.krylovdim, self.tol)
+        theta, _ = h2.exponentiate(dz, theta, self.krylovdim, self.tol, hermitian=H.ishermitian)
         h2.close()
         self.cache.invalidate_edge(n, m)
         split_two_site(psi, theta, n, m, self.trunc, center_on)
@@ -365,7 +365,7 @@ class TDVP2:
     def _site_backward(self, psi, H, m, dz):
         assert psi.center == m
         h1 = eff_h1(self.cache, psi, H, m, self.precision)
-        A, _ = h1.exponentiate(-dz, psi.tensors[m], self.krylovdim, self.tol)
+        A, _ = h1.exponentiate(-dz, psi.tensors[m], self.krylovdim, self.tol, hermitian=H.ishermitian)
         h1.close()
         psi.tensors[m] = A
         self.cache.invalidate_node(m)

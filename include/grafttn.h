@@ -182,10 +182,11 @@ int gtn_permute(gtn_ctx ctx, int rank, const int64_t* dims, const int* perm,
  * groundstate_eigsolve_backend, lib/GraftGroundState/src/GroundState/GroundState.jl:25-39
  * evolution_exponentiate_backend, lib/GraftEvolution/src/Evolution/Evolution.jl:54-68
  */
-/* Lowest eigenpair of the (Hermitian) map by restarted Lanczos with FP64 full
- * re-orthogonalisation on device.  x (device, c128) holds the start vector on entry and
- * the normalised eigenvector on exit.  With rq_fp64 != 0 the returned energy is the
- * FP64 Rayleigh quotient <x|H x> of the final vector (one FP64 apply).
+/* Lowest eigenpair of the (Hermitian) map by thick-restarted Lanczos on device (about 3/5
+ * of the basis kept as Ritz vectors per restart; a local three-term step plus one
+ * DGKS-guarded reorthogonalisation pass per iteration).  x (device, c128) holds the start
+ * vector on entry and the normalised eigenvector on exit.  With rq_fp64 != 0 the returned
+ * energy is the FP64 Rayleigh quotient <x|H x> of the final vector (one FP64 apply).
  * info[0] = restarts, info[1] = matvecs, info[2] = converged flag; resid[0] = residual. */
 int gtn_lanczos_min(gtn_map map, void* x, int krylovdim, double tol, int maxiter,
                     int rq_fp64, double* energy, int* info, double* resid);
@@ -193,6 +194,16 @@ int gtn_lanczos_min(gtn_map map, void* x, int krylovdim, double tol, int maxiter
  * orthogonalisation and sub-stepping to meet tol.  info[0] = substeps, info[1] = matvecs. */
 int gtn_expm_apply(gtn_map map, double dz_re, double dz_im, void* x, int krylovdim,
                    double tol, int* info);
+/* The same for a map that is not Hermitian (exponentiate with ishermitian = false, as the
+ * TDVP sweeps call it for a TTNO without the Hermitian trait, lib/GraftEvolution/src/
+ * Evolution/tdvp.jl:204-281): an Arnoldi basis with two FP64 classical Gram-Schmidt
+ * passes, exp of the small Hessenberg matrix by scaling and squaring, sub-stepping on the
+ * error estimate beta |h(m+1,m)| |e_m^T exp(dz H_m) e_1|.  Same arguments and info. */
+int gtn_expm_apply_arnoldi(gtn_map map, double dz_re, double dz_im, void* x, int krylovdim,
+                           double tol, int* info);
+/* Host utility behind the Arnoldi exponential: E = exp(A) for a dense complex m x m matrix
+ * (1 <= m <= 256), row-major with interleaved real and imaginary parts (2 m^2 doubles). */
+int gtn_expm_small(int m, const double* A, double* E);
 
 /* ---- factorisations (FP64, cuSOLVER runtime calls) --------------------------------
  * split_svd / TruncationScheme, lib/GraftFoundation/src/Backend/Backend.jl:466-505;

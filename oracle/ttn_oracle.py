@@ -861,9 +861,12 @@ def lanczos_min(apply, x0, krylovdim=20, tol=1e-12, maxiter=100):
     return theta, v.reshape(shape), dict(iters=maxiter, matvecs=matvecs, resid=resid)
 
 
-def krylov_expm(apply, dz, x, krylovdim=30, tol=1e-12, max_substeps=64):
-    """exp(dz H) x for a Hermitian map H (Lanczos + exact small exponential, with
-    sub-stepping when the a-posteriori error estimate exceeds tol)."""
+def krylov_expm(apply, dz, x, krylovdim=30, tol=1e-12, max_substeps=64, hermitian=True):
+    """exp(dz H) x (KrylovKit's exponentiate as Evolution.jl:54-68 calls it): Lanczos for a
+    Hermitian map, Arnoldi otherwise, with the exact small exponential and sub-stepping when
+    the a-posteriori error estimate exceeds tol."""
+    if not hermitian:
+        return _arnoldi_expm(apply, dz, x, krylovdim, tol, max_substeps)
     shape = x.shape
     y = x.reshape(-1).astype(np.complex128)
     remaining = 1.0
@@ -895,6 +898,48 @@ def krylov_expm(apply, dz, x, krylovdim=30, tol=1e-12, max_substeps=64):
         evals, Q = np.linalg.eigh(T)
         c = Q @ (np.exp(dz * step * evals) * Q[0].conj())
         err = beta0 * abs(b[m - 1] * c[m - 1]) if m == kd else 0.0
+        if err > tol and steps < max_substeps:
+            frac = step / 2
+            steps += 1
+            continue
+        y = beta0 * (V[:m].T @ c)
+        remaining -= step
+    return y.reshape(shape)
+
+
+def _arnoldi_expm(apply, dz, x, krylovdim=30, tol=1e-12, max_substeps=64):
+    """Arnoldi form of krylov_expm for a map that is not Hermitian: two classical
+    Gram-Schmidt passes, the Hessenberg projection H_m, exp(dz H_m) e_1 by scipy's expm,
+    error estimate beta |h(m+1,m)| |(exp(dz H_m) e_1)_m|."""
+    shape = x.shape
+    y = x.reshape(-1).astype(np.complex128)
+    remaining = 1.0
+    frac = 1.0
+    steps = 0
+    while remaining > 1e-15:
+        step = min(frac, remaining)
+        beta0 = np.linalg.norm(y)
+        if beta0 == 0:
+            return y.reshape(shape)
+        n = y.size
+        kd = min(krylovdim, n)
+        V = np.zeros((kd + 1, n), dtype=np.complex128)
+        V[0] = y / beta0
+        Hm = np.zeros((kd + 1, kd), dtype=np.complex128)
+        m = kd
+        for j in range(kd):
+            w = apply(V[j].reshape(shape)).reshape(-1)
+            for _ in range(2):
+                h = V[: j + 1].conj() @ w
+                w = w - V[: j + 1].T @ h
+                Hm[: j + 1, j] += h
+            Hm[j + 1, j] = np.linalg.norm(w)
+            if Hm[j + 1, j].real < 1e-13 * max(1.0, np.max(np.abs(Hm[: j + 1, j]))):
+                m = j + 1
+                break
+            V[j + 1] = w / Hm[j + 1, j].real
+        c = sla.expm(dz * step * Hm[:m, :m])[:, 0]
+        err = beta0 * abs(Hm[m, m - 1]) * abs(c[m - 1]) if m == kd else 0.0
         if err > tol and steps < max_substeps:
             frac = step / 2
             steps += 1
@@ -1125,16 +1170,19 @@ def dmrg1_3s(psi, Ws, maxdim=100, nsweeps=10, tol=1e-10, krylovdim=20, mixing=1.
     return psi, energies
 
 
-def tdvp1_step(psi, Ws, dz, cache=None, krylovdim=30, tol=1e-12):
+def tdvp1_step(psi, Ws, dz, cache=None, krylovdim=30, tol=1e-12, hermitian=True):
     """Order-2 TDVP1 step (tdvp.jl:171-195): forward half sweep with the turning site
     evolved by the full dz, then the reverse half sweep skipping that site."""
     cache = cache or EnvCache(psi.topo)
-    _tdvp1_sweep(psi, Ws, dz / 2, cache, rev=False, terminal_dz=dz, krylovdim=krylovdim, tol=tol)
-    _tdvp1_sweep(psi, Ws, dz / 2, cache, rev=True, skip_initial=True, krylovdim=krylovdim, tol=tol)
+    _tdvp1_sweep(psi, Ws, dz / 2, cache, rev=False, terminal_dz=dz, krylovdim=krylovdim, tol=tol,
+                 hermitian=hermitian)
+    _tdvp1_sweep(psi, Ws, dz / 2, cache, rev=True, skip_initial=True, krylovdim=krylovdim, tol=tol,
+                 hermitian=hermitian)
     return cache
 
 
-def _tdvp1_sweep(psi, Ws, dz, cache, rev, terminal_dz=None, skip_initial=False, krylovdim=30, tol=1e-12):
+def _tdvp1_sweep(psi, Ws, dz, cache, rev, terminal_dz=None, skip_initial=False, krylovdim=30, tol=1e-12,
+                 hermitian=True):
     """(tdvp.jl:197-249)"""
     t = psi.topo
     order = t.postorder()
@@ -1146,7 +1194,7 @@ def _tdvp1_sweep(psi, Ws, dz, cache, rev, terminal_dz=None, skip_initial=False, 
         if not (skip_initial and i == 0):
             sdz = terminal_dz if (terminal_dz is not None and i == len(order) - 1) else dz
             h1 = eff_h1(cache, psi, Ws, n)
-            A = krylov_expm(h1, sdz, psi.tensors[n], krylovdim=krylovdim, tol=tol)
+            A = krylov_expm(h1, sdz, psi.tensors[n], krylovdim=krylovdim, tol=tol, hermitian=hermitian)
             psi.tensors[n] = A
             cache.invalidate_node(n)
         if i == len(order) - 1:
@@ -1155,12 +1203,12 @@ def _tdvp1_sweep(psi, Ws, dz, cache, rev, terminal_dz=None, skip_initial=False, 
         for j in range(1, len(seg)):
             u, v = seg[j - 1], seg[j]
             if (t.parent[u] == v) != rev:
-                _evolve_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol)
+                _evolve_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol, hermitian)
             else:
                 move_center(psi, v, cache.invalidate_edge)
 
 
-def _evolve_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol):
+def _evolve_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol, hermitian=True):
     """(tdvp.jl:257-301) QR split, backward link evolution with eff_h0, absorb."""
     t = psi.topo
     if t.parent[u] == v:
@@ -1168,7 +1216,7 @@ def _evolve_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol):
         psi.tensors[u] = Q
         cache.invalidate_node(u)
         k0 = eff_h0(cache, psi, Ws, u, v)
-        C = krylov_expm(k0, -dz, C, krylovdim=krylovdim, tol=tol)
+        C = krylov_expm(k0, -dz, C, krylovdim=krylovdim, tol=tol, hermitian=hermitian)
         psi.tensors[v] = absorb_on_leg(psi.tensors[v], C, t.childslot(v, u))
     else:
         k = t.childslot(u, v)
@@ -1177,7 +1225,7 @@ def _evolve_link_and_move(psi, Ws, u, v, dz, cache, krylovdim, tol):
         C = Cd.T
         cache.invalidate_node(u)
         k0 = eff_h0(cache, psi, Ws, v, u)
-        C = krylov_expm(k0, -dz, C, krylovdim=krylovdim, tol=tol)
+        C = krylov_expm(k0, -dz, C, krylovdim=krylovdim, tol=tol, hermitian=hermitian)
         psi.tensors[v] = np.tensordot(psi.tensors[v], C, axes=([psi.tensors[v].ndim - 1], [0]))
     psi.center = v
     cache.invalidate_node(v)

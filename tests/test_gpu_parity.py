@@ -153,6 +153,37 @@ def test_tdvp1_full_rank_vs_exact(ctx):
     assert abs(np.linalg.norm(v1) - 1) < 1e-10
 
 
+def test_tdvp1_non_hermitian_full_rank_vs_exact(ctx):
+    # a TTNO without the Hermitian trait (TFI plus an imaginary field 0.3i Z on every site)
+    # takes the Arnoldi exponential, as the reference's TDVP passes ishermitian(H) = false
+    # to exponentiate (tdvp.jl:204-281); at full bond dimension TDVP1 is exact, and the
+    # evolution is not norm-preserving
+    topo = G.star_topology(3, 2)
+    H = G.tfi(topo, g=0.9)
+    S = G.spin_ops()
+    for i in range(topo.nnodes):
+        H.onsite[i] = H.onsite[i] + 0.3j * S["Z"]
+    H.hermitian = False
+    W = G.TTNO.from_hamiltonian(H, ctx)
+    assert not W.ishermitian
+    Ho = O.tfi(O.star_topology(3, 2), g=0.9)
+    So = O.spin_ops()
+    for i in range(len(Ho.onsite)):
+        Ho.onsite[i] = Ho.onsite[i] + 0.3j * So["Z"]
+    Hd = O.dense_hamiltonian(Ho)
+    assert np.linalg.norm(Hd - Hd.conj().T) > 1.0
+    psi = G.random_ttns(np.random.default_rng(12), topo, 2, 8, ctx=ctx)
+    v0 = O.to_dense(oracle_state(psi))
+    dt, nsteps = 0.02, 5
+    vex = O.exact_evolve(Hd, v0, -1j * dt * nsteps)
+    ev = G.TDVP1(order=2)
+    for _ in range(nsteps):
+        ev.step(psi, W, -1j * dt)
+    v1 = O.to_dense(oracle_state(psi))
+    assert abs(np.linalg.norm(vex) - 1) > 1e-3
+    assert np.linalg.norm(v1 - vex) < 1e-9 * np.linalg.norm(vex)
+
+
 def test_tdvp2_full_rank_vs_exact(ctx):
     topo = G.star_topology(3, 2)
     W = G.TTNO.from_hamiltonian(G.tfi(topo, g=0.9), ctx)

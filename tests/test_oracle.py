@@ -153,6 +153,33 @@ def test_predictor_schemes_span_the_exact_predictor():
         O.predictor_basis(P, 6, "lanczos")
 
 
+def test_tdvp1_non_hermitian_full_rank_vs_exact():
+    # TFI plus an imaginary field 0.3i Z: the Arnoldi exponential (ishermitian = false,
+    # tdvp.jl:204-281); at full bond dimension the TDVP1 splitting reproduces exp(dz H) v
+    # for this non-normal generator as it does for a Hermitian one
+    topo = O.star_topology(3, 2)
+    H = O.tfi(topo, g=0.9)
+    S = O.spin_ops()
+    for i in range(topo.nnodes):
+        H.onsite[i] = H.onsite[i] + 0.3j * S["Z"]
+    Hd = O.dense_hamiltonian(H)
+    psi = O.random_ttns(np.random.default_rng(12), topo, 2, 8)
+    v0 = O.to_dense(psi)
+    vex = O.exact_evolve(Hd, v0, -1j * 0.02 * 5)
+    cache = None
+    for _ in range(5):
+        cache = O.tdvp1_step(psi, O.ttno_nn(H), -1j * 0.02, cache, hermitian=False)
+    v1 = O.to_dense(psi)
+    assert abs(np.linalg.norm(vex) - 1) > 1e-3
+    assert np.linalg.norm(v1 - vex) < 1e-9 * np.linalg.norm(vex)
+    # the Lanczos form on the same generator is measurably wrong
+    psi2 = O.random_ttns(np.random.default_rng(12), topo, 2, 8)
+    cache = None
+    for _ in range(5):
+        cache = O.tdvp1_step(psi2, O.ttno_nn(H), -1j * 0.02, cache)
+    assert np.linalg.norm(O.to_dense(psi2) - vex) > 1e-6 * np.linalg.norm(vex)
+
+
 def test_tdvp2_full_rank_vs_exact():
     # full bond dimension: every two-site and one-site projector is the identity, so the
     # order-2 TDVP2 step equals exact evolution (tdvp.jl:307-431)
