@@ -43,6 +43,16 @@ cudaError_t ctx_red(gtn_ctx ctx, size_t n2) {
   return cudaSuccess;
 }
 
+MapUse::MapUse(gtn_map_s* map) : m(map), ok(map != nullptr && map->busy.exchange(1) == 0) {}
+MapUse::~MapUse() {
+  if (ok) m->busy.store(0);
+}
+
+int map_busy_error(gtn_map_s* map) {
+  return set_err(map->ctx, GTN_ERR_INVALID,
+                 "map is in use by another call: a map is not reentrant (one map per host thread)");
+}
+
 extern "C" {
 
 int gtn_ctx_create(int device, gtn_ctx* out) {
@@ -142,6 +152,7 @@ int gtn_map_create(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t*
 
 int gtn_map_destroy(gtn_map map) {
   if (!map) return GTN_ERR_INVALID;
+  if (map->busy.load() != 0) return map_busy_error(map);
   if (map->ctx) cudaStreamSynchronize(map->ctx->stream);
   map_free(map);
   delete map;
@@ -150,6 +161,8 @@ int gtn_map_destroy(gtn_map map) {
 
 int gtn_map_apply_prec(gtn_map map, int precision, const void* x, void* y) {
   if (!map || !x || !y) return GTN_ERR_INVALID;
+  MapUse use(map);
+  if (!use.ok) return map_busy_error(map);
   return map_run(map, precision, static_cast<const double2*>(x), static_cast<double2*>(y));
 }
 
@@ -161,12 +174,16 @@ int gtn_map_apply(gtn_map map, const void* x, void* y) {
 int gtn_map_apply_profiled(gtn_map map, int precision, const void* x, void* y, int cap, double* ms,
                            int* kind, double* flops, int* count) {
   if (!map || !x || !y || !ms || !kind || !flops || !count) return GTN_ERR_INVALID;
+  MapUse use(map);
+  if (!use.ok) return map_busy_error(map);
   return map_run_profiled(map, precision, static_cast<const double2*>(x), static_cast<double2*>(y), cap, ms,
                           kind, flops, count);
 }
 
 int gtn_map_apply_host(gtn_map map, const void* x_host, void* y_host) {
   if (!map || !x_host || !y_host) return GTN_ERR_INVALID;
+  MapUse use(map);
+  if (!use.ok) return map_busy_error(map);
   gtn_ctx ctx = map->ctx;
   if (!map->dx) {
     if (cudaMalloc(&map->dx, map->x_elems * sizeof(double2)) != cudaSuccess ||

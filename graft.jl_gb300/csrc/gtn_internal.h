@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -293,8 +294,20 @@ struct PlanStep {
   double macs = 0;
 };
 
+// Entry guard of the public calls that run a map: a map owns its workspace and Krylov
+// basis, so like the reference's WorkspaceMap (lib/GraftPlanning/src/Planning/
+// types.jl:503-552) it is task-local and non-reentrant; a second concurrent call is refused.
+struct MapUse {
+  gtn_map_s* m;
+  bool ok;
+  explicit MapUse(gtn_map_s* map);
+  ~MapUse();
+};
+int map_busy_error(gtn_map_s* map);
+
 struct gtn_map_s {
   gtn_ctx ctx = nullptr;
+  std::atomic<int> busy{0};  // set while a public call runs on this map (maps are not reentrant)
   int precision = 0;
   std::vector<int64_t> x_dims, y_dims;
   int64_t x_elems = 0, y_elems = 0;

@@ -283,6 +283,8 @@ int thick_keep(int kd, int m) { return std::max(0, std::min((3 * kd + 2) / 5, m 
 extern "C" int gtn_lanczos_min(gtn_map map, void* xv, int krylovdim, double tol, int maxiter, int rq_fp64,
                                double* energy, int* info, double* resid) {
   if (!map || !xv || !energy) return GTN_ERR_INVALID;
+  MapUse use(map);
+  if (!use.ok) return map_busy_error(map);
   Krylov K;
   int st = krylov_setup(map, std::min<int64_t>(krylovdim, std::max<int64_t>(map->x_elems, 1)), &K);
   if (st != GTN_OK) return st;
@@ -387,6 +389,8 @@ extern "C" int gtn_lanczos_min(gtn_map map, void* xv, int krylovdim, double tol,
 extern "C" int gtn_expm_apply(gtn_map map, double dz_re, double dz_im, void* xv, int krylovdim, double tol,
                               int* info) {
   if (!map || !xv) return GTN_ERR_INVALID;
+  MapUse use(map);
+  if (!use.ok) return map_busy_error(map);
   Krylov K;
   int st = krylov_setup(map, std::min<int64_t>(krylovdim, std::max<int64_t>(map->x_elems, 1)), &K);
   if (st != GTN_OK) return st;
@@ -556,6 +560,8 @@ extern "C" int gtn_expm_small(int m, const double* A, double* E) {
 extern "C" int gtn_expm_apply_arnoldi(gtn_map map, double dz_re, double dz_im, void* xv, int krylovdim, double tol,
                                       int* info) {
   if (!map || !xv) return GTN_ERR_INVALID;
+  MapUse use(map);
+  if (!use.ok) return map_busy_error(map);
   Krylov K;
   int st = krylov_setup(map, std::min<int64_t>(krylovdim, std::max<int64_t>(map->x_elems, 1)), &K);
   if (st != GTN_OK) return st;
