@@ -821,43 +821,77 @@ def expect(psi, Ws):
 # ---------------------------------------------------------------------------
 
 
+def _projected(m, k, a, b, s):
+    """Projected matrix of a thick-restarted Lanczos basis: kept Ritz values a[:k] coupled to
+    column k by the arrow s, then the Lanczos tridiagonal (a, b)."""
+    T = np.zeros((m, m))
+    T[np.arange(m), np.arange(m)] = a[:m]
+    for i in range(k, m - 1):
+        T[i, i + 1] = T[i + 1, i] = b[i]
+    if k < m:
+        T[:k, k] = s[:k]
+        T[k, :k] = s[:k]
+    return T
+
+
 def lanczos_min(apply, x0, krylovdim=20, tol=1e-12, maxiter=100):
-    """Lowest eigenpair of a Hermitian map: Lanczos with full re-orthogonalisation,
-    restarted from the current Ritz vector.  Returns (E, v, info)."""
+    """Lowest eigenpair of a Hermitian map as KrylovKit 0.10's Lanczos eigsolve computes it
+    for the reference's groundstate_eigsolve_backend (GroundState.jl:25-39): full
+    re-orthogonalisation (two classical Gram-Schmidt passes), convergence checked after
+    every step on the absolute residual |beta_m q_m| <= tol, and thick restarts that keep
+    the lowest (3 krylovdim + 2) / 5 Ritz vectors (Wu and Simon's thick-restart Lanczos).
+    Returns (E, v, info)."""
     shape = x0.shape
-    v = x0.reshape(-1).astype(np.complex128)
-    v = v / np.linalg.norm(v)
-    n = v.size
-    theta = None
+    n = x0.size
+    kd = min(krylovdim, n)
+    V = np.zeros((kd + 1, n), dtype=np.complex128)
+    V[0] = x0.reshape(-1) / np.linalg.norm(x0)
+    a = np.zeros(kd)
+    b = np.zeros(kd)
+    s = np.zeros(kd)
+    k = 0
     matvecs = 0
+    theta, resid, v = None, np.inf, V[0]
     for it in range(maxiter):
-        kd = min(krylovdim, n)
-        V = np.zeros((kd + 1, n), dtype=np.complex128)
-        V[0] = v
-        a = np.zeros(kd)
-        b = np.zeros(kd)
-        m = kd
-        for j in range(kd):
+        m, brk = kd, False
+        for j in range(k, kd):
             w = apply(V[j].reshape(shape)).reshape(-1)
             matvecs += 1
-            a[j] = np.vdot(V[j], w).real
-            # two passes of classical Gram-Schmidt against the whole basis
+            hj = 0.0
             for _ in range(2):
-                w = w - V[: j + 1].T @ (V[: j + 1].conj() @ w)
+                h = V[: j + 1].conj() @ w
+                w = w - V[: j + 1].T @ h
+                hj += h[j].real
+            a[j] = hj
             b[j] = np.linalg.norm(w)
             if b[j] < 1e-14 * max(1.0, abs(a[j])):
-                m = j + 1
+                m, brk = j + 1, True
                 break
             V[j + 1] = w / b[j]
-        T = np.diag(a[:m]) + np.diag(b[: m - 1], 1) + np.diag(b[: m - 1], -1)
-        evals, evecs = np.linalg.eigh(T)
-        theta = evals[0]
-        s = evecs[:, 0]
-        resid = abs(b[m - 1] * s[m - 1])
-        v = V[:m].T @ s
-        v = v / np.linalg.norm(v)
-        if resid <= tol * max(1.0, abs(theta)) or m < kd or m == n:
-            return theta, v.reshape(shape), dict(iters=it + 1, matvecs=matvecs, resid=resid)
+            if j + 1 >= 2 or kd == 1:
+                ev, Q = np.linalg.eigh(_projected(j + 1, k, a, b, s))
+                if abs(b[j] * Q[j, 0]) <= tol:
+                    m = j + 1
+                    break
+        ev, Q = np.linalg.eigh(_projected(m, k, a, b, s))
+        theta = ev[0]
+        resid = 0.0 if brk else abs(b[m - 1] * Q[m - 1, 0])
+        converged = brk or resid <= tol or m == n
+        keep = max(0, min((3 * kd + 2) // 5, m - 1))
+        if converged or it == maxiter - 1 or keep == 0:
+            v = V[:m].T @ Q[:, 0]
+            v = v / np.linalg.norm(v)
+            if converged or it == maxiter - 1:
+                return theta, v.reshape(shape), dict(iters=it + 1, matvecs=matvecs, resid=resid)
+            V[0] = v
+            k = 0
+            continue
+        # thick restart: V[:keep] <- V[:m] Q[:, :keep], the residual direction V[m] follows
+        V[:keep] = (V[:m].T @ Q[:, :keep]).T
+        V[keep] = V[m]
+        s[:keep] = b[m - 1] * Q[m - 1, :keep]
+        a[:keep] = ev[:keep]
+        k = keep
     return theta, v.reshape(shape), dict(iters=maxiter, matvecs=matvecs, resid=resid)
 
 
