@@ -55,7 +55,7 @@ def test_map_is_not_reentrant(ctx):
 
     def solve():
         try:
-            h.lanczos_min(x, krylovdim=20, tol=0.0, maxiter=3000)  # runs to maxiter
+            h.lanczos_min(x, krylovdim=20, tol=0.0, maxiter=1000)  # runs to maxiter
         except Exception as e:  # noqa: BLE001
             errors.append(e)
         finally:
