@@ -246,6 +246,26 @@ def test_dmrg1_3s_matches_oracle_and_ed(ctx):
     assert abs(Es[-1] - E0) / abs(E0) < 1e-10
 
 
+@pytest.mark.parametrize("scheme,kw", [("exact", {}), ("rsvd", dict(rsvd_oversample=2)), ("directqr", {}),
+                                       ("rangefinder", dict(rsvd_oversample=2, rsvd_poweriter=1))])
+def test_expand_keeps_the_state_and_grows_the_bond(ctx, scheme, kw):
+    # the reference's expand! gates (test/runtests.jl:702-748) on the device path: a leaf edge
+    # of a bond-1 state of the 4-site star grows within maxdim 4 and the state is unchanged
+    from grafttn.contractions import EnvCache
+    from grafttn.solvers import expand
+    topo = G.star_topology(3, 1)
+    W = G.TTNO.from_hamiltonian(G.tfi(topo, g=0.9), ctx)
+    psi = G.random_ttns(np.random.default_rng(1101), topo, 2, 1, ctx=ctx)
+    v = O.to_dense(oracle_state(psi))
+    leaf = [n for n in range(topo.nnodes) if not topo.children[n]][0]
+    rng = np.random.default_rng(2202) if scheme in ("rsvd", "rangefinder") else None
+    assert expand(EnvCache(topo), psi, W, leaf, topo.parent[leaf], 4, max_add=3, scheme=scheme, rng=rng, **kw)
+    assert np.linalg.norm(O.to_dense(oracle_state(psi)) - v) < 1e-10
+    assert 1 < max(psi.bond_dims()) <= 4
+    with pytest.raises(ValueError):
+        expand(EnvCache(topo), psi, W, leaf, topo.parent[leaf], 4, max_add=3, scheme="unknown")
+
+
 @pytest.mark.parametrize("scheme", ["directqr", "rsvd", "rangefinder"])
 def test_dmrg1_3s_schemes_match_oracle_and_ed(ctx, scheme):
     # expand!'s other predictor schemes (expansion.jl:240-370), probes drawn from the same

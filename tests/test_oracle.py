@@ -125,6 +125,28 @@ def test_dmrg1_3s_schemes_grow_bonds_to_ed(scheme):
     assert abs(Es[-1] - E0) < 1e-9
 
 
+@pytest.mark.parametrize("scheme,kw", [("exact", {}), ("rsvd", dict(oversample=2)), ("directqr", {}),
+                                       ("rangefinder", dict(oversample=2, poweriter=1))])
+def test_expand_keeps_the_state_and_grows_the_bond(scheme, kw):
+    # the reference's expand! gates (test/runtests.jl:702-748): on a leaf edge of a bond-1
+    # state of the 4-site star, every scheme leaves the state unchanged and grows the bond
+    # within maxdim 4; the randomised schemes refuse to run without an rng
+    topo = O.star_topology(3, 1)
+    Ws = O.ttno_nn(O.tfi(topo, g=0.9))
+    psi = O.random_ttns(np.random.default_rng(1101), topo, 2, 1)
+    v = O.to_dense(psi)
+    leaf = [n for n in range(topo.nnodes) if not topo.children[n]][0]
+    rng = np.random.default_rng(2202) if scheme in ("rsvd", "rangefinder") else None
+    O.expand(psi, Ws, O.EnvCache(topo), leaf, topo.parent[leaf], 4, max_add=3, scheme=scheme, rng=rng, **kw)
+    assert np.linalg.norm(O.to_dense(psi) - v) < 1e-10
+    assert 1 < max(O.bond_dims(psi)) <= 4
+    if rng is not None:
+        with pytest.raises(ValueError):
+            O.expand(psi, Ws, O.EnvCache(topo), leaf, topo.parent[leaf], 4, max_add=3, scheme=scheme)
+    with pytest.raises(ValueError):
+        O.expand(psi, Ws, O.EnvCache(topo), leaf, topo.parent[leaf], 4, max_add=3, scheme="unknown")
+
+
 def test_predictor_schemes_span_the_exact_predictor():
     # a rank-12 predictor: rangefinder and rsvd sketches with 12 + oversample columns capture
     # its whole range, so the exact scheme's leading directions lie inside both; directqr
