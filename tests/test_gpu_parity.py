@@ -125,6 +125,44 @@ def test_h0_and_env_match_oracle(ctx):
     assert rel(ctx.download(k0(ctx.upload(x))), ok0(x)) < 1e-12
 
 
+def test_h0_non_square_link_matches_oracle(ctx):
+    # test/contraction_planning.jl:1151-1193: the TDVP1 child -> parent QR seam with a wide
+    # old bond (physical 2, bond 4) leaves a non-square link C (2 x 4); h0 on C and on an
+    # independent probe of that shape matches the oracle
+    topo = G.mps_topology(2)
+    root, child = 0, 1
+    rng = np.random.default_rng(1701)
+    tensors = [O.randn_c(rng, (4, 2, 1)), O.randn_c(rng, (2, 4))]   # root, child
+    psi = G.TTNS(topo, tensors, child, ctx)
+    W = G.TTNO.from_hamiltonian(G.tfi(topo, g=0.37), ctx)
+    Q, C = G.networks.left_orth(ctx, psi.tensors[child])
+    assert tuple(C.shape) == (2, 4)
+    psi.tensors[child] = Q
+    cache = G.EnvCache(topo)
+    k0 = G.eff_h0(cache, psi, W, child, root)
+    o = oracle_state(psi)
+    ok0 = O.eff_h0(O.EnvCache(o.topo), o, O.ttno_nn(O.tfi(O.mps_topology(2), g=0.37)), child, root)
+    assert tuple(ok0.shape) == (2, 4)
+    for x in (ctx.download(C), O.randn_c(np.random.default_rng(1702), (2, 4))):
+        assert rel(ctx.download(k0(ctx.upload(x))), ok0(x)) < 1e-12
+    k0.close()
+
+
+@pytest.mark.parametrize("which", ["mps6", "star32", "bin2"])
+def test_gauge_moves_keep_the_state(ctx, which):
+    # test/runtests.jl:336-347: a random bond-3 state is normalised, and moving its centre
+    # to a leaf leaves the state unchanged
+    topo = {"mps6": G.mps_topology(6), "star32": G.star_topology(3, 2), "bin2": G.binary_topology(2)}[which]
+    psi = G.random_ttns(np.random.default_rng(20), topo, 2, 3, ctx=ctx)
+    assert abs(psi.norm() - 1) < 1e-12
+    v = O.to_dense(oracle_state(psi))
+    assert abs(np.linalg.norm(v) - 1) < 1e-12
+    leaf = [n for n in range(topo.nnodes) if not topo.children[n]][-1]
+    G.move_center(psi, leaf)
+    assert psi.center == leaf
+    assert np.linalg.norm(O.to_dense(oracle_state(psi)) - v) < 1e-12
+
+
 def test_merge_split_roundtrip(ctx):
     topo = G.star_topology(3, 2)
     psi = G.random_ttns(np.random.default_rng(10), topo, 2, 3, ctx=ctx)
