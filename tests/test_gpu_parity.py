@@ -105,6 +105,33 @@ def test_h2_matches_oracle_binary_heisenberg(ctx, precision, tol):
         h2.close()
 
 
+@pytest.mark.parametrize("which", ["fork", "kary"])
+def test_maps_match_oracle_on_fork_and_kary_trees(ctx, which):
+    # planned maps == oracle ncon and Hermitian on the fork and 3-ary trees
+    # (test/contraction_planning.jl:111-160,219-228): eff_h1 at every node, eff_h2 on every edge
+    topo = G.fork_topology(2, 2) if which == "fork" else G.kary_topology(3, 2)
+    W = G.TTNO.from_hamiltonian(G.heisenberg(topo), ctx)
+    psi = G.random_ttns(np.random.default_rng(30), topo, 2, 3, ctx=ctx)
+    rng = np.random.default_rng(31)
+    for n in range(topo.nnodes):
+        G.move_center(psi, n)
+        o = oracle_state(psi)
+        Ws = O.ttno_nn(O.heisenberg(o.topo))
+        cache, ocache = G.EnvCache(topo), O.EnvCache(o.topo)
+        h1, oh1 = G.eff_h1(cache, psi, W, n), O.eff_h1(ocache, o, Ws, n)
+        a, b = O.randn_c(rng, oh1.shape), O.randn_c(rng, oh1.shape)
+        ha, hb = ctx.download(h1(ctx.upload(a))), ctx.download(h1(ctx.upload(b)))
+        assert rel(ha, oh1(a)) < 1e-12, (which, n)
+        assert abs(np.vdot(a, hb) - np.vdot(ha, b)) < 1e-11 * np.linalg.norm(a) * np.linalg.norm(b)
+        h1.close()
+        if topo.parent[n] >= 0:
+            m = topo.parent[n]
+            h2, oh2 = G.eff_h2(cache, psi, W, n, m, "fp64"), O.eff_h2(ocache, o, Ws, n, m)
+            x = O.randn_c(rng, oh2.shape)
+            assert rel(ctx.download(h2(ctx.upload(x))), oh2(x)) < 1e-12, (which, n, m)
+            h2.close()
+
+
 def test_h0_and_env_match_oracle(ctx):
     topo = G.binary_topology(2)
     H = G.heisenberg(topo)
