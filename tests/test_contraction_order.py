@@ -63,13 +63,12 @@ def test_choose_order_keeps_env_first_unless_clearly_cheaper():
     assert GC.choose_order(shapes, labels, order) == order
     # the root of a 4-ary tree at a wide TTNO bond: absorbing every environment before W
     # grows the running tensor by w per leg, and a cheaper chain replaces it
+    # (here W moves ahead of the last two environments, 6.2x cheaper)
     shapes, labels, order = h1_network(G.kary_topology(4, 2), 0, 8, 5)
     chosen = GC.choose_order(shapes, labels, order)
-    if chosen != order:
-        assert 3 * GC._objective(shapes, labels, chosen) < 2 * GC._objective(shapes, labels, order)
-    else:
-        best = GC.best_order(shapes, labels, 0)
-        assert 3 * GC._objective(shapes, labels, best) >= 2 * GC._objective(shapes, labels, order)
+    assert chosen != order
+    assert chosen.index(1) < order.index(1)
+    assert 3 * GC._objective(shapes, labels, chosen) < 2 * GC._objective(shapes, labels, order)
     # more than 13 operands: the given order, without a search
     many = [[-1, 1]] + [[i, i + 1] for i in range(1, 14)] + [[14, -2]]
     shp = [(2, 2)] * len(many)
