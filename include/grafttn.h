@@ -212,7 +212,11 @@ int gtn_expm_small(int m, const double* A, double* E);
 /* Truncated SVD of the row-major m x n matrix A (device c128).  Keeps
  * r = min(maxdim, #{s > max(atol, rtol*s0)}, discarded-weight rank) >= 1 values.
  * U (m x r, row-major), S (r doubles, HOST), Vh (r x n, row-major) must hold
- * min(m,n) columns/rows of capacity.  *rank = r, *discarded = 2-norm of dropped s. */
+ * min(m,n) columns/rows of capacity.  *rank = r, *discarded = 2-norm of dropped s.
+ * Routes: cuSOLVER gesvd below min(m,n) = 384; above it, subspace iteration on
+ * maxdim + max(32, maxdim/2) vectors when four times that fits in min(m,n) and its
+ * leading values settle (environment GTN_SVD_SUBSPACE=0 turns it off), else the Gram
+ * matrix with Zheevd; rows of Vh are re-orthonormalised by a thin QR after both. */
 int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, int64_t maxdim,
                   double atol, double rtol, double discarded_weight, void* U, double* S,
                   void* Vh, int64_t* rank, double* discarded);
