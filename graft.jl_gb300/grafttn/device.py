@@ -60,13 +60,9 @@ class Context:
         return torch.empty(tuple(int(s) for s in shape), dtype=CDT, device=f"cuda:{self.device}")
 
     def copy(self, t):
-        """Copy of a device tensor made on the context's stream, so that it follows the
-        context's pending work (a torch copy would run on torch's stream, unordered with the
-        context's non-blocking one)."""
-        if not t.is_contiguous():
-            self.sync()
-            t = t.contiguous()
-            torch.cuda.current_stream(t.device).synchronize()
+        """Contiguous copy of a device tensor by the library's axpby kernel (the context
+        runs on torch's current stream, so it is ordered with the surrounding work)."""
+        t = t.contiguous()
         y = self.empty(t.shape)
         if t.numel():
             self.axpby(1.0, t, 0.0, y)

@@ -5,8 +5,8 @@ The randomised schemes take their Gaussian probe block from a caller-owned numpy
 in place of the reference's caller-owned Xoshiro stream (whose draws cannot be reproduced
 outside Julia): real parts first, then imaginary parts, scaled to unit complex variance.
 The probe is drawn on the host and uploaded; every product, QR and SVD runs on the device.
-This module only needs a context object with sync / upload / matmul / qr / svd_trunc / axpby /
-scale, so its logic is importable without a GPU.
+This module only needs a context object with upload / matmul / qr / svd_trunc / axpby / scale,
+so its logic is importable without a GPU.
 """
 from __future__ import annotations
 
@@ -53,7 +53,6 @@ def predictor_basis(ctx, P, cap, scheme="exact", rng=None, oversample=8, powerit
         return Q
     rest = int(P.shape[1])
     budget = min(rest, cap + oversample)
-    ctx.sync()  # the upload runs outside the context's stream
     omega = ctx.upload(probe_block(rng, rest, budget))
     Y = ctx.matmul(P, omega)
     if scheme == "rsvd":
@@ -84,12 +83,11 @@ def factorized_rangefinder_enrichment(ctx, Am, P, room, rng, oversample=8, power
     Q, _ = ctx.qr(Am.contiguous())
     if room <= 0 or Am.shape[0] <= Q.shape[1]:
         return Q, None
-    # a copy made on the context's stream (ctx.scale), not by torch on its own stream
+    # P_c is formed in place in a copy of P
     Pc = ctx.axpby(-1.0, ctx.matmul(Q, ctx.matmul(Q, P, conjA=True, transA=True)), 1.0,
                    ctx.scale(P.contiguous(), 1.0))
     rest = int(P.shape[1])
     sk = min(rest, room + oversample)
-    ctx.sync()  # the upload runs outside the context's stream
     omega = ctx.upload(probe_block(rng, rest, sk))
     S, _ = ctx.qr(ctx.matmul(Pc, omega).contiguous())
     for _ in range(poweriter):

@@ -1,7 +1,8 @@
 """Host-side check of the predictor-basis schemes of the bond expansion
 (grafttn/expansion.py; expand!, expansion.jl:240-370) against the oracle.
 
-The scheme logic only talks to its context through sync / upload / matmul / qr / svd_trunc.
+The scheme logic only talks to its context through upload / matmul / qr / svd_trunc / axpby /
+scale.
 HostContext below gives those calls the device context's signatures and results on CPU
 tensors, so the sequence of products, QRs, SVDs and probe draws is checked here without a
 GPU. The device arithmetic itself is covered by tests/test_gpu_parity.py."""
@@ -16,9 +17,6 @@ from oracle import ttn_oracle as O
 class HostContext:
     """The device context's dense calls on CPU complex128 tensors (axpby writes y in place, as
     the device call does)."""
-
-    def sync(self):
-        pass
 
     def upload(self, arr):
         return torch.from_numpy(np.ascontiguousarray(np.asarray(arr, dtype=np.complex128)))
