@@ -44,6 +44,12 @@ WORKLOADS = {
     "heisenberg_bin63_d3d2_D1024_eff_h2": ("binary", "n3_1", 1024),
     "heisenberg_bin63_d3d2_D256_eff_h2": ("binary", "n3_1", 256),
     "heisenberg_chain63_mid_D1024_eff_h2": ("mps", "site32", 1024),
+    # the other D = 256 edge classes of the binary tree that fit one GPU (depth2 -> depth1
+    # holds a 64 GiB two-site block at D = 256; at D = 64 it is 1 GiB)
+    "heisenberg_bin63_d1root_D256_eff_h2": ("binary", "n1_1", 256),
+    "heisenberg_bin63_d4d3_D256_eff_h2": ("binary", "n4_1", 256),
+    "heisenberg_bin63_d5d4_D256_eff_h2": ("binary", "n5_1", 256),
+    "heisenberg_bin63_d2d1_D64_eff_h2": ("binary", "n2_1", 64),
 }
 
 
@@ -53,12 +59,15 @@ DTYPES = {"bf16x6": "bf16x6 split products on tcgen05, f32 accumulate, c128 in/o
 PRODUCTS = {"bf16x6": 6, "fp16x3": 3, "bf16x3": 3}
 
 
-def workload_arrays(name=WORKLOAD, seed=7):
+def workload_arrays(name=WORKLOAD, seed=7, bond_dim=None):
     """Labels, order and seeded synthetic statics of one eff_h2 map of the workload table.
-    Bond dimensions follow the saturated tree: min(D, product of the legs below)."""
+    Bond dimensions follow the saturated tree: min(D, product of the legs below); bond_dim
+    replaces the table's D (small instances for checks).  On a root edge the root's parent
+    leg has dimension 1 and is closed by the ones cap, as eff_h2 does."""
     import grafttn as G
     from grafttn import contractions as GC
     kind, nid, Dm = WORKLOADS[name]
+    Dm = bond_dim or Dm
     topo = G.binary_topology(5) if kind == "binary" else G.mps_topology(63)
     n = topo.index[nid]
     m = topo.parent[n]
@@ -77,11 +86,14 @@ def workload_arrays(name=WORKLOAD, seed=7):
     bond = {v: min(Dm, below[v]) for v in range(topo.nnodes)}
     Ws = G.ttno_tensors(G.heisenberg(topo))
     k = topo.childslot(m, n)
+    root_edge = topo.parent[m] < 0
     x_shape = tuple([bond[c] for c in topo.children[n]] + [d]
-                    + [bond[c] for c in topo.children[m] if c != n] + [d, bond[m]])
+                    + [bond[c] for c in topo.children[m] if c != n] + [d, 1 if root_edge else bond[m]])
     pn = topo.nchildren(n) + 1
     labels, order, envs = GC.h2_spec(topo, n, m, len(x_shape), Ws[n].ndim, Ws[m].ndim, pn)
     statics = [Ws[n], Ws[m]] + [env(bond[w] if w != topo.parent[u] else bond[u]) for (w, u) in envs]
+    if root_edge:
+        statics.append(np.ones((1, 1, 1), dtype=np.complex128))
     theta = crandn(x_shape)
     theta /= np.linalg.norm(theta)
     assert k >= 0
