@@ -25,3 +25,9 @@ def test_root_edge_workload_closes_the_root():
     x_shape, labels, order, statics, _ = bench.workload_arrays("heisenberg_bin63_d1root_D256_eff_h2", bond_dim=4)
     assert x_shape[-1] == 1
     assert statics[-1].shape == (1, 1, 1)
+
+
+def test_metric_labels():
+    assert bench.metric_for(bench.WORKLOAD) == bench.METRIC
+    other = bench.metric_for("heisenberg_bin63_d1root_D256_eff_h2")
+    assert other != bench.METRIC and "d1root_D256" in other
