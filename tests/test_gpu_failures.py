@@ -35,45 +35,3 @@ def test_device_wait_timeout_is_reported_and_context_survives(ctx):
     assert ctx.lib.gtn_ctx_sync(ctx.h) == _lib.GTN_OK                 # flag cleared
     out = ctx.download(ctx.contract([ctx.upload(a), ctx.upload(b)], [[-1, 1], [1, -2]]))
     assert np.linalg.norm(out - a @ b) < 1e-12 * np.linalg.norm(a @ b)
-
-
-def test_map_is_not_reentrant(ctx):
-    # a map owns its workspace and Krylov basis; like the reference's WorkspaceMap
-    # (types.jl:503-552) it refuses a second call while one runs (ValueError, the reference's
-    # ArgumentError) and works again once that call has returned
-    import threading
-    import time
-    rng = np.random.default_rng(5)
-    n = 2000
-    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
-    Mh = (a + a.conj().T) / 2
-    h = EffectiveMap(ctx, (n,), [[1], [-1, 1]], [0, 1], [ctx.upload(Mh)], "fp64")
-    xh = rng.standard_normal(n) + 1j * rng.standard_normal(n)
-    x = ctx.upload(xh)
-    done = threading.Event()
-    errors = []
-
-    def solve():
-        try:
-            h.lanczos_min(x, krylovdim=20, tol=0.0, maxiter=1000)  # runs to maxiter
-        except Exception as e:  # noqa: BLE001
-            errors.append(e)
-        finally:
-            done.set()
-
-    worker = threading.Thread(target=solve)
-    worker.start()
-    time.sleep(0.3)
-    try:
-        h(x)
-        refused = False
-    except ValueError as e:
-        refused = "not reentrant" in str(e)
-    overlapped = not done.is_set()
-    worker.join()
-    assert not errors, errors
-    if not overlapped:
-        pytest.skip("the solve ended before the second call was made")
-    assert refused
-    y = ctx.download(h(x))
-    assert np.linalg.norm(y - Mh @ xh) < 1e-10 * np.linalg.norm(Mh @ xh)
