@@ -245,7 +245,7 @@ def test_tdvp1_non_hermitian_full_rank_vs_exact(ctx):
     for _ in range(nsteps):
         ev.step(psi, W, -1j * dt)
     v1 = O.to_dense(oracle_state(psi))
-    assert abs(np.linalg.norm(vex) - 1) > 1e-3
+    assert abs(np.linalg.norm(vex) - 1) > 1e-6  # not norm-preserving
     assert np.linalg.norm(v1 - vex) < 1e-9 * np.linalg.norm(vex)
 
 

@@ -192,7 +192,7 @@ def test_tdvp1_non_hermitian_full_rank_vs_exact():
     for _ in range(5):
         cache = O.tdvp1_step(psi, O.ttno_nn(H), -1j * 0.02, cache, hermitian=False)
     v1 = O.to_dense(psi)
-    assert abs(np.linalg.norm(vex) - 1) > 1e-3
+    assert abs(np.linalg.norm(vex) - 1) > 1e-6  # not norm-preserving
     assert np.linalg.norm(v1 - vex) < 1e-9 * np.linalg.norm(vex)
     # the Lanczos form on the same generator is measurably wrong
     psi2 = O.random_ttns(np.random.default_rng(12), topo, 2, 8)
