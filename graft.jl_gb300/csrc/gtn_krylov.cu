@@ -3,12 +3,15 @@
 //  lib/GraftEvolution/src/Evolution/Evolution.jl:54-68).
 //
 // Krylov vectors live in HBM as complex FP64.  Each Lanczos step applies the map (in its
-// precision mode), then runs two passes of classical Gram-Schmidt against the whole basis
-// in FP64 (batched projections h = V^H w and one linear combination per pass), then
-// normalises.  Only the tridiagonal coefficients cross to the host; the small symmetric
-// eigenproblem is solved there by cyclic Jacobi rotations.  The eigensolver restarts thick:
-// the lowest Ritz vectors are rotated in place at the front of the basis and the expansion
-// continues from the residual direction.
+// precision mode), takes the local three-term step against the two newest vectors in FP64,
+// then one reorthogonalisation pass against the whole basis (FP32 products for mixed-
+// precision maps, FP64 otherwise; a second FP64 pass when the DGKS test asks for it), then
+// normalises.  The first step of an expansion runs two full FP64 passes.  Only the projected
+// coefficients cross to the host; the small symmetric eigenproblem is solved there by
+// cyclic Jacobi rotations.  The eigensolver restarts thick: the lowest Ritz vectors are
+// rotated in place at the front of the basis and the expansion continues from the residual
+// direction.  Maps without the Hermitian trait take the Arnoldi exponential (two FP64
+// passes per step, exp of the Hessenberg matrix on the host).
 #include "gtn_internal.h"
 
 #include <algorithm>
