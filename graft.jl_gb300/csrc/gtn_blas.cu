@@ -1,6 +1,9 @@
-// FP64 vector kernels for the device-resident Krylov solvers (HBM-bound): batched
-// Gram-Schmidt projections h = V^H w, linear combinations w = b*w + s*V*c, and small
-// helpers for the factorisation paths.
+// Vector kernels for the device-resident Krylov solvers: batched Gram-Schmidt projections
+// h = V^H w, linear combinations w = b*w + s*V*c, their FP32-product variants, the thick-
+// restart basis rotation, and small helpers for the factorisation paths.  In FP64 a complex
+// multiply-add per element and vector costs four DFMA, which on this part bounds the
+// projections near 1.5 TB/s of streamed data, below HBM; the FP32 variants and the
+// one-to-two-vector kernels are bound by memory latency and HBM.
 #include "gtn_internal.h"
 
 namespace {
