@@ -176,19 +176,21 @@ class ClockSampler:
 
 def cpu_apply_rate(x_shape, labels, order, statics, theta, budget_s=20.0, max_applies=3, warm=False):
     """Applications of the oracle's env-first map per second on the host cores; stops after
-    `max_applies` or once `budget_s` is spent (at least one application)."""
+    `max_applies` or once `budget_s` is spent (at least one application).  Also returns the
+    oracle's output y = H_eff theta, the parity reference of the GPU results."""
     from oracle import ttn_oracle as O
     hm = O.EffMap(labels, order, statics, x_shape)
     if warm:
         hm(theta)
     n, t0 = 0, time.perf_counter()
+    y = None
     while n < max_applies:
-        hm(theta)
+        y = hm(theta)
         n += 1
         if time.perf_counter() - t0 > budget_s:
             break
     el = time.perf_counter() - t0
-    return n / el, n, el
+    return n / el, n, el, y
 
 
 def blas_threads():
@@ -430,9 +432,13 @@ def run_ours(args, rank, world):
     tot = sum(v[1] for v in by.values())
     kernels = {k: {"launches": v[0], "ms": round(v[1], 4), "share": round(v[1] / tot, 4)} for k, v in by.items()}
     tc = by.get("tc_gemm", [1, 1e-9, 0.0])
+    exec_flops = sum(v[2] for v in by.values())           # flops of the executed (grouped) chain
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
-    achieved = tc[2] / (tc[1] / 1000.0) / 1e12          # algorithmic complex flops / time
-    executed = achieved * PRODUCTS[args.precision]        # slice products per complex MAC
+    # roofline of the dominant kernel: the env-first chain's algorithmic flops of one
+    # application (8 per complex MAC) over the tc_gemm launches' event time of one application
+    achieved = flops / (tc[1] / 1000.0) / 1e12
+    # the tensor pipe's executed work: flops of the executed tc steps times the slice products
+    executed = tc[2] * PRODUCTS[args.precision] / (tc[1] / 1000.0) / 1e12
     traffic = profile_traffic("tc_gemm", args.workload)
 
     # end to end through the C ABI with host buffers (pinned), copies inside the timed region
@@ -449,10 +455,26 @@ def run_ours(args, rank, world):
 
     # CPU baseline: the oracle on the host cores, bounded sample of the same workload; the
     # oracle's count of the chain's flop checks the library's
-    cpu_rate, cpu_n, cpu_el = cpu_apply_rate(x_shape, labels, order, statics, theta, budget_s=20.0, max_applies=2)
+    cpu_rate, cpu_n, cpu_el, y_oracle = cpu_apply_rate(x_shape, labels, order, statics, theta, budget_s=20.0,
+                                                        max_applies=2)
     oflops = oracle_flops(x_shape, labels, order, statics)
     assert abs(flops - oflops) / oflops < 1e-12, (flops, oflops)
     del statics
+    # parity of the headline map itself: the GPU's FP64 and mixed outputs against the
+    # oracle's output for the same theta (complex128 numpy tensordot chain)
+    y64_h, ymix_h = ctx.download(y64), ctx.download(y)
+    ref_norm = float(np.linalg.norm(y_oracle))
+    fp64_vs_oracle = float(np.linalg.norm(y64_h - y_oracle) / ref_norm)
+    mixed_vs_oracle = float(np.linalg.norm(ymix_h - y_oracle) / ref_norm)
+    del y64_h, ymix_h, y_oracle
+    parity_ok = fp64_vs_oracle <= 1e-12 and mixed_vs_oracle <= 2e-5
+
+    segment = None
+    if not args.skip_extra and not args.no_dmrg_segment:
+        try:
+            segment = dmrg_segment(ctx, args.segment_steps, args.precision)
+        except Exception as exc:  # reported, never hides the headline
+            segment = {"error": f"{type(exc).__name__}: {exc}"}
 
     extra = {}
     alt = {}
@@ -485,6 +507,8 @@ def run_ours(args, rank, world):
                 extra[name] = {"error": f"{type(exc).__name__}: {exc}"}
 
     clocks = clk.summary()
+    from grafttn import _lib as GL
+    tuning = GL.tc_tune_report()
     line = {
         "metric": metric_for(args.workload), "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -496,12 +520,18 @@ def run_ours(args, rank, world):
         "fp64_gpu": {"value": fp64_rate, "unit": "applies/s", "speedup_mixed_vs_fp64": value / world / fp64_rate,
                      "samples": fp64_steps},
         "mixed_vs_fp64_rel_err": mixed_rel_err,
+        "fp64_vs_oracle_rel_err": fp64_vs_oracle,
+        "mixed_vs_oracle_rel_err": mixed_vs_oracle,
+        "parity_ok": parity_ok,
         "algorithmic_tflops": flops * value / world / 1e12,
         "kernels": kernels,
         "roofline": {"bound": "tensor", "kernel": "tc_gemm", "achieved": achieved, "peak": bf16_peak,
                      "unit": "TFLOP/s", "frac": achieved / bf16_peak, "peak_kind": f"bf16 dense burst ({peak_kind})",
+                     "achieved_definition": ("algorithmic flops of one application (8 x complex MACs of the "
+                                             "reference's env-first chain) / the tc_gemm launches' event time "
+                                             "of one application"),
+                     "tc_ms_per_apply": tc[1], "executed_macs_ratio": exec_flops / flops,
                      "executed_tensor_tflops": executed, "frac_executed": executed / bf16_peak,
-                     "achieved_definition": "8*M*N*K complex-MAC flops of the tc_gemm launches / their event time",
                      "traffic": traffic},
         "cpu_baseline": {"value": cpu_rate, "unit": "applies/s", "cores": blas_threads(), "kind": "port",
                          "sample": f"{cpu_n} eff_h2 application(s) of the same workload, {cpu_el:.1f} s"},
@@ -510,9 +540,83 @@ def run_ours(args, rank, world):
                 "path": "gtn_map_apply_host (C ABI, pinned host buffers)"},
         "gpu_launches": launches,
         "clocks": clocks,
+        "tc_tile_choices": tuning,
     }
+    if segment is not None:
+        line["dmrg_segment"] = segment
     line.update(extra)
     print(json.dumps(line), flush=True)
+    if not parity_ok:
+        sys.exit(f"parity failure: fp64 vs oracle {fp64_vs_oracle:.3e} (bound 1e-12), "
+                 f"mixed vs oracle {mixed_vs_oracle:.3e} (bound 2e-5)")
+
+
+def dmrg_segment(ctx, steps, precision, D=1024, refine_tol=1e-8):
+    """The DMRG half of the metric, bounded: `steps` consecutive two-site dmrg2 steps in the
+    middle of the dense Heisenberg chain mps_topology(63) at bond dimension D (Θ = [D,2,2,D]),
+    from one seeded random state (seed 7, bonds min(D, 2^k)), once in the mixed mode and once
+    in FP64 on the same state.  A step is the reference's local update (GroundState.jl:102-143):
+    gauge move, merge, eff_h2 build, Lanczos (krylovdim 20, tol 1e-10), truncated SVD split at
+    maxdim D.  In the mixed arm the Lanczos vector is then refined with FP64 residuals
+    (gtn_lanczos_refine) until |H v - E v| <= refine_tol * |E|, and its energy is the FP64
+    Rayleigh quotient.  The environments of the first step are built before the clock starts
+    (they are the same for both arms); environment rebuilds after each split are timed."""
+    import torch
+    import grafttn as G
+    from grafttn.contractions import EnvCache, eff_h2
+    from grafttn.networks import move_center, split_two_site, two_site_tensor
+    from grafttn.solvers import refine_local
+    L = 63
+    topo = G.mps_topology(L)
+    H = G.TTNO.from_hamiltonian(G.heisenberg(topo), ctx)
+    bond = {}
+    for c in range(topo.nnodes):
+        if topo.parent[c] >= 0:
+            below = len(topo.subtree_nodes(c, topo.parent[c]))
+            bond[c] = int(min(D, 2 ** min(below, 40), 2 ** min(L - below, 40)))
+    psi0 = G.random_ttns(np.random.default_rng(7), topo, 2, bond, ctx=ctx)
+    n0 = topo.index["site31"]
+    cache0 = EnvCache(topo)
+    move_center(psi0, n0, cache0)
+    eff_h2(cache0, psi0, H, n0, topo.parent[n0], G._lib.PREC_FP64).close()  # builds the step-1 envs
+    ctx.sync()
+    trunc = G.TruncationScheme(maxdim=D)
+    out = {"workload": f"mps63 Heisenberg (XX+YY+ZZ, Pauli), dense c128, D={D}, middle bonds site31->site32..",
+           "steps": steps, "krylovdim": 20, "lanczos_tol": 1e-10, "refine_tol_rel": refine_tol, "runs": {}}
+    for prec in (precision, "fp64"):
+        psi, cache = psi0.copy(), cache0.copy()
+        pcode = G._lib.PRECISIONS[prec]
+        n = n0
+        recs = []
+        for _ in range(steps):
+            m = topo.parent[n]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            move_center(psi, n, cache)
+            theta = two_site_tensor(psi, n, m)
+            h2 = eff_h2(cache, psi, H, n, m, pcode)
+            E, v, info = h2.lanczos_min(theta, krylovdim=20, tol=1e-10, maxiter=100)
+            rstats = {}
+            if pcode != G._lib.PREC_FP64:
+                E, v = refine_local(h2, E, v, refine_tol, stats=rstats)
+            h2.close()
+            cache.invalidate_edge(n, m)
+            split_two_site(psi, v, n, m, trunc, "m")
+            torch.cuda.synchronize()
+            recs.append({"bond": [topo.ids[n], topo.ids[m]], "s": time.perf_counter() - t0, "energy": E,
+                         "matvecs": info["matvecs"], "converged": info["converged"],
+                         "refine_fp64_matvecs": rstats.get("refine_fp64_matvecs", 0),
+                         "refine_mixed_matvecs": rstats.get("refine_mixed_matvecs", 0)})
+            n = m
+        out["runs"][prec] = {"step_s": [r["s"] for r in recs], "energies": [r["energy"] for r in recs],
+                             "matvecs": [r["matvecs"] for r in recs], "total_s": sum(r["s"] for r in recs),
+                             "refine_fp64_matvecs": [r["refine_fp64_matvecs"] for r in recs],
+                             "refine_mixed_matvecs": [r["refine_mixed_matvecs"] for r in recs]}
+    r64 = out["runs"]["fp64"]
+    rm = out["runs"][precision]
+    out["rel_energy_vs_fp64"] = [abs(a - b) / abs(b) for a, b in zip(rm["energies"], r64["energies"])]
+    out["time_ratio_fp64_over_mixed"] = r64["total_s"] / rm["total_s"]
+    return out
 
 
 def run_dmrg(args):
@@ -769,6 +873,9 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--skip-extra", action="store_true", help="only the headline workload")
     ap.add_argument("--precision", default="fp16x3", choices=sorted(DTYPES), help="mixed mode of the headline map")
+    ap.add_argument("--no-dmrg-segment", action="store_true",
+                    help="leave out the bounded D=1024 dmrg2 segment (mixed vs FP64) of the default line")
+    ap.add_argument("--segment-steps", type=int, default=1)
     ap.add_argument("--dmrg", action="store_true", help="measure DMRG sweeps instead of map applications")
     ap.add_argument("--dmrg-topology", default="mps", choices=["mps", "binary"])
     ap.add_argument("--dmrg-sites", type=int, default=63)

@@ -1,12 +1,27 @@
 // C ABI entry points: contexts, maps, one-shot contractions, permutations and vector helpers.
 #include "gtn_internal.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 
+namespace {
+// The message of the last failure on each host thread, with the context it belongs to.
+// gtn_last_error reads this copy on the thread that made the failing call, so a call
+// refused on one thread (a busy map) never races with a message written on another.
+thread_local std::string t_err;
+thread_local const void* t_err_ctx = nullptr;
+}  // namespace
+
 int set_err(gtn_ctx ctx, int code, const std::string& msg) {
-  if (ctx) ctx->err = msg;
+  if (ctx) {
+    t_err = msg;
+    t_err_ctx = ctx;
+    std::lock_guard<std::mutex> lock(ctx->err_mu);
+    ctx->err = msg;
+  }
   return code;
 }
 
@@ -116,7 +131,12 @@ int gtn_ctx_set_stream(gtn_ctx ctx, void* stream) {
 
 void* gtn_ctx_stream(gtn_ctx ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
 
-const char* gtn_last_error(gtn_ctx ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+const char* gtn_last_error(gtn_ctx ctx) {
+  if (!ctx) return "null context";
+  if (t_err_ctx == ctx) return t_err.c_str();
+  std::lock_guard<std::mutex> lock(ctx->err_mu);
+  return ctx->err.c_str();
+}
 
 int64_t gtn_ctx_launch_count(gtn_ctx ctx) { return ctx ? ctx->launches : -1; }
 
@@ -152,7 +172,8 @@ int gtn_map_create(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t*
 
 int gtn_map_destroy(gtn_map map) {
   if (!map) return GTN_ERR_INVALID;
-  if (map->busy.load() != 0) return map_busy_error(map);
+  // claim the map so that no call can start on it between this check and the free
+  if (map->busy.exchange(1) != 0) return map_busy_error(map);
   if (map->ctx) cudaStreamSynchronize(map->ctx->stream);
   map_free(map);
   delete map;
@@ -256,6 +277,140 @@ int gtn_contract(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* d
   return st;
 }
 
+// Adjoint of one operand of a contraction (the VJP behind an rrule).  For
+// y = contract(operands) and a cotangent ybar shaped like y, out = G with
+// <G, d op_slot> = <ybar, dy> for every perturbation of the operand as it enters the
+// contraction (after its conj flag), i.e.
+//   G = contract(ybar, conj(op_i) for i != slot)   with op_slot's legs as the output.
+// The label graph is rewritten: ybar takes the output legs (new positive labels), the legs
+// op_slot shared become output legs -1..-r in op_slot's leg order, every other operand's
+// conj flag flips.  Without an order the chain starts at ybar and absorbs, greedily, the
+// operand sharing the largest contracted extent with the running tensor (ties: the
+// smaller result), so that no step is an outer product while a contraction is available.
+int gtn_contract_vjp(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dims, const int* labels,
+                     const int* conj, const int* order, const void* const* operands, int slot, const void* ybar,
+                     void* out, int precision) {
+  if (!ctx || !ranks || !dims || !labels || !operands || !ybar || !out)
+    return set_err(ctx, GTN_ERR_INVALID, "contract_vjp: null argument");
+  if (n_operands < 1 || slot < 0 || slot >= n_operands)
+    return set_err(ctx, GTN_ERR_INVALID, "contract_vjp: slot outside 0..n_operands-1");
+  std::vector<int64_t> off(n_operands + 1, 0);
+  for (int i = 0; i < n_operands; ++i) {
+    if (ranks[i] < 0 || ranks[i] > 16) return set_err(ctx, GTN_ERR_INVALID, "contract_vjp: rank outside 0..16");
+    off[i + 1] = off[i] + ranks[i];
+  }
+  int maxlab = 0, nout = 0;
+  std::vector<int64_t> outdim(64, -1);
+  for (int64_t j = 0; j < off[n_operands]; ++j) {
+    const int l = labels[j];
+    if (l > 0) maxlab = std::max(maxlab, l);
+    if (l < 0) {
+      if (-l > 63) return set_err(ctx, GTN_ERR_INVALID, "contract_vjp: more than 63 output legs");
+      if (outdim[-l] >= 0) return set_err(ctx, GTN_ERR_INVALID, "contract_vjp: output label used twice");
+      outdim[-l] = dims[j];
+      nout = std::max(nout, -l);
+    }
+  }
+  for (int k = 1; k <= nout; ++k)
+    if (outdim[k] < 0) return set_err(ctx, GTN_ERR_INVALID, "contract_vjp: output labels must be -1..-R");
+  // new operands: 0 = ybar, then every operand except slot
+  std::vector<int> nr, nl, nc;
+  std::vector<int64_t> nd;
+  std::vector<const void*> np;
+  std::vector<int> src;  // original index of each new operand (-1 for ybar)
+  nr.push_back(nout);
+  for (int k = 1; k <= nout; ++k) {
+    nd.push_back(outdim[k]);
+    nl.push_back(maxlab + k);
+  }
+  nc.push_back(0);
+  np.push_back(ybar);
+  src.push_back(-1);
+  for (int i = 0; i < n_operands; ++i) {
+    if (i == slot) continue;
+    nr.push_back(ranks[i]);
+    for (int64_t j = off[i]; j < off[i + 1]; ++j) {
+      nd.push_back(dims[j]);
+      nl.push_back(labels[j] < 0 ? maxlab - labels[j] : labels[j]);
+    }
+    nc.push_back(conj && conj[i] ? 0 : 1);
+    np.push_back(operands[i]);
+    src.push_back(i);
+  }
+  // the legs op_slot shared become the result's legs -1..-r
+  for (int64_t j = off[slot]; j < off[slot + 1]; ++j) {
+    const int l = labels[j];
+    const int target = l > 0 ? l : maxlab - l;
+    int hits = 0;
+    for (size_t q = 0; q < nl.size(); ++q)
+      if (nl[q] == target) {
+        nl[q] = -(int)(j - off[slot] + 1);
+        ++hits;
+      }
+    if (hits != 1) return set_err(ctx, GTN_ERR_INVALID, "contract_vjp: a label of the slot is not shared exactly once");
+  }
+  const int nn = (int)nr.size();
+  std::vector<int64_t> noff(nn + 1, 0);
+  for (int i = 0; i < nn; ++i) noff[i + 1] = noff[i] + nr[i];
+  std::vector<int> ord;
+  if (order) {
+    ord.assign(order, order + nn);
+  } else {
+    std::vector<int> cur(nl.begin() + noff[0], nl.begin() + noff[1]);
+    std::vector<int64_t> curd(nd.begin() + noff[0], nd.begin() + noff[1]);
+    std::vector<bool> used(nn, false);
+    used[0] = true;
+    ord.push_back(0);
+    for (int step = 1; step < nn; ++step) {
+      int best = -1;
+      double best_shared = -1, best_size = 0;
+      for (int q = 1; q < nn; ++q) {
+        if (used[q]) continue;
+        double shared = 1, size = 1;
+        bool any = false;
+        for (int64_t j = noff[q]; j < noff[q + 1]; ++j) {
+          bool in_cur = false;
+          for (size_t c = 0; c < cur.size(); ++c)
+            if (nl[j] > 0 && cur[c] == nl[j]) in_cur = true;
+          if (in_cur) { shared *= (double)nd[j]; any = true; }
+          else size *= (double)nd[j];
+        }
+        for (size_t c = 0; c < cur.size(); ++c) {
+          bool in_q = false;
+          for (int64_t j = noff[q]; j < noff[q + 1]; ++j)
+            if (cur[c] > 0 && nl[j] == cur[c]) in_q = true;
+          if (!in_q) size *= (double)curd[c];
+        }
+        if (!any) shared = 0;
+        if (shared > best_shared || (shared == best_shared && size < best_size)) {
+          best = q;
+          best_shared = shared;
+          best_size = size;
+        }
+      }
+      used[best] = true;
+      ord.push_back(best);
+      std::vector<int> nxt;
+      std::vector<int64_t> nxtd;
+      for (size_t c = 0; c < cur.size(); ++c) {
+        bool in_q = false;
+        for (int64_t j = noff[best]; j < noff[best + 1]; ++j)
+          if (cur[c] > 0 && nl[j] == cur[c]) in_q = true;
+        if (!in_q) { nxt.push_back(cur[c]); nxtd.push_back(curd[c]); }
+      }
+      for (int64_t j = noff[best]; j < noff[best + 1]; ++j) {
+        bool in_cur = false;
+        for (size_t c = 0; c < cur.size(); ++c)
+          if (nl[j] > 0 && cur[c] == nl[j]) in_cur = true;
+        if (!in_cur) { nxt.push_back(nl[j]); nxtd.push_back(nd[j]); }
+      }
+      cur.swap(nxt);
+      curd.swap(nxtd);
+    }
+  }
+  return gtn_contract(ctx, nn, nr.data(), nd.data(), nl.data(), nc.data(), ord.data(), np.data(), out, precision);
+}
+
 int gtn_permute(gtn_ctx ctx, int rank, const int64_t* dims, const int* perm, const void* in, void* out) {
   if (!ctx || rank < 1 || rank > 16 || !dims || !perm || !in || !out)
     return set_err(ctx, GTN_ERR_INVALID, "gtn_permute: bad argument");
@@ -340,6 +495,27 @@ int gtn_diag_scale(gtn_ctx ctx, int64_t rows, int64_t cols, const double* d_host
                                       ctx->stream));
   ctx->launches++;
   // the host factors are pageable: the copy above is synchronous with respect to the host
+  return GTN_OK;
+}
+
+int gtn_restrict_leg(gtn_ctx ctx, int rank, const int64_t* dims, int leg, int64_t nsel, const int64_t* idx_host,
+                     const void* in, void* out) {
+  if (!ctx || !dims || !idx_host || !in || !out || rank < 1 || rank > 16 || leg < 0 || leg >= rank || nsel < 0)
+    return set_err(ctx, GTN_ERR_INVALID, "gtn_restrict_leg: bad argument");
+  int64_t A = 1, B = 1;
+  for (int i = 0; i < leg; ++i) A *= dims[i];
+  for (int i = leg + 1; i < rank; ++i) B *= dims[i];
+  for (int64_t j = 0; j < nsel; ++j)
+    if (idx_host[j] < 0 || idx_host[j] >= dims[leg])
+      return set_err(ctx, GTN_ERR_INVALID, "gtn_restrict_leg: index outside the leg");
+  if (nsel == 0 || A == 0 || B == 0) return GTN_OK;
+  void* ws = nullptr;
+  GTN_CUDA_TRY(ctx, ctx_workspace(ctx, (size_t)nsel * sizeof(int64_t) + 256, &ws));
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(ws, idx_host, nsel * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+  GTN_CUDA_TRY(ctx, launch_restrict_leg(static_cast<const double2*>(in), static_cast<double2*>(out), A, dims[leg], nsel,
+                                        B, static_cast<const int64_t*>(ws), ctx->stream));
+  ctx->launches++;
+  // the index list is pageable host memory: the copy above completes before the call returns
   return GTN_OK;
 }
 

@@ -16,16 +16,24 @@ __device__ __forceinline__ double2 cmul_conj(double2 a, double2 b) {  // conj(a)
 }
 
 // double -> float by bit manipulation on the integer pipe: mantissa truncated to 23 bits,
-// magnitudes below float's normal range flushed to signed zero, above it clamped to the
-// largest float.  The hardware F2F conversion runs at the FP64 rate on this part, which
-// would make the FP32-product kernels as slow as FP64 ones.
+// magnitudes below float's normal range flushed to signed zero, finite values above it
+// clamped to the largest float.  Inf stays Inf and NaN stays NaN (a quiet NaN), so a
+// non-finite basis entry propagates into the projections instead of being hidden.  The
+// hardware F2F conversion runs at the FP64 rate on this part, which would make the
+// FP32-product kernels as slow as FP64 ones.
 __device__ __forceinline__ float dtof_trunc(double d) {
   const unsigned hi = (unsigned)__double2hiint(d);
   const unsigned lo = (unsigned)__double2loint(d);
   const unsigned sign = hi & 0x80000000u;
-  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const unsigned ebits = (hi >> 20) & 0x7ffu;
+  const int e = (int)ebits - 1023 + 127;
   const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
-  const unsigned bits = e <= 0 ? sign : e >= 255 ? (sign | 0x7f7fffffu) : (sign | ((unsigned)e << 23) | mant);
+  const bool nonfinite = ebits == 0x7ffu;
+  const bool nan = nonfinite && (((hi & 0xfffffu) | lo) != 0u);
+  const unsigned bits = nonfinite ? (sign | 0x7f800000u | (nan ? 0x00400000u : 0u))
+                        : e <= 0  ? sign
+                        : e >= 255 ? (sign | 0x7f7fffffu)
+                                   : (sign | ((unsigned)e << 23) | mant);
   return __uint_as_float(bits);
 }
 
@@ -232,6 +240,20 @@ __global__ void fill_kernel(double2* __restrict__ x, double2 v, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     x[i] = v;
+}
+
+// out[a][j][b] = in[a][idx[j]][b]: one leg of a row-major tensor restricted to a list of
+// indices (a = outer legs, b = inner legs).
+__global__ void restrict_leg_kernel(const double2* __restrict__ in, double2* __restrict__ out, int64_t A,
+                                    int64_t Lin, int64_t nsel, int64_t B, const int64_t* __restrict__ idx) {
+  const int64_t total = A * nsel * B;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i % B;
+    const int64_t r = i / B;
+    const int64_t j = r % nsel;
+    const int64_t a = r / nsel;
+    out[i] = in[(a * Lin + idx[j]) * B + b];
+  }
 }
 
 __global__ void conj_kernel(double2* __restrict__ x, int64_t n) {
@@ -456,6 +478,14 @@ cudaError_t launch_fill_c128(double2* x, double2 v, int64_t n, cudaStream_t s) {
   fill_kernel<<<grid_for(n), 256, 0, s>>>(x, v, n);
   return cudaGetLastError();
 }
+cudaError_t launch_restrict_leg(const double2* in, double2* out, int64_t A, int64_t Lin, int64_t nsel, int64_t B,
+                                const int64_t* idx, cudaStream_t s) {
+  const int64_t total = A * nsel * B;
+  if (total <= 0) return cudaSuccess;
+  restrict_leg_kernel<<<grid_for(total), 256, 0, s>>>(in, out, A, Lin, nsel, B, idx);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_conj_inplace(double2* x, int64_t n, cudaStream_t s) {
   conj_kernel<<<grid_for(n), 256, 0, s>>>(x, n);
   return cudaGetLastError();

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 #include <memory>
+#include <mutex>
 
 #include "../../include/grafttn.h"
 
@@ -33,7 +34,8 @@ struct gtn_ctx_s {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  std::string err;
+  std::string err;          // last failure message (any thread), guarded by err_mu
+  std::mutex err_mu;
   int64_t launches = 0;
   int* d_errflag = nullptr;
   int sm_count = 0;
@@ -263,6 +265,9 @@ cudaError_t launch_fill_c128(double2* x, double2 v, int64_t n, cudaStream_t s);
 // x[i] = (u, v), u and v uniform in [-1, 1), a fixed function of (seed, i).
 cudaError_t launch_fill_uniform_c128(double2* x, int64_t n, uint64_t seed, cudaStream_t s);
 cudaError_t launch_conj_inplace(double2* x, int64_t n, cudaStream_t s);
+// out[a][j][b] = in[a][idx[j]][b] for j < nsel (idx: device int64, entries < Lin)
+cudaError_t launch_restrict_leg(const double2* in, double2* out, int64_t A, int64_t Lin, int64_t nsel, int64_t B,
+                                const int64_t* idx, cudaStream_t s);
 cudaError_t launch_transpose_c128(const double2* in, int64_t rows, int64_t cols, double2* out,
                                   cudaStream_t s);  // out[c][r] = in[r][c]
 cudaError_t launch_zero_lower(double2* R, int64_t rows, int64_t cols, cudaStream_t s);

@@ -391,6 +391,121 @@ extern "C" int gtn_lanczos_min(gtn_map map, void* xv, int krylovdim, double tol,
   return converged ? GTN_OK : set_err(ctx, GTN_ERR_NOT_CONVERGED, "Lanczos reached maxiter");
 }
 
+// Iterative refinement of an approximate lowest eigenvector in FP64 accuracy, with the
+// bulk of the work on the map's (mixed-precision) arithmetic.  Each outer step:
+//   1. y = H v with the FP64 plan, theta = <v, y>, r = y - theta v (all FP64): the only
+//      FP64 application of the step; stop when |r| <= tol.
+//   2. A mixed-precision Lanczos basis q_1 = r / |r|, q_2, ... of the map restricted to the
+//      complement of v (every new vector orthogonalised against v and the basis).
+//   3. Rayleigh-Ritz on span(v, q_1..q_m).  The projected matrix is an arrow: T[0,0] = theta
+//      and T[0,1] = |r| come from the FP64 residual exactly (<q_j, H v> = <q_j, r> = 0 for
+//      j > 1), the q-block is the mixed tridiagonal.  v <- the lowest Ritz vector.
+// The mixed error E (|E| ~ 2e-5 |H|) enters only through the q-block, which acts on the
+// correction: each step shrinks the error of v by about |E| / gap, against a floor of
+// |E| / gap for the mixed solve alone.  The returned energy is the FP64 Rayleigh quotient
+// of the returned vector.  This is the classical defect-correction scheme for eigenpairs
+// (residual in high precision, correction in low precision; Dongarra, Moler and Wilkinson,
+// SIAM J. Numer. Anal. 20 (1983)) with a Davidson-style projected correction.
+extern "C" int gtn_lanczos_refine(gtn_map map, void* xv, int inner_dim, double tol, int max_outer, double* energy,
+                                  int* info, double* resid) {
+  if (!map || !xv || !energy) return GTN_ERR_INVALID;
+  MapUse use(map);
+  if (!use.ok) return map_busy_error(map);
+  if (inner_dim < 1 || max_outer < 0) return set_err(map->ctx, GTN_ERR_INVALID, "inner_dim >= 1, max_outer >= 0");
+  Krylov K;
+  const int kd = (int)std::min<int64_t>(inner_dim + 1, std::max<int64_t>(map->x_elems, 1));
+  int st = krylov_setup(map, std::min(kd, kMaxKrylov), &K);
+  if (st != GTN_OK) return st;
+  gtn_ctx ctx = K.ctx;
+  cudaStream_t s = ctx->stream;
+  double2* x = static_cast<double2*>(xv);
+  const int m_max = std::min(kd, kMaxKrylov);
+  int mixed_mv = 0, fp64_mv = 0, outer = 0;
+  // V[0] = v (normalised)
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(K.V, x, K.n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  double nrm;
+  st = normalize(K, K.V, &nrm);
+  if (st != GTN_OK) return st;
+  if (nrm == 0) return set_err(ctx, GTN_ERR_INVALID, "zero start vector");
+  double theta = 0.0, rnorm = 0.0;
+  bool converged = false;
+  std::vector<double> a, b, sarr, w, Q;
+  for (;;) {
+    // FP64 residual of v: y in V[1], r = y - theta v in V[1]
+    double2* v = K.V;
+    double2* r = K.V + K.n;
+    st = map_run(map, GTN_PREC_FP64, v, r);
+    if (st != GTN_OK) return st;
+    fp64_mv++;
+    GTN_CUDA_TRY(ctx, launch_multidot(v, 0, 1, r, K.n, K.coef + 130, K.part, K.nblk, s, K.part_cap));
+    ctx->launches += 2;
+    double2 h;
+    st = fetch(K, K.coef + 130, 1, &h);
+    if (st != GTN_OK) return st;
+    theta = h.x;
+    GTN_CUDA_TRY(ctx, launch_axpby(K.n, make_double2(-theta, 0.0), v, make_double2(1.0, 0.0), r, s));
+    ctx->launches++;
+    // |r| may be far below |H|: remove the rounding-level component along v explicitly (two
+    // passes) so that q_1 is orthogonal to v to working accuracy
+    for (int pass = 0; pass < 2; ++pass) {
+      GTN_CUDA_TRY(ctx, launch_multidot(v, 0, 1, r, K.n, K.coef, K.part, K.nblk, s, K.part_cap));
+      GTN_CUDA_TRY(ctx, launch_lincomb(r, make_double2(1.0, 0.0), v, K.n, 1, K.coef, make_double2(-1.0, 0.0), K.n, s));
+      ctx->launches += multidot_launch_count(1) + 1;
+    }
+    st = normalize(K, r, &rnorm);  // q_1 = r / |r|
+    if (st != GTN_OK) return st;
+    if (rnorm <= tol || rnorm == 0.0) {
+      converged = true;
+      break;
+    }
+    if (outer >= max_outer || m_max < 2) break;
+    ++outer;
+    // mixed Lanczos on the complement of v, from q_1; stop once the lowest Ritz pair of the
+    // arrow matrix has a residual below 1 % of |r| (or the tolerance)
+    a.assign(m_max, 0.0);
+    b.assign(m_max, 0.0);
+    sarr.assign(1, rnorm);
+    int m = 0;
+    bool brk = false;
+    auto stop = [&](int mm, const std::vector<double>& aa, const std::vector<double>& bb) {
+      if (mm < 3) return false;
+      std::vector<double> a2(aa), ww, QQ;
+      a2[0] = theta;
+      projected_eig(mm, 1, a2, bb, sarr, ww, QQ);
+      const double rin = std::fabs(bb[mm - 1] * QQ[(size_t)(mm - 1) * mm + 0]);
+      return rin <= std::max(tol, 1e-2 * rnorm);
+    };
+    int mv = 0;
+    st = lanczos_expand(K, 1, m_max, map->precision, a, b, &m, &mv, &brk, stop);
+    if (st != GTN_OK) return st;
+    mixed_mv += mv;
+    a[0] = theta;
+    projected_eig(m, 1, a, b, sarr, w, Q);
+    // v <- sum_i Q[i, 0] V_i, normalised (into x, then back to V[0])
+    std::vector<double2> c(m);
+    for (int i = 0; i < m; ++i) c[i] = make_double2(Q[(size_t)i * m + 0], 0.0);
+    st = push(K, c, K.coef + 192);
+    if (st != GTN_OK) return st;
+    GTN_CUDA_TRY(ctx, launch_lincomb(x, make_double2(0.0, 0.0), K.V, K.n, m, K.coef + 192, make_double2(1.0, 0.0), K.n, s));
+    ctx->launches++;
+    st = normalize(K, x, &nrm);
+    if (st != GTN_OK) return st;
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(K.V, x, K.n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  }
+  // the returned vector is V[0] (normalised); its FP64 Rayleigh quotient is theta
+  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(x, K.V, K.n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  *energy = theta;
+  if (info) {
+    info[0] = outer;
+    info[1] = mixed_mv;
+    info[2] = fp64_mv;
+    info[3] = converged ? 1 : 0;
+  }
+  if (resid) *resid = rnorm;
+  return converged ? GTN_OK : set_err(ctx, GTN_ERR_NOT_CONVERGED, "refinement reached max_outer");
+}
+
 extern "C" int gtn_expm_apply(gtn_map map, double dz_re, double dz_im, void* xv, int krylovdim, double tol,
                               int* info) {
   if (!map || !xv) return GTN_ERR_INVALID;

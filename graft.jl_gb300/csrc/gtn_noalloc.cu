@@ -18,7 +18,11 @@
 //    to be cleared between calls; the array keeps the last call's partials.
 //  * The first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (and reads the SM count) with that device current; make that
-//    first call before any stream capture.
+//    first call before any stream capture.  The resolved address is cached per device for
+//    the life of the process: it does not survive cudaDeviceReset.
+//  * An error left pending on the calling thread by earlier, unrelated CUDA work is not
+//    consumed: the call then returns GTN_ERR_CUDA without launching, and the caller's own
+//    cudaGetLastError still reports that error.
 #include "gtn_internal.h"
 
 #include <algorithm>
@@ -46,6 +50,8 @@ extern "C" int gtn_multidot_noalloc(void* stream, int64_t n, int J, const void* 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return GTN_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return GTN_ERR_UNSUPPORTED;
+  // Do not launch over (and then swallow) an error that the caller's own work left pending.
+  if (cudaPeekAtLastError() != cudaSuccess) return GTN_ERR_CUDA;
   double2* scratch = nullptr;
   int nblk = 0;
   {

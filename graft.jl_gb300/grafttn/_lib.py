@@ -65,8 +65,10 @@ SIGNATURES = {
     "gtn_blockmap_info": (_i, [_p, _pd, _pi, _pi64]),
     "gtn_blockmap_destroy": (_i, [_p]),
     "gtn_contract": (_i, [_p, _i, _pi, _pi64, _pi, _pi, _pi, C.POINTER(_p), _p, _i]),
+    "gtn_contract_vjp": (_i, [_p, _i, _pi, _pi64, _pi, _pi, _pi, C.POINTER(_p), _i, _p, _p, _i]),
     "gtn_permute": (_i, [_p, _i, _pi64, _pi, _p, _p]),
     "gtn_lanczos_min": (_i, [_p, _p, _i, _d, _i, _i, _pd, _pi, _pd]),
+    "gtn_lanczos_refine": (_i, [_p, _p, _i, _d, _i, _pd, _pi, _pd]),
     "gtn_expm_apply": (_i, [_p, _d, _d, _p, _i, _d, _pi]),
     "gtn_expm_apply_arnoldi": (_i, [_p, _d, _d, _p, _i, _d, _pi]),
     "gtn_expm_small": (_i, [_i, _pd, _pd]),
@@ -76,9 +78,46 @@ SIGNATURES = {
     "gtn_axpby": (_i, [_p, _i64, _d, _d, _p, _d, _d, _p]),
     "gtn_diag_scale": (_i, [_p, _i64, _i64, _pd, _i, _p]),
     "gtn_copy2d": (_i, [_p, _i64, _i64, _p, _i64, _p, _i64]),
+    "gtn_restrict_leg": (_i, [_p, _i, _pi64, _i, _i64, _pi64, _p, _p]),
     "gtn_multidot_noalloc": (_i, [_p, _i64, _i, _p, _i64, _p, _p]),
     "gtn_selftest_wait": (_i, [_p, _i64]),
+    "gtn_tc_tuning": (_i, [_i, _i]),
+    "gtn_tensor_create": (_i, [_p, _i, _pi64, C.POINTER(_p)]),
+    "gtn_tensor_wrap": (_i, [_p, _i, _pi64, _p, C.POINTER(_p)]),
+    "gtn_tensor_destroy": (_i, [_p]),
+    "gtn_tensor_data": (_p, [_p]),
+    "gtn_tensor_shape": (_i, [_p, _pi, _pi64]),
+    "gtn_tensor_upload": (_i, [_p, _p, _i64]),
+    "gtn_tensor_download": (_i, [_p, _p, _i64]),
+    "gtn_site_labels": (_i, [_p, _i, _pi, _pi, _pi, _pi]),
+    "gtn_map_create_kind": (_i, [_p, _p, _i, C.POINTER(_p), _i, C.POINTER(_p)]),
+    "gtn_env_build": (_i, [_p, _p, _p, _p, _i, C.POINTER(_p), _p, _i]),
+    "gtn_tc_tune_report": (_i, [C.c_char_p, _i64, _pi64]),
 }
+
+MAP_H1, MAP_H2, MAP_H0, MAP_ENV = 1, 2, 3, 4
+
+
+class SiteDesc(C.Structure):
+    """gtn_site_desc: a node's (or edge's) local structure for the kind-based calls."""
+    _fields_ = [("kind", C.c_int), ("n_children", C.c_int), ("n_is_root", C.c_int), ("m_children", C.c_int),
+                ("slot", C.c_int), ("m_is_root", C.c_int)]
+
+
+def site_labels(desc):
+    """(labels per operand, order) of a site description, from the library (no device)."""
+    n = C.c_int()
+    cap = 512
+    ranks, labs, order = (C.c_int * 64)(), (C.c_int * cap)(), (C.c_int * 64)()
+    check(lib().gtn_site_labels(C.byref(desc), cap, C.byref(n), ranks, labs, order))
+    out, o = [], 0
+    for i in range(n.value):
+        out.append([labs[o + j] for j in range(ranks[i])])
+        o += ranks[i]
+    return out, [order[i] for i in range(n.value)]
+
+
+TC_VARIANTS = {"ps32": 0, "ps64": 1, "ps128": 2, "ps128x2": 3, "ps256": 4, "pair256": 5, "persist128": 6}
 
 
 class GraftError(RuntimeError):
@@ -171,3 +210,33 @@ class BlockGather(C.Structure):
 class BlockGemm(C.Structure):
     _fields_ = [("b_index", C.c_int32), ("c_buf", C.c_int32), ("c_off", C.c_int64), ("M", C.c_int64),
                 ("N", C.c_int64), ("K", C.c_int64)]
+
+
+def tc_tuning(mode=-1, clear=False):
+    """Tile-shape selection of the tensor-core steps: 'ladder' (fixed rule), 'measured'
+    (default: the first launch of each problem class times every candidate and caches the
+    fastest) or a variant name of TC_VARIANTS to force it; None keeps the mode.  clear
+    forgets the cached choices.  Returns the previous mode as an int."""
+    if mode is None or mode == -1:
+        code = -1
+    elif mode == "ladder":
+        code = 0
+    elif mode == "measured":
+        code = 1
+    elif isinstance(mode, str):
+        code = 2 + TC_VARIANTS[mode]
+    else:
+        code = int(mode)
+    old = lib().gtn_tc_tuning(code, 1 if clear else 0)
+    if old < 0:
+        raise ValueError(f"tc_tuning: bad mode {mode!r}")
+    return old
+
+
+def tc_tune_report():
+    """The cached tile-shape choices, one text line per problem class."""
+    need = C.c_int64()
+    lib().gtn_tc_tune_report(None, 0, C.byref(need))
+    buf = C.create_string_buffer(int(need.value) + 64)
+    check(lib().gtn_tc_tune_report(buf, len(buf), C.byref(need)))
+    return [l for l in buf.value.decode().split("\n") if l]

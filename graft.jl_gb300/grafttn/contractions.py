@@ -247,6 +247,31 @@ def choose_order(shapes, labels, order):
 class EffectiveMap:
     """Callable y = H_eff x backed by a compiled libgrafttn plan (types.jl:410-445)."""
 
+    @classmethod
+    def from_kind(cls, ctx: Context, desc, statics, precision=_lib.PREC_FP64):
+        """The map of a site description (gtn_map_create_kind: the library writes the label
+        graph); statics as gtn_map_create_kind lists them, as device tensors."""
+        from .device import TensorHandle
+        prec = _lib.PRECISIONS.get(precision, precision) if isinstance(precision, str) else precision
+        hs = [TensorHandle(ctx, s) for s in statics]
+        arr = (C.c_void_p * max(1, len(hs)))(*[h.h for h in hs])
+        h = C.c_void_p()
+        check(ctx.lib.gtn_map_create_kind(ctx.h, C.byref(desc), len(hs), arr, prec, C.byref(h)), ctx.h,
+              "map_create_kind")
+        self = cls.__new__(cls)
+        self.ctx, self.h, self.precision = ctx, h, prec
+        self._statics, self.labels, self.order = list(statics), None, None
+        rank = C.c_int()
+        odims = (C.c_int64 * 32)()
+        check(ctx.lib.gtn_map_out_shape(self.h, C.byref(rank), odims), ctx.h, "map_out_shape")
+        self.y_shape = tuple(odims[i] for i in range(rank.value))
+        self.x_shape = self.y_shape
+        xe, ye, fl, ns, by = C.c_int64(), C.c_int64(), C.c_double(), C.c_int(), C.c_int64()
+        check(ctx.lib.gtn_map_info(self.h, C.byref(xe), C.byref(ye), C.byref(fl), C.byref(ns), C.byref(by)),
+              ctx.h, "map_info")
+        self.flops, self.n_steps, self.bytes = fl.value, ns.value, by.value
+        return self
+
     def __init__(self, ctx: Context, x_shape, labels, order, statics, precision=_lib.PREC_FP64):
         self.ctx = ctx
         self.x_shape = tuple(int(s) for s in x_shape)
@@ -255,7 +280,9 @@ class EffectiveMap:
         dims = list(self.x_shape) + [int(d) for s in statics for d in s.shape]
         labs = [int(l) for lab in labels for l in lab]
         h = C.c_void_p()
-        self._statics = statics  # keep alive until the packing kernels ran
+        self._statics = statics  # keep alive until the packing kernels ran (and for vjp)
+        self.labels = [list(l) for l in labels]
+        self.order = list(order)
         st = ctx.lib.gtn_map_create(ctx.h, len(ranks), int_array(ranks), i64_array(dims), int_array(labs),
                                     int_array([0] * len(ranks)), int_array(order),
                                     ptr_array([0] + [s.data_ptr() for s in statics]), self.precision,
@@ -327,6 +354,26 @@ class EffectiveMap:
             check(st, self.ctx.h, "lanczos")
         return E.value, x, dict(restarts=info[0], matvecs=info[1], converged=bool(info[2]), resid=res.value)
 
+    def vjp(self, x, ybar, slot):
+        """Adjoint of operand `slot` (0 = x, 1.. = statics) of y = H_eff x at this x: the
+        tensor G with <G, d op_slot> = <ybar, dy> (gtn_contract_vjp), in FP64."""
+        return self.ctx.contract_vjp([x.contiguous()] + list(self._statics), self.labels, ybar.contiguous(), slot)
+
+    def refine(self, x0, tol=1e-8, max_outer=6, inner_dim=20):
+        """FP64 iterative refinement of an approximate lowest eigenvector (gtn_lanczos_refine):
+        FP64 residuals, corrections from mixed-precision Lanczos bases.  Returns (E, x, info)
+        with E the FP64 Rayleigh quotient of the returned x; x0 untouched."""
+        x = self.ctx.copy(x0)
+        E = C.c_double()
+        info = (C.c_int * 4)()
+        res = C.c_double()
+        st = self.ctx.lib.gtn_lanczos_refine(self.h, C.c_void_p(x.data_ptr()), inner_dim, tol, max_outer,
+                                             C.byref(E), info, C.byref(res))
+        if st not in (_lib.GTN_OK, _lib.GTN_ERR_NOT_CONVERGED):
+            check(st, self.ctx.h, "lanczos_refine")
+        return E.value, x, dict(corrections=info[0], mixed_matvecs=info[1], fp64_matvecs=info[2],
+                                converged=bool(info[3]), resid=res.value)
+
     def exponentiate(self, dz, x0, krylovdim=30, tol=1e-12, hermitian=True):
         """exp(dz H) x0 (evolution_exponentiate_backend, Evolution.jl:54-68): Lanczos for a
         Hermitian map, Arnoldi otherwise (KrylovKit's exponentiate with ishermitian, as the
@@ -394,6 +441,14 @@ class EnvCache:
         self.bytes = 0
         self.builds = 0
         self.evictions = 0
+
+    def copy(self):
+        """A cache holding the same environments (the device tensors are shared: an
+        environment is never modified in place, only dropped and rebuilt)."""
+        c = EnvCache(self.topo, self.max_env_bytes)
+        c.envs.update(self.envs)
+        c.bytes = self.bytes
+        return c
 
     def _drop(self, key):
         E = self.envs.pop(key)

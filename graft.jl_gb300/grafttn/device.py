@@ -102,6 +102,57 @@ class Context:
         check(st, self.h, f"contract {[tuple(t.shape) for t in operands]} labels {labels} order {order}")
         return out
 
+    def contract_vjp(self, operands, labels, ybar, slot, conj=None, order=None, precision=_lib.PREC_FP64):
+        """Adjoint of operand `slot` of contract(operands, labels, conj): the tensor G shaped
+        like operands[slot] with <G, d op_slot> = <ybar, d y> (gtn_contract_vjp)."""
+        n = len(operands)
+        conj = conj or [False] * n
+        ranks = [t.dim() for t in operands]
+        dims = [int(s) for t in operands for s in t.shape]
+        labs = [int(l) for lab in labels for l in lab]
+        for t in list(operands) + [ybar]:
+            if not t.is_contiguous() or t.dtype != CDT:
+                raise ValueError("operands must be contiguous complex128 device tensors")
+        out = self.empty(tuple(operands[slot].shape))
+        st = self.lib.gtn_contract_vjp(self.h, n, int_array(ranks), i64_array(dims), int_array(labs),
+                                       int_array([1 if c else 0 for c in conj]),
+                                       None if order is None else int_array(order),
+                                       ptr_array([t.data_ptr() for t in operands]), slot, C.c_void_p(ybar.data_ptr()),
+                                       C.c_void_p(out.data_ptr()), precision)
+        check(st, self.h, f"contract_vjp slot {slot} labels {labels}")
+        return out
+
+    def tensor_handle(self, t):
+        """A gtn_tensor view of the contiguous c128 device tensor t (gtn_tensor_wrap); the
+        handle keeps t referenced and is destroyed with the returned object."""
+        return TensorHandle(self, t)
+
+    def env_build(self, desc, A, W, envs, precision=_lib.PREC_FP64):
+        """env(u->v) from the site description (GTN_MAP_ENV), A_u, W_u and the other
+        neighbours' environments (gtn_env_build); returns [ket, op, bra]."""
+        hA, hW = TensorHandle(self, A), TensorHandle(self, W)
+        he = [TensorHandle(self, e) for e in envs]
+        K = desc.n_children
+        open_leg = K + 1 if desc.slot < 0 else desc.slot
+        wleg = K + 2 if desc.slot < 0 else desc.slot
+        out = self.empty((int(A.shape[open_leg]), int(W.shape[wleg]), int(A.shape[open_leg])))
+        arr = (C.c_void_p * max(1, len(he)))(*[h.h for h in he])
+        check(self.lib.gtn_env_build(self.h, C.byref(desc), hA.h, hW.h, len(he), arr, C.c_void_p(out.data_ptr()),
+                                     precision), self.h, "env_build")
+        return out
+
+    def restrict_leg(self, t, leg, idx):
+        """t with leg `leg` restricted to the indices idx (gtn_restrict_leg, on the device)."""
+        t = t.contiguous()
+        idx = [int(i) for i in idx]
+        shape = list(t.shape)
+        shape[leg] = len(idx)
+        out = self.empty(tuple(shape))
+        check(self.lib.gtn_restrict_leg(self.h, t.dim(), i64_array([int(s) for s in t.shape]), leg, len(idx),
+                                        i64_array(idx), C.c_void_p(t.data_ptr()), C.c_void_p(out.data_ptr())),
+              self.h, "restrict_leg")
+        return out
+
     def permute(self, t, perm):
         if t.dim() == 0:
             return self.copy(t)
@@ -194,3 +245,24 @@ def default_context(device=0):
             ctx = Context(device)
             _DEFAULT[(threading.get_ident(), device)] = ctx
         return ctx
+
+
+class TensorHandle:
+    """gtn_tensor view of a device tensor (no copy)."""
+
+    def __init__(self, ctx, t):
+        if not t.is_contiguous() or t.dtype != CDT:
+            raise ValueError("tensor handles need contiguous complex128 device tensors")
+        self.ctx, self.t = ctx, t
+        h = C.c_void_p()
+        check(ctx.lib.gtn_tensor_wrap(ctx.h, t.dim(), i64_array([int(x) for x in t.shape]), C.c_void_p(t.data_ptr()),
+                                      C.byref(h)), ctx.h, "tensor_wrap")
+        self.h = h
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.lib.gtn_tensor_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass

@@ -86,3 +86,22 @@ class DistributedChannelMap:
         mine = owned_slices(len(self.sliced.slices), self.rank, self.world)
         y = self.sliced.apply_slices(x, mine, self.add, self.zeros_like)
         return self.all_reduce(y)
+
+
+def device_h1_slicer(cache, psi, H, n, precision="fp64"):
+    """Channel slices of the device one-site map at node n (effective.jl:445-520): returns
+    (make_slice, channel_dim, full) where make_slice(selected) builds an EffectiveMap on the
+    device whose TTNO tensor and matching environment keep only the operator channels
+    `selected` (restricted on the device by gtn_restrict_leg), and full is the unsliced map."""
+    from .contractions import eff_h1
+    from .contractions import EffectiveMap
+    ctx, t = psi.ctx, psi.topo
+    full = eff_h1(cache, psi, H, n, precision)
+    targets, cdim = h1_channel_target(t, n, tuple(H.tensors[n].shape))
+
+    def make_slice(sel):
+        statics = list(full._statics)
+        for slot, leg in targets:
+            statics[slot] = ctx.restrict_leg(statics[slot], leg, sel)
+        return EffectiveMap(ctx, full.x_shape, full.labels, full.order, statics, full.precision)
+    return make_slice, cdim, full

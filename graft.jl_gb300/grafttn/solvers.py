@@ -16,14 +16,30 @@ from .networks import (TTNO, TTNS, TruncationScheme, absorb_on_leg, left_orth, m
                        orth_factor_leg, split_two_site, two_site_tensor)
 
 
+def refine_local(h2, E, v, refine_tol, max_outer=8, inner_dim=20, stats=None):
+    """FP64 iterative refinement of a local eigenvector of a mixed-precision map
+    (gtn_lanczos_refine): FP64 residuals, mixed-precision corrections.  The tolerance is
+    relative to the energy: |H v - E v| <= refine_tol * max(1, |E|).  Returns (E, v)."""
+    E2, v2, info = h2.refine(v, tol=refine_tol * max(1.0, abs(E)), max_outer=max_outer, inner_dim=inner_dim)
+    if stats is not None:
+        stats["refine_fp64_matvecs"] = stats.get("refine_fp64_matvecs", 0) + info["fp64_matvecs"]
+        stats["refine_mixed_matvecs"] = stats.get("refine_mixed_matvecs", 0) + info["mixed_matvecs"]
+    return E2, v2
+
+
 def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10, tol=1e-10,
           krylovdim=20, precision="fp64", rq_fp64=None, lanczos_tol=1e-12, maxiter=100,
-          verbose=False, stats=None):
+          verbose=False, stats=None, refine="off", refine_tol=1e-8):
     """Two-site DMRG; returns (psi, energies per sweep).  ``precision`` selects the map
     arithmetic.  With a mixed mode the energy that closes each sweep (the one returned and
     used for the convergence test) is the FP64 Rayleigh quotient of the last local
     eigenvector (``rq_fp64`` defaults to True for mixed modes); the other local solves keep
-    their mixed-precision Ritz values, which nothing downstream reads."""
+    their mixed-precision Ritz values, which nothing downstream reads.
+
+    ``refine`` ("off", "last" or "all"; mixed modes only) refines the local eigenvectors of
+    the sweep-closing solve or of every solve to FP64 accuracy (refine_local): the FP64
+    residual |H v - E v| is brought below refine_tol * max(1, |E|), and the energy is the
+    FP64 Rayleigh quotient of the refined vector."""
     if not H.ishermitian:
         raise ValueError("dmrg2: DMRG requires ishermitian(H) == true")
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
@@ -58,9 +74,13 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
             tt = mark("t_env_and_map", tt)
             last = step == len(sched) - 1 or (stats is not None and stats.get("max_steps") is not None
                                                and step == stats["max_steps"] - 1)
+            do_refine = prec != _lib.PREC_FP64 and (refine == "all" or (refine == "last" and last))
             E, v, info = h2.lanczos_min(theta, krylovdim=krylovdim, tol=lanczos_tol, maxiter=maxiter,
-                                        rq_fp64=rq_fp64 and last)
+                                        rq_fp64=rq_fp64 and last and not do_refine)
             tt = mark("t_lanczos", tt)
+            if do_refine:
+                E, v = refine_local(h2, E, v, refine_tol, inner_dim=krylovdim, stats=stats)
+                tt = mark("t_refine", tt)
             if stats is not None:
                 stats["matvecs"] = stats.get("matvecs", 0) + info["matvecs"]
                 stats["steps"] = stats.get("steps", 0) + 1

@@ -110,6 +110,71 @@ int gtn_map_apply_profiled(gtn_map map, int precision, const void* x, void* y, i
 /* Output leg dims of the map (rank written to *rank, dims to dims[0..rank-1]). */
 int gtn_map_out_shape(gtn_map map, int* rank, int64_t* dims);
 
+/* ---- tile shapes of the tensor-core steps ---------------------------------------------
+ * The reference chooses how to run a contraction from an analytic cost model
+ * (lib/GraftFoundation/src/Backend/Backend.jl:309-368).  Here the tensor-core steps of dense
+ * maps choose their tile shape by measurement: the first launch of a problem class (plane
+ * count, fp16 or bf16 planes, product count, ceil(log2 M), 2N in steps of 64, ceil(log2
+ * k-blocks)) outside stream capture times every candidate tile shape on that problem (one
+ * warm-up and two timed launches each, on the caller's stream; this synchronises once) and
+ * caches the fastest for the process.  Every candidate computes the same products in the
+ * same order per output element, so the choice never changes results.
+ * gtn_tc_tuning(mode, clear): mode 0 = fixed ladder, 1 = measured (default), 2 + v = force
+ * variant v (0 ps32, 1 ps64, 2 ps128, 3 ps128x2, 4 ps256, 5 pair256 = 256 x 256 tiles on an
+ * SM pair, 6 persist128 = persistent 128 x 128) where it is a candidate; mode -1 keeps the
+ * mode.  clear != 0 forgets the cached choices.  Returns the previous mode, or -1 for a mode
+ * outside -1 .. 8.  Grouped launches (block-sparse steps, batched maps) always run the
+ * persistent kernel; in the measured mode their tile width (the widest problem's ladder width
+ * or half of it) is measured per problem list the same way.
+ * gtn_tc_tune_report writes one text line per cached class (the candidates' times and the
+ * choice) into buf (cap bytes, NUL-terminated); *needed = bytes required. */
+int gtn_tc_tuning(int mode, int clear);
+int gtn_tc_tune_report(char* buf, int64_t cap, int64_t* needed);
+
+/* ---- tensor objects and maps by kind ---------------------------------------------------
+ * The reference's drop-in seams hand over TensorMaps and ask for eff_h1 / eff_h2 / eff_h0 /
+ * env updates by the node's place in the tree (lib/GraftContractions/src/Contractions/
+ * effective.jl:627-797,878-1034; envcache.jl:919-999,1010-1101).  A gtn_tensor is a dense
+ * c128 tensor on the context's device (row-major, legs as documented above): library-owned
+ * (gtn_tensor_create, then gtn_tensor_upload / gtn_tensor_download from host memory) or a
+ * view of the caller's device buffer (gtn_tensor_wrap, e.g. a CuArray; never freed here).
+ * gtn_map_create_kind builds the map from a gtn_site_desc and the statics as tensors; the
+ * label graph and env-first order are the reference's, the input's dims follow from the
+ * statics, and the root cap is supplied by the library.  Statics, in order:
+ *   GTN_MAP_H1: W_n, env(w->n) for n's children in slot order, then for n's parent (none at
+ *               the root).  Input: A_n (children..., phys, parent).
+ *   GTN_MAP_H2: W_n, W_m, env(w->n) for n's children, env(w->m) for m's children except n
+ *               in slot order, then for m's parent (none when m is the root).  Input: the
+ *               two-site block (n's children..., phys_n, m's other children..., phys_m,
+ *               m's parent).
+ *   GTN_MAP_H0: env(n->m), env(m->n).  Input: the link matrix C.
+ * gtn_env_build writes env(u->v)[ket, op, bra] for GTN_MAP_ENV (n_children, n_is_root
+ * describe u; slot = v's child slot of u, or -1 for u's parent) from A_u, W_u and the
+ * environments env(w->u) of u's other neighbours (children in slot order, then parent).
+ * gtn_site_labels returns the label graph and order of a description (no device needed). */
+typedef struct gtn_tensor_s* gtn_tensor;
+enum { GTN_MAP_H1 = 1, GTN_MAP_H2 = 2, GTN_MAP_H0 = 3, GTN_MAP_ENV = 4 };
+typedef struct {
+  int kind;        /* GTN_MAP_H1 / H2 / H0 / ENV */
+  int n_children;  /* children of n (H1, H2) or of u (ENV) */
+  int n_is_root;   /* H1: n is the root; ENV: u is the root */
+  int m_children;  /* H2: children of m, n's parent */
+  int slot;        /* H2: n's child slot in m; ENV: the open neighbour's child slot, -1 = parent */
+  int m_is_root;   /* H2: m is the root */
+} gtn_site_desc;
+int gtn_tensor_create(gtn_ctx ctx, int rank, const int64_t* dims, gtn_tensor* out);
+int gtn_tensor_wrap(gtn_ctx ctx, int rank, const int64_t* dims, void* device_data, gtn_tensor* out);
+int gtn_tensor_destroy(gtn_tensor t);
+void* gtn_tensor_data(gtn_tensor t);
+int gtn_tensor_shape(gtn_tensor t, int* rank, int64_t* dims);
+int gtn_tensor_upload(gtn_tensor t, const void* host, int64_t elems);
+int gtn_tensor_download(gtn_tensor t, void* host, int64_t elems);
+int gtn_site_labels(const gtn_site_desc* desc, int cap, int* n_operands, int* ranks, int* labels, int* order);
+int gtn_map_create_kind(gtn_ctx ctx, const gtn_site_desc* desc, int n_tensors, const gtn_tensor* tensors,
+                        int precision, gtn_map* out);
+int gtn_env_build(gtn_ctx ctx, const gtn_site_desc* desc, gtn_tensor A, gtn_tensor W, int n_envs,
+                  const gtn_tensor* envs, void* out, int precision);
+
 /* ---- batches of independent maps --------------------------------------------------
  * Replaces the reference's threaded fan-out of many small maps (channel slices,
  * lib/GraftContractions/src/Contractions/effective.jl:26-30,153-165; sibling environment
@@ -174,6 +239,22 @@ int gtn_contract(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* d
                  const int* labels, const int* conj, const int* order,
                  const void* const* operands, void* out, int precision);
 
+/* Adjoint of one operand of a contraction: the vector-Jacobian product behind an rrule of
+ * a map application or an environment update (no counterpart in the reference, which has
+ * no AD; gradient rules there would wrap eff_h1/eff_h2 maps, lib/GraftContractions/src/
+ * Contractions/effective.jl:709-797, and env updates, envcache.jl:1010-1101).  Takes the
+ * label graph and operands of the forward contraction (as gtn_contract / gtn_map_create:
+ * operand 0 first, conj flags), a cotangent ybar shaped like the output (legs -1, -2, ...)
+ * and writes to out, shaped like operand `slot`, the tensor G with
+ *     <G, d op_slot> = <ybar, dy>   (<a, b> = sum conj(a) b)
+ * for every perturbation of op_slot as it enters the contraction (after its conj flag):
+ * G = contract(ybar, conj(op_i), i != slot).  It runs through the same contraction engine
+ * (tcgen05 steps in the mixed precisions).  order (may be NULL) orders the rewritten
+ * operand list [ybar, op_i for i != slot]; NULL picks a greedy chain from ybar. */
+int gtn_contract_vjp(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dims, const int* labels,
+                     const int* conj, const int* order, const void* const* operands, int slot, const void* ybar,
+                     void* out, int precision);
+
 /* Row-major permutation of a c128 tensor: out has legs (perm[0], perm[1], ...). */
 int gtn_permute(gtn_ctx ctx, int rank, const int64_t* dims, const int* perm,
                 const void* in, void* out);
@@ -190,6 +271,19 @@ int gtn_permute(gtn_ctx ctx, int rank, const int64_t* dims, const int* perm,
  * info[0] = restarts, info[1] = matvecs, info[2] = converged flag; resid[0] = residual. */
 int gtn_lanczos_min(gtn_map map, void* x, int krylovdim, double tol, int maxiter,
                     int rq_fp64, double* energy, int* info, double* resid);
+/* Iterative refinement of an approximate lowest eigenvector (e.g. the result of
+ * gtn_lanczos_min on a mixed-precision map) to FP64 accuracy.  Each outer step applies the
+ * FP64 plan once to get the residual r = H x - theta x in FP64, builds a Lanczos basis of up
+ * to inner_dim vectors from r in the map's own (mixed) precision on the complement of x,
+ * and replaces x by the lowest Ritz vector of span(x, basis), whose coupling to x is the
+ * exact FP64 |r|.  Stops when |r| <= tol (absolute) or after max_outer corrections.
+ * x (device c128): start vector in, normalised refined vector out.  energy = FP64 Rayleigh
+ * quotient of the returned x.  info[0] = corrections, info[1] = mixed matvecs, info[2] = FP64
+ * matvecs, info[3] = converged; resid = FP64 |r| of the returned x.  The reference has no
+ * separate call: its eigsolve hook (lib/GraftGroundState/src/GroundState/GroundState.jl:
+ * 25-39) is FP64 throughout, and this call is how the mixed modes meet its accuracy. */
+int gtn_lanczos_refine(gtn_map map, void* x, int inner_dim, double tol, int max_outer, double* energy,
+                       int* info, double* resid);
 /* x <- exp((dz_re + i dz_im) H) x by a Lanczos Krylov exponential with FP64
  * orthogonalisation and sub-stepping to meet tol.  info[0] = substeps, info[1] = matvecs. */
 int gtn_expm_apply(gtn_map map, double dz_re, double dz_im, void* x, int krylovdim,
@@ -235,10 +329,21 @@ int gtn_axpby(gtn_ctx ctx, int64_t n, double a_re, double a_im, const void* x,
  * w has n elements; out (device) receives J values.  Limits: 1 <= J <= 64; partial sums
  * live in a library-owned 512 KiB __device__ array shared by all calls on a device, so
  * calls that overlap on the GPU race (order them on one stream).  The first call on each
- * device resolves that array's address; make it before any stream capture.  Returns
- * GTN_ERR_INVALID for J outside 1..64 or bad pointers / strides; never allocates. */
+ * device resolves that array's address (cached until exit; it does not survive
+ * cudaDeviceReset); make it before any stream capture.  Returns GTN_ERR_INVALID for J
+ * outside 1..64 or bad pointers / strides, and GTN_ERR_CUDA without launching when an
+ * earlier CUDA error is pending on the calling thread (left for the caller to read);
+ * never allocates. */
 int gtn_multidot_noalloc(void* stream, int64_t n, int J, const void* V, int64_t ldv, const void* w,
                          void* out);
+
+/* One leg of a row-major c128 tensor restricted to an index list (host int64, each below
+ * dims[leg]): out has the same legs with dims[leg] replaced by nsel,
+ * out[..., j, ...] = in[..., idx[j], ...].  This is the operator-channel restriction of a
+ * channel-sliced map's statics (the TTNO leg and the matching environment leg;
+ * lib/GraftContractions/src/Contractions/effective.jl:445-520), done on the device. */
+int gtn_restrict_leg(gtn_ctx ctx, int rank, const int64_t* dims, int leg, int64_t nsel, const int64_t* idx,
+                     const void* in, void* out);
 
 /* Strided 2-D copy of c128 data: dst[i*dst_ld + j] = src[i*src_ld + j] for i < rows, j < cols
  * (column concatenation of factors, e.g. the expanded isometry [Q E] of a bond expansion). */

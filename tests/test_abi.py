@@ -49,3 +49,21 @@ def test_null_handles_are_rejected_without_a_gpu():
     assert lib.gtn_map_apply(None, None, None) == _lib.GTN_ERR_INVALID
     assert lib.gtn_map_destroy(None) == _lib.GTN_ERR_INVALID
     assert lib.gtn_selftest_wait(None, 1000) == _lib.GTN_ERR_INVALID
+
+
+def test_tile_tuner_mode_switch_without_gpu():
+    # the tuner's mode and cache are host state: no device call is made
+    import __graft_entry__
+    __graft_entry__.build()
+    from grafttn import _lib
+    old = _lib.tc_tuning("ladder", clear=True)
+    try:
+        assert _lib.tc_tuning(None) == 0
+        assert _lib.tc_tuning("pair256") == 0
+        assert _lib.tc_tuning("measured") == 2 + _lib.TC_VARIANTS["pair256"]
+        assert _lib.tc_tune_report() == []
+        import pytest
+        with pytest.raises(ValueError):
+            _lib.tc_tuning(99)
+    finally:
+        _lib.tc_tuning(old)

@@ -1,5 +1,5 @@
-"""The allocation-free projection entry point (gtn_multidot_noalloc) against the regular
-gtn_dot entry point, through the C ABI.  It serves callers that cannot let the library
+"""The allocation-free projection entry point (gtn_multidot_noalloc) against numpy's
+V.conj() @ w and against the regular gtn_dot entry point, through the C ABI.  It serves callers that cannot let the library
 allocate device memory (their own pool owns the GPU's memory, or cudaMalloc's device-wide
 synchronisation is unacceptable), so it keeps its partial sums in a fixed library array.
 This file is collected last so that a failure here comes after every other test ran."""
@@ -27,8 +27,10 @@ def test_multidot_noalloc_matches_dot(ctx):
         assert st == _lib.GTN_OK
         torch.cuda.synchronize()
         got = ctx.download(out)
-        ref = np.array([ctx.dot(dV[j], dw) for j in range(J)])   # the existing entry point
         tol = 1e-12 * np.linalg.norm(V, axis=1) * np.linalg.norm(w)
+        exact = V.conj() @ w                                      # numpy, complex128
+        assert np.all(np.abs(got - exact) <= tol), (call, np.max(np.abs(got - exact)))
+        ref = np.array([ctx.dot(dV[j], dw) for j in range(J)])   # the existing entry point
         assert np.all(np.abs(got - ref) <= tol), (call, np.max(np.abs(got - ref)))
 
 
