@@ -498,6 +498,14 @@ int gtn_diag_scale(gtn_ctx ctx, int64_t rows, int64_t cols, const double* d_host
   return GTN_OK;
 }
 
+int gtn_fill(gtn_ctx ctx, int64_t n, double re, double im, void* x) {
+  if (!ctx || !x || n < 0) return set_err(ctx, GTN_ERR_INVALID, "gtn_fill: bad argument");
+  if (n == 0) return GTN_OK;
+  GTN_CUDA_TRY(ctx, launch_fill_c128(static_cast<double2*>(x), make_double2(re, im), n, ctx->stream));
+  ctx->launches++;
+  return GTN_OK;
+}
+
 int gtn_restrict_leg(gtn_ctx ctx, int rank, const int64_t* dims, int leg, int64_t nsel, const int64_t* idx_host,
                      const void* in, void* out) {
   if (!ctx || !dims || !idx_host || !in || !out || rank < 1 || rank > 16 || leg < 0 || leg >= rank || nsel < 0)

@@ -12,7 +12,7 @@
 
 namespace {
 
-bool is_tc_prec(int p) { return p == GTN_PREC_BF16X6 || p == GTN_PREC_BF16X3; }
+bool is_tc_prec(int p) { return p == GTN_PREC_BF16X6 || p == GTN_PREC_BF16X3 || p == GTN_PREC_FP16X3; }
 int planes_of(int p) { return p == GTN_PREC_BF16X6 ? 3 : 2; }
 
 void flat_groups(int64_t n, GroupSpec* mg, GroupSpec* kg, int64_t* M, int64_t* K) {
@@ -42,15 +42,14 @@ int map_run_batched(gtn_map* maps_in, int n, int precision, const double2* const
     if (m->ctx != ctx) return set_err(ctx, GTN_ERR_INVALID, "batched maps must share one context");
     maps[i] = (precision == GTN_PREC_FP64 && m->fp64_alt) ? m->fp64_alt : m;
   }
-  if (precision == GTN_PREC_FP16X3)
-    return set_err(ctx, GTN_ERR_UNSUPPORTED, "batched maps: fp16x3 planes are not implemented (use bf16x6)");
   const bool fp64 = precision == GTN_PREC_FP64;
+  const bool f16 = precision == GTN_PREC_FP16X3;
   const bool tc = is_tc_prec(precision);
   const int P = tc ? planes_of(precision) : 0;
   if (tc)
     for (gtn_map m : maps)
       for (auto& st : m->steps)
-        if (!st.small && (!st.bpl || st.bplanes != P))
+        if (!st.small && (!st.bpl || st.bplanes != P || st.bfp16 != (f16 ? 1 : 0) || (f16 && !m->amax)))
           return set_err(ctx, GTN_ERR_INVALID, "a batched map was not created for this tcgen05 precision");
   std::vector<const void*> cur(n);
   std::vector<bool> cur64(n, true);
@@ -133,6 +132,12 @@ int map_run_batched(gtn_map* maps_in, int n, int precision, const double2* const
         a.Kp = st.Kp;
         a.a_planes = P;
         a.b_planes = P;
+        if (f16) {  // fp16 planes: rows of A scaled by their maxima, complex rows of B by theirs
+          G.amax = m->amax;
+          a.fp16 = 1;
+          a.a_max = m->amax;
+          a.b_max = st.bmax;
+        }
         if (P == 3) {
           const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
           a.nprod = 6;
@@ -161,6 +166,12 @@ int map_run_batched(gtn_map* maps_in, int n, int precision, const double2* const
       e = launch_small_grouped(small.data(), (int)small.size(), fp64 ? 1 : 0, s);
       ctx->launches += (int64_t)((small.size() + kGatherJobMax - 1) / kGatherJobMax);
     }
+    if (f16)
+      for (int t = 0; t < 2 && e == cudaSuccess; ++t)
+        if (!gath[t].empty()) {
+          e = launch_rowmax_grouped(gath[t].data(), (int)gath[t].size(), t, s);
+          ctx->launches += (int64_t)((gath[t].size() + kGatherJobMax - 1) / kGatherJobMax);
+        }
     for (int t = 0; t < 2 && e == cudaSuccess; ++t)
       if (!gath[t].empty()) {
         e = launch_gather_grouped(gath[t].data(), (int)gath[t].size(), t, fp64 ? 1 : 0, s);

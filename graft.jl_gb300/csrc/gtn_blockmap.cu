@@ -52,6 +52,7 @@ struct gtn_blockmap_s {
   cudaGraphExec_t exec = nullptr;
   bool use_graph = false;
   int64_t launches_per_run = 0;
+  gtn_map proxy = nullptr;       // Krylov operator view (basis storage lives there)
 };
 
 namespace {
@@ -163,6 +164,11 @@ int run(gtn_blockmap bm, const double2* x, double2* y) {
 }
 
 void bm_free(gtn_blockmap bm) {
+  if (bm->proxy) {
+    map_free(bm->proxy);
+    delete bm->proxy;
+    bm->proxy = nullptr;
+  }
   if (bm->exec) cudaGraphExecDestroy(bm->exec);
   if (bm->graph) cudaGraphDestroy(bm->graph);
   for (void* p : bm->owned) cudaFree(p);
@@ -171,7 +177,54 @@ void bm_free(gtn_blockmap bm) {
 
 }  // namespace
 
+int blockmap_run(gtn_blockmap bm, const double2* x, double2* y) { return run(bm, x, y); }
+int blockmap_precision(gtn_blockmap bm) { return bm->precision; }
+
+namespace {
+// The Krylov operator view of a block map (created once, kept with the map).
+int proxy_of(gtn_blockmap bm, gtn_blockmap bm64, gtn_map* out) {
+  gtn_ctx ctx = bm->ctx;
+  if (bm64 && (bm64->ctx != ctx || bm64->x_elems != bm->x_elems || bm64->y_elems != bm->y_elems ||
+               bm64->precision != GTN_PREC_FP64))
+    return set_err(ctx, GTN_ERR_INVALID, "the FP64 block map must be an FP64 map of the same shape and context");
+  if (bm->x_elems != bm->y_elems) return set_err(ctx, GTN_ERR_SHAPE, "Krylov solvers need a square map");
+  if (!bm->proxy) {
+    gtn_map m = new (std::nothrow) gtn_map_s();
+    if (!m) return set_err(ctx, GTN_ERR_MEMORY, "host allocation failed");
+    m->ctx = ctx;
+    m->precision = bm->precision;
+    m->x_elems = bm->x_elems;
+    m->y_elems = bm->y_elems;
+    m->bm = bm;
+    bm->proxy = m;
+  }
+  bm->proxy->bm64 = bm64;
+  *out = bm->proxy;
+  return GTN_OK;
+}
+}  // namespace
+
 extern "C" {
+
+int gtn_blockmap_lanczos_min(gtn_blockmap bm, gtn_blockmap bm64, void* x, int krylovdim, double tol, int maxiter,
+                             int rq_fp64, double* energy, int* info, double* resid) {
+  if (!bm) return GTN_ERR_INVALID;
+  gtn_map m = nullptr;
+  const int st = proxy_of(bm, bm64, &m);
+  if (st != GTN_OK) return st;
+  return gtn_lanczos_min(m, x, krylovdim, tol, maxiter, rq_fp64, energy, info, resid);
+}
+
+int gtn_blockmap_lanczos_refine(gtn_blockmap bm, gtn_blockmap bm64, void* x, int inner_dim, double tol, int max_outer,
+                                double* energy, int* info, double* resid) {
+  if (!bm) return GTN_ERR_INVALID;
+  if (!bm64 && bm->precision != GTN_PREC_FP64)
+    return set_err(bm->ctx, GTN_ERR_INVALID, "refinement needs the FP64 block map");
+  gtn_map m = nullptr;
+  const int st = proxy_of(bm, bm64, &m);
+  if (st != GTN_OK) return st;
+  return gtn_lanczos_refine(m, x, inner_dim, tol, max_outer, energy, info, resid);
+}
 
 int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const int* step_ngemm,
                         const gtn_block_gather* gathers, const gtn_block_gemm* gemms, int nfinal,

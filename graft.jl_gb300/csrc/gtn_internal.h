@@ -129,6 +129,7 @@ struct GatherJob {
   int64_t ld;        // complex output: row pitch
   int64_t pstride;   // split output: plane pitch (bf16 elements)
   int nplanes;       // 0: complex output, 2 or 3: bf16 slice planes (row pitch 2*Kw)
+  const float* amax = nullptr;  // with nplanes == 2: fp16 planes scaled by these row maxima
 };
 struct SmallJob {
   const void* A;
@@ -139,6 +140,8 @@ struct SmallJob {
   void* C;
 };
 cudaError_t launch_gather_grouped(const GatherJob* jobs, int njobs, int in_is64, int out_is64, cudaStream_t s);
+// Row maxima of the jobs that carry amax (zeroed first), for their fp16 splits.
+cudaError_t launch_rowmax_grouped(const GatherJob* jobs, int njobs, int in_is64, cudaStream_t s);
 // Device-resident gather jobs (block-sparse maps): buffers resolved per launch.
 struct BlockBases {
   void* buf[6];  // 0 x, 1 y, 2/3 running buffers, 4 staging, 5 fp16 row maxima
@@ -340,6 +343,10 @@ struct gtn_map_s {
   void* dx = nullptr; void* dy = nullptr;     // staging for the host-buffer entry point
   int64_t bytes = 0;
   std::vector<void*> owned;
+  // a Krylov operator backed by block-sparse maps instead of a plan (gtn_blockmap_lanczos_*):
+  // applications go to bm (its own precision) or, in FP64, to bm64
+  struct gtn_blockmap_s* bm = nullptr;
+  struct gtn_blockmap_s* bm64 = nullptr;
   // Krylov scratch
   double2* kv = nullptr; int kv_cap = 0;     // (krylovdim+1) vectors
   double2* kcoef = nullptr; double2* kscratch = nullptr; int kscratch_cap = 0;
@@ -349,6 +356,9 @@ int plan_build(gtn_ctx ctx, int n_operands, const int* ranks, const int64_t* dim
                const int* labels, const int* conj, const int* order, const void* const* statics,
                int precision, gtn_map map, bool allow_group = true, bool alloc_ws = true);
 int map_run(gtn_map map, int precision, const double2* x, double2* y);
+// One eager application of a block-sparse map (no graph), in its own precision.
+int blockmap_run(struct gtn_blockmap_s* bm, const double2* x, double2* y);
+int blockmap_precision(struct gtn_blockmap_s* bm);
 int map_run_profiled(gtn_map map, int precision, const double2* x, double2* y, int cap, double* ms,
                      int* kind, double* flops, int* count);
 void map_free(gtn_map map);

@@ -12,6 +12,7 @@
 // h2_spec / env_spec (checked label by label by the CPU tests).
 #include "gtn_internal.h"
 
+#include <algorithm>
 #include <new>
 
 struct gtn_tensor_s {
@@ -294,6 +295,23 @@ int spec_dims(const Spec& s, int kind, const std::vector<const gtn_tensor_s*>& g
   return GTN_OK;
 }
 
+// Column-major operands (TensorKit/Julia arrays): an array with legs (l1..lN), first leg
+// fastest, is the row-major tensor with legs (lN..l1).  Reverse every operand's labels and
+// dims, and renumber the output legs -k -> -(R + 1 - k) so that the output comes out
+// column-major in the reference's leg order too.
+void to_row_major(std::vector<int>& ranks, std::vector<int>& labels, std::vector<int64_t>& dims) {
+  int R = 0;
+  for (int l : labels) R = std::max(R, -l);
+  size_t off = 0;
+  for (int r : ranks) {
+    std::reverse(labels.begin() + off, labels.begin() + off + r);
+    std::reverse(dims.begin() + off, dims.begin() + off + r);
+    off += r;
+  }
+  for (int& l : labels)
+    if (l < 0) l = -(R + 1 + l);
+}
+
 }  // namespace
 
 extern "C" {
@@ -418,6 +436,7 @@ int gtn_map_create_kind(gtn_ctx ctx, const gtn_site_desc* desc, int n_tensors, c
     ranks.push_back((int)l.size());
     for (int v : l) labels.push_back(v);
   }
+  if (desc->col_major) to_row_major(ranks, labels, dims);
   std::vector<const void*> ptrs(nops, nullptr);
   void* capbuf = nullptr;
   for (int i = 1, gi = 0; i < nops; ++i) {
@@ -463,6 +482,7 @@ int gtn_env_build(gtn_ctx ctx, const gtn_site_desc* desc, gtn_tensor A, gtn_tens
     ranks.push_back((int)l.size());
     for (int v : l) labels.push_back(v);
   }
+  if (desc->col_major) to_row_major(ranks, labels, dims);
   std::vector<const void*> ptrs(nops, nullptr);
   void* capbuf = nullptr;
   int gi = 0;

@@ -287,8 +287,8 @@ struct Split16Writer {
 // amax[m] = max over k of max(|re|, |im|) of the K-major gather (atomic max of the
 // non-negative float bits; amax zeroed before the launch).
 template <typename Tin, class Off, int TM, int TK>
-__global__ void __launch_bounds__(256) rowmax_kernel(const Tin* __restrict__ T, Off off, int64_t M, int64_t K,
-                                                     int m_fast, float* __restrict__ amax) {
+__device__ __forceinline__ void rowmax_tile(const Tin* __restrict__ T, const Off& off, int64_t M, int64_t K, int m_fast,
+                                            float* __restrict__ amax, int64_t m0, int64_t k0) {
   // TM x TK = 2048 elements per tile (8 loads in flight per thread); 256 x 8 when the rows
   // are the unit-stride index (long contiguous runs per k), else 64 x 32
   static_assert(TM * TK == 2048 && TK <= 32, "tile shape");
@@ -296,7 +296,6 @@ __global__ void __launch_bounds__(256) rowmax_kernel(const Tin* __restrict__ T, 
   __shared__ int64_t offK[TK];
   __shared__ float tile[TM][TK + 1];
   const int tid = threadIdx.x + 32 * threadIdx.y;
-  const int64_t m0 = (int64_t)blockIdx.x * TM, k0 = (int64_t)blockIdx.y * TK;
   for (int i = tid; i < TM + TK; i += 256) {
     if (i < TM)
       offM[i] = m0 + i < M ? off.m(m0 + i) : 0;
@@ -330,6 +329,12 @@ __global__ void __launch_bounds__(256) rowmax_kernel(const Tin* __restrict__ T, 
     for (int o = TK / 2; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
     if (c == 0 && m0 + r < M && x > 0.f) atomicMax(reinterpret_cast<unsigned int*>(amax) + m0 + r, __float_as_uint(x));
   }
+}
+
+template <typename Tin, class Off, int TM, int TK>
+__global__ void __launch_bounds__(256) rowmax_kernel(const Tin* __restrict__ T, Off off, int64_t M, int64_t K,
+                                                     int m_fast, float* __restrict__ amax) {
+  rowmax_tile<Tin, Off, TM, TK>(T, off, M, K, m_fast, amax, (int64_t)blockIdx.x * TM, (int64_t)blockIdx.y * TK);
 }
 
 // bmax[n] = max over k of max(|re|, |im|) of B[n][:], one CTA per row
@@ -460,7 +465,11 @@ __global__ void __launch_bounds__(256) gather_grouped_kernel(const __grid_consta
   const int t = b - g.tile_start[p];
   const int64_t m0 = (int64_t)(t % g.tiles_m[p]) * 32, k0 = (int64_t)(t / g.tiles_m[p]) * 32;
   __shared__ Smem32<Tin> sm;
-  if (J.nplanes > 0) {
+  if (J.nplanes > 0 && J.amax) {
+    Split16Writer w{static_cast<__half*>(J.out), 2 * (J.ld > 0 ? J.ld : J.Kw), J.pstride, J.amax};
+    gather_tile<Tin, Split16Writer>(static_cast<const Tin*>(J.T), J.mg, J.kg, J.M, J.K, J.Kw, g.m_fast[p], w, m0, k0,
+                                    sm);
+  } else if (J.nplanes > 0) {
     SplitWriter w{static_cast<__nv_bfloat16*>(J.out), 2 * (J.ld > 0 ? J.ld : J.Kw), J.pstride, J.nplanes};
     gather_tile<Tin, SplitWriter>(static_cast<const Tin*>(J.T), J.mg, J.kg, J.M, J.K, J.Kw, g.m_fast[p], w, m0, k0,
                                   sm);
@@ -705,6 +714,54 @@ cudaError_t launch_gather_grouped(const GatherJob* jobs, int njobs, int in_is64,
   if (in_is64) return launch_gather_grouped_t<double2, float2>(jobs, njobs, s);
   if (out_is64) return launch_gather_grouped_t<float2, double2>(jobs, njobs, s);
   return launch_gather_grouped_t<float2, float2>(jobs, njobs, s);
+}
+
+// Row maxima of every job's K-major gather (fp16 planes of grouped launches): 64 x 32 tiles,
+// amax of each job zeroed first.
+template <typename Tin>
+__global__ void __launch_bounds__(256) rowmax_grouped_kernel(const __grid_constant__ GatherJobsP g) {
+  const int b = blockIdx.x;
+  const int p = find_job(g.tile_start, g.n, b);
+  const GatherJob& J = g.j[p];
+  const int t = b - g.tile_start[p];
+  const int64_t m0 = (int64_t)(t % g.tiles_m[p]) * 64, k0 = (int64_t)(t / g.tiles_m[p]) * 32;
+  rowmax_tile<Tin, GrpOff, 64, 32>(static_cast<const Tin*>(J.T), GrpOff{J.mg, J.kg}, J.M, J.K, 0,
+                                   const_cast<float*>(J.amax), m0, k0);
+}
+
+template <typename Tin>
+static cudaError_t launch_rowmax_grouped_t(const GatherJob* jobs, int njobs, cudaStream_t s) {
+  for (int q = 0; q < njobs; ++q)
+    if (jobs[q].amax && jobs[q].M > 0) {
+      cudaError_t e = cudaMemsetAsync(const_cast<float*>(jobs[q].amax), 0, (size_t)jobs[q].M * sizeof(float), s);
+      if (e != cudaSuccess) return e;
+    }
+  for (int base = 0; base < njobs; base += kGatherJobMax) {
+    const int cnt = std::min(kGatherJobMax, njobs - base);
+    GatherJobsP g;
+    std::memset(&g, 0, sizeof(g));
+    int tiles = 0, n = 0;
+    for (int q = 0; q < cnt; ++q) {
+      const GatherJob& J = jobs[base + q];
+      if (!J.amax || J.M <= 0 || J.K <= 0) continue;
+      g.j[n] = J;
+      g.tiles_m[n] = (int)((J.M + 63) / 64);
+      g.tile_start[n] = tiles;
+      tiles += g.tiles_m[n] * (int)((J.K + 31) / 32);
+      ++n;
+    }
+    g.tile_start[n] = tiles;
+    g.n = n;
+    if (tiles == 0) continue;
+    rowmax_grouped_kernel<Tin><<<tiles, dim3(32, 8), 0, s>>>(g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_rowmax_grouped(const GatherJob* jobs, int njobs, int in_is64, cudaStream_t s) {
+  return in_is64 ? launch_rowmax_grouped_t<double2>(jobs, njobs, s) : launch_rowmax_grouped_t<float2>(jobs, njobs, s);
 }
 
 template <typename T>

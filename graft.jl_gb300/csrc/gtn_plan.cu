@@ -624,6 +624,11 @@ static void prof_end(cudaStream_t s, int kind, double flops) {
 }
 
 int map_run(gtn_map map, int precision, const double2* x, double2* y) {
+  if (map->bm) {  // a block-sparse Krylov operator
+    if (precision == blockmap_precision(map->bm)) return blockmap_run(map->bm, x, y);
+    if (precision == GTN_PREC_FP64 && map->bm64) return blockmap_run(map->bm64, x, y);
+    return set_err(map->ctx, GTN_ERR_INVALID, "block map: no map of the requested precision (pass an FP64 block map)");
+  }
   if (precision == GTN_PREC_FP64 && map->fp64_alt) return map_run(map->fp64_alt, precision, x, y);
   gtn_ctx ctx = map->ctx;
   cudaStream_t s = ctx->stream;

@@ -19,7 +19,7 @@ __all__ = [
 
 
 _DEVICE_MODULES = ("device", "networks", "contractions", "solvers", "cbe", "gradients", "blocksparse", "parallel",
-                   "observables", "expansion")
+                   "observables", "expansion", "u1")
 
 
 def __getattr__(name):

@@ -64,6 +64,8 @@ SIGNATURES = {
     "gtn_blockmap_set_graph": (_i, [_p, _i]),
     "gtn_blockmap_info": (_i, [_p, _pd, _pi, _pi64]),
     "gtn_blockmap_destroy": (_i, [_p]),
+    "gtn_blockmap_lanczos_min": (_i, [_p, _p, _p, _i, _d, _i, _i, _pd, _pi, _pd]),
+    "gtn_blockmap_lanczos_refine": (_i, [_p, _p, _p, _i, _d, _i, _pd, _pi, _pd]),
     "gtn_contract": (_i, [_p, _i, _pi, _pi64, _pi, _pi, _pi, C.POINTER(_p), _p, _i]),
     "gtn_contract_vjp": (_i, [_p, _i, _pi, _pi64, _pi, _pi, _pi, C.POINTER(_p), _i, _p, _p, _i]),
     "gtn_permute": (_i, [_p, _i, _pi64, _pi, _p, _p]),
@@ -79,6 +81,7 @@ SIGNATURES = {
     "gtn_diag_scale": (_i, [_p, _i64, _i64, _pd, _i, _p]),
     "gtn_copy2d": (_i, [_p, _i64, _i64, _p, _i64, _p, _i64]),
     "gtn_restrict_leg": (_i, [_p, _i, _pi64, _i, _i64, _pi64, _p, _p]),
+    "gtn_fill": (_i, [_p, _i64, _d, _d, _p]),
     "gtn_multidot_noalloc": (_i, [_p, _i64, _i, _p, _i64, _p, _p]),
     "gtn_selftest_wait": (_i, [_p, _i64]),
     "gtn_tc_tuning": (_i, [_i, _i]),
@@ -101,7 +104,7 @@ MAP_H1, MAP_H2, MAP_H0, MAP_ENV = 1, 2, 3, 4
 class SiteDesc(C.Structure):
     """gtn_site_desc: a node's (or edge's) local structure for the kind-based calls."""
     _fields_ = [("kind", C.c_int), ("n_children", C.c_int), ("n_is_root", C.c_int), ("m_children", C.c_int),
-                ("slot", C.c_int), ("m_is_root", C.c_int)]
+                ("slot", C.c_int), ("m_is_root", C.c_int), ("col_major", C.c_int)]
 
 
 def site_labels(desc):

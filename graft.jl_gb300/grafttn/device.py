@@ -59,6 +59,19 @@ class Context:
     def empty(self, shape):
         return torch.empty(tuple(int(s) for s in shape), dtype=CDT, device=f"cuda:{self.device}")
 
+    def zeros(self, shape):
+        """A zero-filled device tensor (gtn_fill)."""
+        y = self.empty(shape)
+        if y.numel():
+            check(self.lib.gtn_fill(self.h, y.numel(), 0.0, 0.0, C.c_void_p(y.data_ptr())), self.h, "fill")
+        return y
+
+    def copy_into(self, dst, src):
+        """dst <- src (same number of elements, both contiguous) by the library's axpby kernel."""
+        if src.numel():
+            self.axpby(1.0, src.contiguous().reshape(dst.shape), 0.0, dst)
+        return dst
+
     def copy(self, t):
         """Contiguous copy of a device tensor by the library's axpby kernel (the context
         runs on torch's current stream, so it is ordered with the surrounding work)."""

@@ -151,7 +151,8 @@ int gtn_tc_tune_report(char* buf, int64_t cap, int64_t* needed);
  * gtn_env_build writes env(u->v)[ket, op, bra] for GTN_MAP_ENV (n_children, n_is_root
  * describe u; slot = v's child slot of u, or -1 for u's parent) from A_u, W_u and the
  * environments env(w->u) of u's other neighbours (children in slot order, then parent).
- * gtn_site_labels returns the label graph and order of a description (no device needed). */
+ * gtn_site_labels returns the label graph and order of a description (no device needed),
+ * always in the row-major leg order. */
 typedef struct gtn_tensor_s* gtn_tensor;
 enum { GTN_MAP_H1 = 1, GTN_MAP_H2 = 2, GTN_MAP_H0 = 3, GTN_MAP_ENV = 4 };
 typedef struct {
@@ -161,6 +162,9 @@ typedef struct {
   int m_children;  /* H2: children of m, n's parent */
   int slot;        /* H2: n's child slot in m; ENV: the open neighbour's child slot, -1 = parent */
   int m_is_root;   /* H2: m is the root */
+  int col_major;   /* 1: every tensor, the input and the output are column-major arrays with
+                      dims given in the reference's leg order (a TensorKit/Julia array's
+                      layout, first leg fastest); 0: row-major as everywhere else */
 } gtn_site_desc;
 int gtn_tensor_create(gtn_ctx ctx, int rank, const int64_t* dims, gtn_tensor* out);
 int gtn_tensor_wrap(gtn_ctx ctx, int rank, const int64_t* dims, void* device_data, gtn_tensor* out);
@@ -231,6 +235,17 @@ int gtn_blockmap_apply(gtn_blockmap map, const void* x, void* y);
 int gtn_blockmap_set_graph(gtn_blockmap map, int use_graph);
 int gtn_blockmap_info(gtn_blockmap map, double* flops, int* n_problems, int64_t* bytes);
 int gtn_blockmap_destroy(gtn_blockmap map);
+
+/* The eigensolver hook over a block-sparse map (groundstate_eigsolve_backend on abelian
+ * TensorMaps, lib/GraftGroundState/src/GroundState/GroundState.jl:25-39): gtn_lanczos_min
+ * and gtn_lanczos_refine with the block map as the operator, on the flat block buffer x
+ * (every block of the map's input, in its layout).  bm64 (may be NULL when bm is FP64 or
+ * neither the FP64 Rayleigh quotient nor refinement is asked for) is the FP64 block map of
+ * the same plan: it serves the FP64 applications.  Same arguments and results otherwise. */
+int gtn_blockmap_lanczos_min(gtn_blockmap bm, gtn_blockmap bm64, void* x, int krylovdim, double tol,
+                             int maxiter, int rq_fp64, double* energy, int* info, double* resid);
+int gtn_blockmap_lanczos_refine(gtn_blockmap bm, gtn_blockmap bm64, void* x, int inner_dim, double tol,
+                                int max_outer, double* energy, int* info, double* resid);
 
 /* One-shot contraction of a label graph where every operand is given (environment
  * builds, envcache.jl:1010-1101; two-site merge, effective.jl:827-843).  Operand 0 starts
@@ -344,6 +359,9 @@ int gtn_multidot_noalloc(void* stream, int64_t n, int J, const void* V, int64_t 
  * lib/GraftContractions/src/Contractions/effective.jl:445-520), done on the device. */
 int gtn_restrict_leg(gtn_ctx ctx, int rank, const int64_t* dims, int leg, int64_t nsel, const int64_t* idx,
                      const void* in, void* out);
+
+/* x[i] = re + i im for i < n (device c128): zero-filled work buffers of the host drivers. */
+int gtn_fill(gtn_ctx ctx, int64_t n, double re, double im, void* x);
 
 /* Strided 2-D copy of c128 data: dst[i*dst_ld + j] = src[i*src_ld + j] for i < rows, j < cols
  * (column concatenation of factors, e.g. the expanded isometry [Q E] of a bond expansion). */

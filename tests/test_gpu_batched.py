@@ -9,7 +9,7 @@ from oracle import ttn_oracle as O
 
 pytestmark = pytest.mark.gpu
 
-RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 1e-5, "bf16x3": 1e-3}
+RTOL = {"fp64": 1e-12, "fp32": 2e-5, "bf16x6": 1e-5, "bf16x3": 1e-3, "fp16x3": 1e-5}
 
 
 def h1_instance(rng, dims, w=5, d=2):
@@ -44,7 +44,7 @@ def make_batch(ctx, rng, count, dmin, dmax, prec):
     return maps, xs, refs
 
 
-@pytest.mark.parametrize("prec", ["fp64", "bf16x6", "bf16x3", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "bf16x6", "bf16x3", "fp32", "fp16x3"])
 def test_batched_h1_matches_single_and_oracle(ctx, prec):
     rng = np.random.default_rng(31)
     maps, xs, refs = make_batch(ctx, rng, 12, 4, 96, prec)
@@ -59,16 +59,17 @@ def test_batched_h1_matches_single_and_oracle(ctx, prec):
         m.close()
 
 
-def test_batch_graph_replay_64_instances(ctx):
+@pytest.mark.parametrize("prec", ["bf16x6", "fp16x3"])
+def test_batch_graph_replay_64_instances(ctx, prec):
     rng = np.random.default_rng(32)
-    maps, xs, refs = make_batch(ctx, rng, 64, 16, 256, "bf16x6")
+    maps, xs, refs = make_batch(ctx, rng, 64, 16, 256, prec)
     ys = [ctx.empty(m.y_shape) for m in maps]
     b = MapBatch(maps, xs, ys, graph=True)
     for _ in range(3):             # eager, capture + launch, replay
         b.run()
         ctx.sync()
         for y, ref in zip(ys, refs):
-            assert np.linalg.norm(ctx.download(y) - ref) / np.linalg.norm(ref) < RTOL["bf16x6"]
+            assert np.linalg.norm(ctx.download(y) - ref) / np.linalg.norm(ref) < RTOL[prec]
     b.close()
     for m in maps:
         m.close()

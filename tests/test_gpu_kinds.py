@@ -48,7 +48,7 @@ def test_maps_by_kind_match_host_graphs(ctx, precision, tol):
         # eff_h1
         ref = eff_h1(cache, psi, H, n, precision)
         envs = [cache.env(psi, H, w, n) for w in topo.neighbors(n)]
-        km = EffectiveMap.from_kind(ctx, _lib.SiteDesc(_lib.MAP_H1, K, int(root), 0, 0, 0), [H.tensors[n]] + envs,
+        km = EffectiveMap.from_kind(ctx, _lib.SiteDesc(_lib.MAP_H1, K, int(root), 0, 0, 0, 0), [H.tensors[n]] + envs,
                                     precision)
         assert km.x_shape == ref.x_shape
         x = ctx.upload(rng.standard_normal(ref.x_shape) + 1j * rng.standard_normal(ref.x_shape))
@@ -96,3 +96,49 @@ def test_env_build_by_kind_matches_cache(ctx):
                               H.tensors[u], others)
             ref = cache.env(psi, H, u, v)
             assert rel(ctx.download(E), ctx.download(ref)) < 1e-13, (u, v)
+
+
+def test_col_major_tensors_match_row_major(ctx):
+    # TensorKit/Julia arrays: column-major buffers with dims in the reference's leg order
+    topo = G.binary_topology(3)
+    H = G.TTNO.from_hamiltonian(G.heisenberg(topo), ctx)
+    psi = G.random_ttns(np.random.default_rng(8), topo, 2, 6, ctx=ctx)
+    n = 3
+    m = topo.parent[n]
+    G.move_center(psi, n)
+    cache = EnvCache(topo)
+    K, Km = topo.nchildren(n), topo.nchildren(m)
+    envs = [cache.env(psi, H, w, n) for w in topo.children[n]]
+    envs += [cache.env(psi, H, w, m) for w in topo.neighbors(m) if w != n]
+    statics = [H.tensors[n], H.tensors[m]] + envs
+    desc = _lib.SiteDesc(_lib.MAP_H2, K, 0, Km, topo.childslot(m, n), int(topo.parent[m] < 0), 0)
+    row = EffectiveMap.from_kind(ctx, desc, statics, "fp64")
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal(row.x_shape) + 1j * rng.standard_normal(row.x_shape)
+    y_row = ctx.download(row(ctx.upload(x)))
+
+    def colmajor(a):  # the same array stored first-leg-fastest: a row-major buffer of a.T
+        return np.ascontiguousarray(np.transpose(a))
+    cm_statics = [ctx.upload(colmajor(ctx.download(s))) for s in statics]
+    import ctypes as C
+    from grafttn.device import TensorHandle
+    hs = []
+    for s_dev, s_orig in zip(cm_statics, statics):
+        h = C.c_void_p()
+        dims = (C.c_int64 * s_orig.dim())(*[int(v) for v in s_orig.shape])
+        assert ctx.lib.gtn_tensor_wrap(ctx.h, s_orig.dim(), dims, C.c_void_p(s_dev.data_ptr()), C.byref(h)) == 0
+        hs.append(h)
+    desc.col_major = 1
+    arr = (C.c_void_p * len(hs))(*[h.value for h in hs])
+    mh = C.c_void_p()
+    assert ctx.lib.gtn_map_create_kind(ctx.h, C.byref(desc), len(hs), arr, 0, C.byref(mh)) == 0
+    xc = ctx.upload(colmajor(x))
+    yc = ctx.empty(tuple(reversed(row.y_shape)))
+    assert ctx.lib.gtn_map_apply(mh, C.c_void_p(xc.data_ptr()), C.c_void_p(yc.data_ptr())) == 0
+    y_col = np.transpose(ctx.download(yc))
+    assert rel(y_col, y_row) < 1e-13
+    ctx.lib.gtn_map_destroy(mh)
+    for h in hs:
+        ctx.lib.gtn_tensor_destroy(h)
+    row.close()
+    del TensorHandle
