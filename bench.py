@@ -499,6 +499,32 @@ def run_ours(args, rank, world):
         except Exception as exc:
             alt[prec] = {"error": f"{type(exc).__name__}: {exc}"}
     extra["other_mixed_modes"] = alt
+    # the grouping choice: the same map compiled as the plain env-first chain (no
+    # pre-contracted static groups), timed the same way
+    try:
+        os.environ["GTN_STATIC_GROUPING"] = "0"
+        hm3 = EffectiveMap(ctx, x_shape, labels, order, dstat, args.precision)
+        os.environ.pop("GTN_STATIC_GROUPING", None)
+        y3 = ctx.empty(hm3.y_shape)
+        for _ in range(2):
+            hm3.apply_into(x, y3)
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b0.record(stream)
+        for _ in range(args.steps):
+            hm3.apply_into(x, y3)
+        b1.record(stream)
+        torch.cuda.synchronize()
+        recs3 = hm3.apply_profiled(x, y3)
+        extra["grouping_ab"] = {"grouped_ms_per_apply": ms / args.steps,
+                                "env_first_ms_per_apply": b0.elapsed_time(b1) / args.steps,
+                                "env_first_executed_flops": sum(f for _, _, f in recs3),
+                                "grouped_executed_flops": exec_flops, "algorithmic_flops": flops,
+                                "env_first_tc_launches": sum(1 for k, _, _ in recs3 if k == "tc_gemm")}
+        hm3.close()
+        del y3
+    except Exception as exc:
+        os.environ.pop("GTN_STATIC_GROUPING", None)
+        extra["grouping_ab"] = {"error": f"{type(exc).__name__}: {exc}"}
     if not args.skip_extra:
         for name, fn in (("u1_blocksparse", bench_u1), ("batched_eff_h1", bench_batched)):
             try:
@@ -557,10 +583,13 @@ def dmrg_segment(ctx, steps, precision, D=1024, refine_tol=1e-8):
     from one seeded random state (seed 7, bonds min(D, 2^k)), once in the mixed mode and once
     in FP64 on the same state.  A step is the reference's local update (GroundState.jl:102-143):
     gauge move, merge, eff_h2 build, Lanczos (krylovdim 20, tol 1e-10), truncated SVD split at
-    maxdim D.  In the mixed arm the Lanczos vector is then refined with FP64 residuals
+    maxdim D.  In the mixed arm the Lanczos vector is then refined with FP64-accurate residuals
     (gtn_lanczos_refine) until |H v - E v| <= refine_tol * |E|, and its energy is the FP64
-    Rayleigh quotient.  The environments of the first step are built before the clock starts
-    (they are the same for both arms); environment rebuilds after each split are timed."""
+    Rayleigh quotient; the FP64-accurate work of that arm (residuals, environment rebuilds)
+    runs on the tensor cores in GTN_PREC_FP64E (an FP64E twin of the map).  The FP64 arm is
+    the plain FP64 GPU path: FP64 maps, FP64 environments.  The environments of the first
+    step are built before the clock starts (the same for both arms); environment rebuilds
+    after each split are timed."""
     import torch
     import grafttn as G
     from grafttn.contractions import EnvCache, eff_h2
@@ -586,6 +615,8 @@ def dmrg_segment(ctx, steps, precision, D=1024, refine_tol=1e-8):
     for prec in (precision, "fp64"):
         psi, cache = psi0.copy(), cache0.copy()
         pcode = G._lib.PRECISIONS[prec]
+        if pcode != G._lib.PREC_FP64:
+            cache.precision = G._lib.PREC_FP64E
         n = n0
         recs = []
         for _ in range(steps):
@@ -595,11 +626,17 @@ def dmrg_segment(ctx, steps, precision, D=1024, refine_tol=1e-8):
             move_center(psi, n, cache)
             theta = two_site_tensor(psi, n, m)
             h2 = eff_h2(cache, psi, H, n, m, pcode)
+            h2e = None
+            if pcode != G._lib.PREC_FP64:
+                h2e = eff_h2(cache, psi, H, n, m, G._lib.PREC_FP64E)
+                h2.set_fp64_map(h2e)
             E, v, info = h2.lanczos_min(theta, krylovdim=20, tol=1e-10, maxiter=100)
             rstats = {}
             if pcode != G._lib.PREC_FP64:
                 E, v = refine_local(h2, E, v, refine_tol, stats=rstats)
             h2.close()
+            if h2e is not None:
+                h2e.close()
             cache.invalidate_edge(n, m)
             split_two_site(psi, v, n, m, trunc, "m")
             torch.cuda.synchronize()

@@ -180,6 +180,19 @@ int gtn_map_destroy(gtn_map map) {
   return GTN_OK;
 }
 
+int gtn_map_set_fp64(gtn_map map, gtn_map fp64_map) {
+  if (!map) return GTN_ERR_INVALID;
+  if (fp64_map) {
+    if (fp64_map == map || fp64_map->ctx != map->ctx || fp64_map->x_elems != map->x_elems ||
+        fp64_map->y_elems != map->y_elems || fp64_map->fp64_map)
+      return set_err(map->ctx, GTN_ERR_INVALID, "gtn_map_set_fp64: a different map of the same shape and context");
+    if (fp64_map->precision != GTN_PREC_FP64 && fp64_map->precision != GTN_PREC_FP64E)
+      return set_err(map->ctx, GTN_ERR_INVALID, "gtn_map_set_fp64: the map must be FP64 or FP64-grade");
+  }
+  map->fp64_map = fp64_map;
+  return GTN_OK;
+}
+
 int gtn_map_apply_prec(gtn_map map, int precision, const void* x, void* y) {
   if (!map || !x || !y) return GTN_ERR_INVALID;
   MapUse use(map);

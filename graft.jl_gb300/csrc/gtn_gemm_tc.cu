@@ -15,7 +15,7 @@
 // Every mbarrier wait is bounded (globaltimer, 4 s); on timeout the CTA records an error
 // code in the context's device flag, drains its own copies and MMAs, frees TMEM, returns.
 #include "gtn_internal.h"
-#include <cuda.h>
+#include "gtn_tcgen05.h"
 
 #include <algorithm>
 #include <atomic>
@@ -27,11 +27,11 @@
 #include <tuple>
 
 namespace {
+using namespace gtn_tc;
 
 constexpr int BM = 128;
 constexpr int BKE = 64;  // bf16 elements per k-block = 128 bytes = one SW128 row
 constexpr int A_BYTES = BM * BKE * 2;
-constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 constexpr int kTcGroupMax = 56;
 
@@ -41,51 +41,6 @@ struct ProdList {
   int b[9];
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_local(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait on a phase parity.  Returns false on timeout or when another role of the
-// CTA has already aborted.
-__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
-                          uint64_t timeout_ns = kTimeoutNs) {
-  uint64_t t0 = 0;
-  for (uint32_t it = 0;; ++it) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 255u) == 255u) {
-      if (*abort_flag) return false;
-      const uint64_t now = globaltimer();
-      if (t0 == 0) t0 = now;
-      else if (now - t0 > timeout_ns) return false;
-    }
-  }
-}
-
 // A wait that runs out: an mbarrier expecting one arrival that never comes.
 __global__ void wait_selftest_kernel(int* __restrict__ errflag, uint64_t timeout_ns) {
   __shared__ __align__(8) uint64_t bar;
@@ -94,76 +49,6 @@ __global__ void wait_selftest_kernel(int* __restrict__ errflag, uint64_t timeout
   no_abort = 0;
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   if (!mbar_wait(&bar, 0u, &no_abort, timeout_ns)) atomicCAS(errflag, 0, DEVERR_SELFTEST_TIMEOUT);
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* tm, uint64_t* bar, int x,
-                                            int y, int z) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
-      "[%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(tm)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart.
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)1u << 16;            // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024u >> 4) << 32;  // stride byte offset
-  d |= (uint64_t)1u << 46;            // descriptor version
-  d |= (uint64_t)2u << 61;            // SWIZZLE_128B
-  return d;
-}
-
-// Shared-memory matrix descriptor: K-major, SWIZZLE_64B, 8-row groups 512 B apart.
-__device__ __forceinline__ uint64_t sdesc64(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)1u << 16;            // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(512u >> 4) << 32;   // stride byte offset
-  d |= (uint64_t)1u << 46;            // descriptor version
-  d |= (uint64_t)4u << 61;            // SWIZZLE_64B
-  return d;
-}
-
-// Instruction descriptor, kind::f16: D=f32, A=B=bf16, both K-major.
-__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-// The same with A=B=f16 (format code 0 in both operand fields).
-__host__ __device__ constexpr uint32_t idesc_f16(int m, int n) {
-  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
-                                          uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-      "l"(da), "l"(db), "r"(idesc), "r"(accumulate));
-}
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                   smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-        "=r"(v[14]), "=r"(v[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 template <int BN> struct Cfg {
@@ -507,17 +392,14 @@ __global__ void __launch_bounds__(128, CPS)
 // bytes per MAC are 2/3 of a one-CTA 128 x 256 tile: 256 rows of operands per k-block
 // against 384.  Both TMEM accumulators (leading product, corrections) take 256 columns.
 //
-// Cross-CTA hand-offs are plain mbarrier arrivals at cluster scope on the peer's
-// barriers (no TMA or commit to several CTAs at once):
-//   * the odd CTA's forwarding thread waits for its own stage to land and arrives on the
-//     leader's full barrier of that stage (the leader's barrier counts 2 arrivals: its own
-//     expect_tx and the forward);
-//   * the leader's producer, after the MMA commit released a stage, arrives on the odd
-//     CTA's empty barrier of that stage;
-//   * leader thread 0, after the accumulators are complete, arrives on the odd CTA's
-//     accumulator barrier.
-// Every wait is bounded like the one-CTA kernel's; a cluster barrier before TMEM is freed
-// keeps either CTA from leaving while the other may still touch its shared memory.
+// Cross-CTA hand-offs (no copy or commit goes to several CTAs at once):
+//   * both CTAs' TMA copies of a stage complete on the leader's full barrier (the
+//     .cta_group::2 form of cp.async.bulk.tensor); the leader's producer announces the
+//     bytes of both halves;
+//   * the leader's MMA thread commits each stage to the empty barriers of both CTAs (one
+//     commit per barrier) and the finished accumulators to both accumulator barriers.
+// Every wait is bounded like the one-CTA kernel's; cluster barriers at the end keep either
+// CTA from leaving while the other may still use its memory.
 __device__ __forceinline__ uint32_t cluster_ctarank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -531,9 +413,6 @@ __device__ __forceinline__ uint32_t peer_addr(const void* p, uint32_t rank) {
   uint32_t r;
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
   return r;
-}
-__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait_cl(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
@@ -568,9 +447,20 @@ __device__ __forceinline__ void umma_pair(uint32_t tmem_d, uint64_t da, uint64_t
       "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
       "l"(da), "l"(db), "r"(idesc), "r"(accumulate));
 }
-__device__ __forceinline__ void umma_commit_pair(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
+// Arrive on the mbarrier at shared::cluster address `bar` (this CTA's or the peer's) once
+// every MMA issued so far has completed.
+__device__ __forceinline__ void umma_commit_pair(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+// TMA tile load into this CTA's shared memory whose completion is counted on the mbarrier
+// at shared::cluster address `bar`, which may be the peer CTA's (.cta_group::2).
+__device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const CUtensorMap* tm, uint32_t bar, int x, int y,
+                                                 int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 "
+      "[%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(bar), "r"(x), "r"(y), "r"(z)
+      : "memory");
 }
 
 template <int P> struct CfgPair {
@@ -601,7 +491,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
   __shared__ __align__(8) uint64_t accum_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
-  __shared__ int n_issued, n_consumed;
+  __shared__ int n_issued, n_consumed, peer_issued;
 
   const uint32_t rank = cluster_ctarank();
   const bool leader = rank == 0;
@@ -615,13 +505,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < CF::STAGES; ++s) {
-      mbar_init(&full_bar[s], leader ? 2 : 1);
+      mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
     mbar_init(&accum_bar, 1);
     abort_flag = 0;
     n_issued = 0;
     n_consumed = 0;
+    peer_issued = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
@@ -634,11 +525,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
   }
   fence_before();
   __syncthreads();
-  cluster_sync();  // both CTAs' barriers exist before either side arrives on the other's
+  cluster_sync();  // both CTAs' barriers exist before either side signals the other's
   fence_after();
   const uint32_t tmem_d = tmem_slot;
 
   if (warp == 0 && lane == 0) {
+    const uint32_t leader_full0 = peer_addr(&full_bar[0], 0u);
     int it = 0;
     for (; it < nkb; ++it) {
       const int s = it % CF::STAGES;
@@ -648,35 +540,24 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
         atomicCAS(errflag, 0, DEVERR_TMA_TIMEOUT);
         break;
       }
-      // the MMAs that read stage s in both CTAs are done: release the odd CTA's copy too
-      if (leader && it >= CF::STAGES) mbar_arrive_remote(peer_addr(&empty_bar[s], peer));
       const uint32_t sa = smem_u32(smem + s * CF::STAGE_BYTES);
       const uint32_t sb = sa + P * CF::A_PLANE;
-      mbar_expect_tx(&full_bar[s], CF::STAGE_BYTES);
+      const uint32_t fb = leader_full0 + (uint32_t)(s * sizeof(uint64_t));
+      if (leader) mbar_expect_tx(&full_bar[s], 2 * CF::STAGE_BYTES);  // both halves
 #pragma unroll
       for (int p = 0; p < P; ++p) {
-        tma_load_3d(sa + p * CF::A_PLANE, &tmA, &full_bar[s], it * BKE2, m0, p);
-        tma_load_3d(sb + p * CF::B_PLANE, &tmB, &full_bar[s], it * BKE2, rb, p);
+        tma_load_3d_pair(sa + p * CF::A_PLANE, &tmA, fb, it * BKE2, m0, p);
+        tma_load_3d_pair(sb + p * CF::B_PLANE, &tmB, fb, it * BKE2, rb, p);
       }
     }
     n_issued = it;
-  } else if (warp == 1 && lane == 0 && !leader) {
-    // forwarder: this CTA's half of stage s has landed -> tell the leader
-    int it = 0;
-    const uint32_t remote_full0 = peer_addr(&full_bar[0], peer);
-    for (; it < nkb; ++it) {
-      const int s = it % CF::STAGES;
-      const uint32_t ph = (uint32_t)(it / CF::STAGES) & 1u;
-      if (!mbar_wait_cl(&full_bar[s], ph, &abort_flag)) {
-        abort_flag = 1;
-        atomicCAS(errflag, 0, DEVERR_MMA_TIMEOUT);
-        break;
-      }
-      mbar_arrive_remote(remote_full0 + (uint32_t)(s * sizeof(uint64_t)));
+    if (!leader) {  // tell the leader how many stages this CTA issued (its drain covers them)
+      const uint32_t dst = peer_addr(&peer_issued, 0u);
+      asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(dst), "r"(it) : "memory");
     }
-    n_consumed = it;
-  } else if (warp == 1 && lane == 0) {
+  } else if (warp == 1 && lane == 0 && leader) {
     const uint32_t idesc = sc.fp16 ? idesc_f16(256, CF::TILE_N) : idesc_bf16(256, CF::TILE_N);
+    const uint32_t peer_empty0 = peer_addr(&empty_bar[0], peer);
     bool lead_started = false, corr_started = false;
     int it = 0;
     for (; it < nkb; ++it) {
@@ -702,10 +583,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
           if (lead) lead_started = true; else corr_started = true;
         }
       }
-      umma_commit_pair(&empty_bar[s]);
+      umma_commit_pair(smem_u32(&empty_bar[s]));
+      umma_commit_pair(peer_empty0 + (uint32_t)(s * sizeof(uint64_t)));
     }
     n_consumed = it;
-    umma_commit_pair(&accum_bar);
+    umma_commit_pair(smem_u32(&accum_bar));
+    umma_commit_pair(peer_addr(&accum_bar, peer));
   }
   __syncwarp();
 
@@ -714,7 +597,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
     abort_flag = 1;
     atomicCAS(errflag, 0, DEVERR_EPI_TIMEOUT);
   }
-  if (ok && leader && threadIdx.x == 0) mbar_arrive_remote(peer_addr(&accum_bar, peer));
   __syncwarp();
   fence_after();
   if (ok) {
@@ -750,11 +632,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
   }
   fence_before();
   __syncthreads();
-  // drain this CTA's copies that no consumer waited for (abort path only)
-  if (threadIdx.x == 0) {
-    for (int it = n_consumed; it < n_issued; ++it) {
+  cluster_sync();  // the odd CTA's issue count has reached the leader
+  // drain: copies of either CTA that no MMA waited for (abort path only) land on the
+  // leader's full barriers before anyone leaves
+  if (leader && threadIdx.x == 0) {
+    const int issued = n_issued > peer_issued ? n_issued : peer_issued;
+    for (int it = n_consumed; it < issued; ++it) {
       volatile int no_abort = 0;
-      mbar_wait_cl(&full_bar[it % CF::STAGES], (uint32_t)(it / CF::STAGES) & 1u, &no_abort);
+      mbar_wait_cl(&full_bar[it % CF::STAGES], (uint32_t)(it / CF::STAGES) & 1u, &no_abort, 50000000ull);
     }
   }
   __syncthreads();
@@ -1032,26 +917,6 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_grouped_kernel(const __grid_co
   const int t = b - g.tile_start[p];
   const int tn = t % g.tiles_n[p], tm = t / g.tiles_n[p];  // N tile fastest
   tc_tile<BN>(&g.tmA[p], &g.tmB[p], g.C[p], g.M[p], g.N[p], g.nkb[p], g.prods, tm * BM, tn * BN, errflag);
-}
-
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn get_encode() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
-  return fn;
 }
 
 // 3-D map over bf16 planes: (2Kp elements, rows, planes), box (64, box_rows, 1).

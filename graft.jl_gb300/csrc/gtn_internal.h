@@ -237,6 +237,28 @@ __host__ __device__ inline float fp16_row_scale(float mx) {
   return r;
 }
 cudaError_t launch_tc_gemm(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why);
+
+// ---- FP64-grade GEMM on the tensor cores (gtn_gemm_f64e.cu) ------------------------------
+// C (complex FP64, [N][M]) = A B^T from integer digit planes: A [S][M][2Kp] (rows scaled by
+// 2^k(a_max[m])), B' [S][2N][2Kp] (complex rows scaled by 2^k(b_max[n])), S = kF64eSlices.
+constexpr int kF64eSlices = 7;
+struct F64eGemmArgs {
+  const __nv_bfloat16* A = nullptr;
+  const __nv_bfloat16* B = nullptr;
+  double2* C = nullptr;
+  int64_t M = 0, N = 0, Kp = 0;
+  const float* a_max = nullptr;
+  const float* b_max = nullptr;
+};
+cudaError_t launch_f64e_gemm(const F64eGemmArgs& a, int* errflag, cudaStream_t s, std::string* why);
+// digit planes of the running tensor's K-major view (c128), rows scaled by amax (from
+// launch_rowmax_*), and of a static B [N][K] (bmax written here)
+cudaError_t launch_split_i7_tab(const double2* T, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                               int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s);
+cudaError_t launch_split_i7_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                                 int64_t Kp, int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s);
+cudaError_t launch_pack_b_planes_i7(const double2* B, int64_t N, int64_t K, int64_t Kp, int64_t pstride,
+                                    __nv_bfloat16* out, float* bmax, cudaStream_t s);
 bool tc_gemm_supported(int cc_major, int cc_minor);
 // Independent problems in one launch per 56 problems (same product list for all).
 cudaError_t launch_tc_gemm_grouped(const TcGemmArgs* probs, int nprob, int* errflag, cudaStream_t s,
@@ -328,6 +350,7 @@ struct gtn_map_s {
   double exec_flops = 0;   // FLOPs of the executed (possibly grouped) chain
   int n_groups = 0;
   gtn_map fp64_alt = nullptr;  // FP64-optimal plan sharing this map's workspace
+  gtn_map fp64_map = nullptr;  // caller-set map serving this map's FP64 applications (not owned)
   int64_t max_t = 0;       // largest running tensor (elements)
   int64_t max_a = 0;       // largest A operand (elements, for permuted / split staging)
   int64_t max_apl = 0;     // largest split-plane staging (bf16 elements per plane * planes)

@@ -284,6 +284,91 @@ struct Split16Writer {
   }
 };
 
+// ---- integer digit planes of the FP64-grade tensor-core GEMM (gtn_gemm_f64e.cu) ---------
+// x 2^k (|x| 2^k < 1, k from the row maximum) as kF64eSlices signed base-128 digits,
+// x 2^k = sum_i d_i 2^{-7(i+1)}: the fixed-point value N = round(x 2^{k + 7 S}) is formed
+// from the double's bits with integer operations (no FP64 arithmetic), then peeled from the
+// top digit down with round-half-up shifts; |d_0| <= 128, |d_i| <= 64, all exact in bf16.
+__device__ __forceinline__ int f64e_row_exp(float mx) {
+  const uint32_t b = __float_as_uint(mx);
+  const int e = (int)((b >> 23) & 0xffu);
+  return mx > 0.f ? 126 - e : 0;
+}
+__device__ __forceinline__ void i7_digits(double x, int k, __nv_bfloat16* d) {
+  constexpr int NB = 7 * kF64eSlices;
+  const long long bits = __double_as_longlong(x);
+  const int E = (int)((bits >> 52) & 0x7ff);
+  long long N = 0;
+  if (E != 0 && E != 0x7ff) {
+    const long long mant = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+    const int r = 1075 - E - k - NB;  // >= 4 whenever |x| 2^k < 1
+    if (r <= 0) N = mant << (r < -10 ? 10 : -r);
+    else if (r < 63) N = (mant + (1LL << (r - 1))) >> r;
+    if (bits < 0) N = -N;
+  }
+#pragma unroll
+  for (int i = 0; i < kF64eSlices; ++i) {
+    const int w = 7 * (kF64eSlices - 1 - i);
+    long long di;
+    if (w > 0) {
+      di = (N + (1LL << (w - 1))) >> w;
+      N -= di << w;
+    } else {
+      di = N;
+    }
+    d[i] = __float2bfloat16_rn((float)di);
+  }
+}
+__device__ __forceinline__ void i7_digits(float x, int k, __nv_bfloat16* d) { i7_digits((double)x, k, d); }
+
+struct Int7Writer {
+  __nv_bfloat16* out;
+  int64_t ld2;      // row pitch (= 2 Kp)
+  int64_t pstride;  // plane pitch
+  const float* amax;
+  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v) const {
+    const int e = f64e_row_exp(amax[m]);
+    __nv_bfloat16 dr[kF64eSlices], di[kF64eSlices];
+    i7_digits(v.x, e, dr);
+    i7_digits(v.y, e, di);
+    __nv_bfloat16* row = out + m * ld2 + 2 * k;
+#pragma unroll
+    for (int p = 0; p < kF64eSlices; ++p) {
+      __nv_bfloat162 pr;
+      pr.x = dr[p];
+      pr.y = di[p];
+      *reinterpret_cast<__nv_bfloat162*>(row + p * pstride) = pr;
+    }
+  }
+};
+
+__global__ void pack_b_planes_i7_kernel(const double2* __restrict__ B, int64_t N, int64_t K, int64_t Kp,
+                                        int64_t pstride, const float* __restrict__ bmax,
+                                        __nv_bfloat16* __restrict__ out) {
+  const int64_t total = 2 * N * Kp;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = idx / Kp;
+    const int64_t k = idx - row * Kp;
+    const int64_t n = row >> 1;
+    const int e = f64e_row_exp(bmax[n]);
+    double v0 = 0.0, v1 = 0.0;
+    if (k < K) {
+      const double2 b = B[n * K + k];
+      if ((row & 1) == 0) { v0 = b.x; v1 = -b.y; } else { v0 = b.y; v1 = b.x; }
+    }
+    __nv_bfloat16 d0[kF64eSlices], d1[kF64eSlices];
+    i7_digits(v0, e, d0);
+    i7_digits(v1, e, d1);
+    for (int p = 0; p < kF64eSlices; ++p) {
+      __nv_bfloat162 pr;
+      pr.x = d0[p];
+      pr.y = d1[p];
+      *reinterpret_cast<__nv_bfloat162*>(out + p * pstride + row * (2 * Kp) + 2 * k) = pr;
+    }
+  }
+}
+
 // amax[m] = max over k of max(|re|, |im|) of the K-major gather (atomic max of the
 // non-negative float bits; amax zeroed before the launch).
 template <typename Tin, class Off, int TM, int TK>
@@ -873,6 +958,28 @@ cudaError_t launch_split16_tab(const void* T, int is64, const GatherTab& t, int6
   const Split16Writer w{reinterpret_cast<__half*>(out), 2 * Kp, pstride, amax};
   return is64 ? launch_gather_tab(static_cast<const double2*>(T), t.om, t.ok, M, K, Kp, t.m_fast, w, s)
               : launch_gather_tab(static_cast<const float2*>(T), t.om, t.ok, M, K, Kp, t.m_fast, w, s);
+}
+cudaError_t launch_split_i7_tab(const double2* T, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                               int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s) {
+  const Int7Writer w{out, 2 * Kp, pstride, amax};
+  return launch_gather_tab(T, t.om, t.ok, M, K, Kp, t.m_fast, w, s);
+}
+cudaError_t launch_split_i7_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                                 int64_t Kp, int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s) {
+  const Int7Writer w{out, 2 * Kp, pstride, amax};
+  return launch_gather(T, mg, kg, M, K, Kp, w, s);
+}
+cudaError_t launch_pack_b_planes_i7(const double2* B, int64_t N, int64_t K, int64_t Kp, int64_t pstride,
+                                    __nv_bfloat16* out, float* bmax, cudaStream_t s) {
+  if (N <= 0) return cudaSuccess;
+  if (N > 2147483647LL) return cudaErrorInvalidConfiguration;
+  bmax_kernel<<<(unsigned)N, 256, 0, s>>>(B, K, bmax);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int64_t total = 2 * N * Kp;
+  int64_t blocks = std::min<int64_t>(std::max<int64_t>((total + 255) / 256, 1), 152 * 32);
+  pack_b_planes_i7_kernel<<<(unsigned)blocks, 256, 0, s>>>(B, N, K, Kp, pstride, bmax, out);
+  return cudaGetLastError();
 }
 cudaError_t launch_gather_tab_to_c128(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t ldo,
                                       double2* out, cudaStream_t s) {

@@ -11,6 +11,8 @@
 // tcgen05 path).  Statics are permuted/conjugated/packed once when the map is created.
 #include "gtn_internal.h"
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -81,6 +83,7 @@ bool is_tc(int precision) {
 }
 int nplanes_of(int precision) { return precision == GTN_PREC_BF16X6 ? 3 : 2; }
 bool is_fp16(int precision) { return precision == GTN_PREC_FP16X3; }
+bool is_f64e(int precision) { return precision == GTN_PREC_FP64E; }
 
 // Device table of the element offsets of indices 0..n-1 of an index group (digits outer..
 // inner, the innermost one incremented first), owned by the map.
@@ -143,6 +146,10 @@ double est_step_time(int prec, double M, double K, double N) {
   if (small) return t + (M * K + M * N) * e / hbm + flops / (fp64 ? 1.1e12 : 15e12);
   if (fp64) return t + flops / 1.1e12 + (2 * M * K + M * N) * e / hbm;
   if (prec == GTN_PREC_FP32) return t + flops / 20e12 + (2 * M * K + M * N) * e / hbm;
+  if (prec == GTN_PREC_FP64E) {  // 28 digit products; 7 digit planes of A written and read
+    const double Kp = std::ceil(K / 32.0) * 32.0;
+    return t + flops / 40e12 + (M * K * 16.0 + M * 2 * Kp * 7 * 2 * 2 + M * N * 16.0) / hbm;
+  }
   const double rate = prec == GTN_PREC_BF16X6 ? 200e12 : 300e12;  // bf16x3 and fp16x3: 3 products
   const double P = prec == GTN_PREC_BF16X6 ? 3.0 : 2.0;
   const double Kp = std::ceil(K / 32.0) * 32.0;
@@ -247,8 +254,8 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
                const int* conj, const int* order, const void* const* statics, int precision,
                gtn_map map, bool allow_group, bool alloc_ws) {
   if (n < 2) return set_err(ctx, GTN_ERR_INVALID, "map needs the input and at least one static");
-  if (precision < 0 || precision > GTN_PREC_FP16X3) return set_err(ctx, GTN_ERR_INVALID, "unknown precision");
-  if (is_tc(precision) && !tc_gemm_supported(ctx->cc_major, ctx->cc_minor))
+  if (precision < 0 || precision > GTN_PREC_FP64E) return set_err(ctx, GTN_ERR_INVALID, "unknown precision");
+  if ((is_tc(precision) || is_f64e(precision)) && !tc_gemm_supported(ctx->cc_major, ctx->cc_minor))
     return set_err(ctx, GTN_ERR_UNSUPPORTED, "tcgen05 precision modes need an sm_10x device");
   std::vector<std::vector<int64_t>> D(n);
   std::vector<std::vector<int>> L(n);
@@ -304,7 +311,8 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   map->max_a = 0;
   map->max_apl = 0;
   const bool tc = is_tc(precision);
-  const int P = tc ? nplanes_of(precision) : 0;
+  const bool f64e = is_f64e(precision);
+  const int P = tc ? nplanes_of(precision) : (f64e ? kF64eSlices : 0);
 
   // ---- the reference's env-first chain and the grouped chain we execute ------------------
   ChainOp X{L[0], D[0]};
@@ -315,6 +323,10 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   const int ns = n - 1;
   std::vector<int> best_cut(ns, 1);  // cut[i] = 1: a group ends after static i
   double best_t = ref_cost.first;
+  // GTN_STATIC_GROUPING=0 keeps the env-first chain of single statics (no pre-contracted
+  // groups): the comparison point of the grouping choice
+  const char* genv = std::getenv("GTN_STATIC_GROUPING");
+  if (genv && genv[0] == '0') allow_group = false;
   if (allow_group && statics && ns >= 2 && ns <= 12) {
     for (uint32_t mask = 0; mask < (1u << (ns - 1)); ++mask) {
       std::vector<ChainOp> chain;
@@ -437,7 +449,7 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
     if (!make_group(DT, freeT, &st.mg) || !make_group(DT, sh, &st.kg))
       return set_err(ctx, GTN_ERR_UNSUPPORTED, "too many non-contiguous leg groups");
     st.small = st.K <= kSmallK && small_contract_fits((int)st.K, (int)std::min<int64_t>(st.N, 1 << 20), sizeof(double2));
-    st.tc = tc && !st.small;
+    st.tc = (tc || f64e) && !st.small;
     st.Kp = ((st.K + 31) / 32) * 32;
     // C legs: S free (S order), then T free (T order)
     for (int b : freeS) { st.out_labels.push_back(LS[b]); st.out_dims.push_back(DS[b]); }
@@ -466,8 +478,8 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
         e = launch_conj_inplace(st.b64, st.N * st.K, ctx->stream);
         ctx->launches++;
       }
-      // (a one-shot FP64 contraction never reads the complex FP32 copy)
-      if (e == cudaSuccess && !(map->oneshot && precision == GTN_PREC_FP64)) {
+      // (a one-shot FP64 contraction and an FP64-grade plan never read the complex FP32 copy)
+      if (e == cudaSuccess && !(map->oneshot && precision == GTN_PREC_FP64) && !f64e) {
         e = dalloc(map, &st.b32, (size_t)st.N * st.K * sizeof(float2));
         if (e == cudaSuccess) {
           const int64_t ne = st.N * st.K;
@@ -481,7 +493,13 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
         st.bplanes = P;
         const int64_t pstride = 2 * st.N * 2 * st.Kp;
         e = dalloc(map, &st.bpl, (size_t)P * pstride * sizeof(__nv_bfloat16));
-        if (e == cudaSuccess && is_fp16(precision)) {
+        if (e == cudaSuccess && f64e) {
+          st.bfp16 = 2;  // integer digit planes
+          e = dalloc(map, &st.bmax, (size_t)st.N * sizeof(float));
+          if (e == cudaSuccess) e = launch_pack_b_planes_i7(st.b64, st.N, st.K, st.Kp, pstride, st.bpl, st.bmax,
+                                                            ctx->stream);
+          ctx->launches += 2;
+        } else if (e == cudaSuccess && is_fp16(precision)) {
           st.bfp16 = 1;
           e = dalloc(map, &st.bmax, (size_t)st.N * sizeof(float));
           if (e == cudaSuccess) e = launch_pack_b_planes_f16(st.b64, st.N, st.K, st.Kp, pstride, st.bpl, st.bmax,
@@ -568,7 +586,7 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
   if (dalloc(map, &map->buf0, tbytes) != cudaSuccess || dalloc(map, &map->buf1, tbytes) != cudaSuccess ||
       dalloc(map, &map->abuf, std::max<size_t>(abytes, 256)) != cudaSuccess)
     return set_err(ctx, GTN_ERR_MEMORY, "map workspace allocation failed");
-  if (is_fp16(precision) && map->max_mtc > 0 &&
+  if ((is_fp16(precision) || f64e) && map->max_mtc > 0 &&
       dalloc(map, &map->amax, (size_t)map->max_mtc * sizeof(float)) != cudaSuccess)
     return set_err(ctx, GTN_ERR_MEMORY, "map workspace allocation failed");
   if (max_sk > 0 && dalloc(map, reinterpret_cast<double2**>(&map->skbuf), (size_t)max_sk * sizeof(double2)) !=
@@ -629,6 +647,10 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
     if (precision == GTN_PREC_FP64 && map->bm64) return blockmap_run(map->bm64, x, y);
     return set_err(map->ctx, GTN_ERR_INVALID, "block map: no map of the requested precision (pass an FP64 block map)");
   }
+  if (precision == GTN_PREC_FP64 && map->fp64_map) {  // e.g. an FP64-grade tensor-core twin
+    gtn_map m2 = map->fp64_map;
+    return map_run(m2, m2->precision, x, y);
+  }
   if (precision == GTN_PREC_FP64 && map->fp64_alt) return map_run(map->fp64_alt, precision, x, y);
   gtn_ctx ctx = map->ctx;
   cudaStream_t s = ctx->stream;
@@ -638,7 +660,13 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
       if (!st.small && (!st.bpl || st.bplanes != nplanes_of(precision) || st.bfp16 != (is_fp16(precision) ? 1 : 0)))
         return set_err(ctx, GTN_ERR_INVALID, "map was not created for this tcgen05 precision");
   }
-  const bool fp64 = precision == GTN_PREC_FP64;
+  const bool f64e = is_f64e(precision);
+  if (f64e) {
+    for (auto& st : map->steps)
+      if (!st.small && (!st.bpl || st.bplanes != kF64eSlices || st.bfp16 != 2 || !map->amax))
+        return set_err(ctx, GTN_ERR_INVALID, "map was not created for the FP64-grade tensor-core precision");
+  }
+  const bool fp64 = precision == GTN_PREC_FP64 || f64e;  // complex FP64 running tensors
   const int P = tc ? nplanes_of(precision) : 0;
   void* bufs[2] = {map->buf0, map->buf1};
   const void* cur = x;
@@ -655,6 +683,42 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
                                        (int)st.N, st.b64, static_cast<double2*>(out), s);
         prof_end(s, GTN_KERNEL_SMALL, 8.0 * st.macs);
         ctx->launches++;
+      } else if (f64e) {
+        // integer digit planes of the running tensor (row maxima first), then the exact
+        // chunked digit-product GEMM straight into complex FP64
+        __nv_bfloat16* Apl = static_cast<__nv_bfloat16*>(map->abuf);
+        const int64_t pstride = st.M * 2 * st.Kp;
+        prof_begin(s);
+        if (st.tab.om) {
+          e = launch_rowmax_tab(cur, 1, st.tab, st.M, st.K, map->amax, s);
+          if (e == cudaSuccess)
+            e = launch_split_i7_tab(static_cast<const double2*>(cur), st.tab, st.M, st.K, st.Kp, pstride, map->amax,
+                                    Apl, s);
+        } else {
+          e = launch_rowmax_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, map->amax, s);
+          if (e == cudaSuccess)
+            e = launch_split_i7_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
+                                     map->amax, Apl, s);
+        }
+        prof_end(s, GTN_KERNEL_SPLIT, 0.0);
+        ctx->launches += 2;
+        if (e == cudaSuccess) {
+          F64eGemmArgs a;
+          a.A = Apl;
+          a.B = st.bpl;
+          a.C = static_cast<double2*>(out);
+          a.M = st.M;
+          a.N = st.N;
+          a.Kp = st.Kp;
+          a.a_max = map->amax;
+          a.b_max = st.bmax;
+          std::string why;
+          prof_begin(s);
+          e = launch_f64e_gemm(a, ctx->d_errflag, s, &why);
+          prof_end(s, GTN_KERNEL_TC_GEMM, 8.0 * st.macs);
+          ctx->launches++;
+          if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, "f64e_gemm: " + why + " " + cudaGetErrorString(e));
+        }
       } else {
         double2* A = static_cast<double2*>(map->abuf);
         prof_begin(s);

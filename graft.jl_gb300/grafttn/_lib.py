@@ -25,10 +25,11 @@ PREC_BF16X6 = 1
 PREC_BF16X3 = 2
 PREC_FP32 = 3
 PREC_FP16X3 = 4
+PREC_FP64E = 5
 KERNEL_NAMES = {0: "small_contract", 1: "gather", 2: "split_bf16", 3: "zgemm_simt", 4: "cgemm_simt",
                 5: "tc_gemm", 6: "convert", 7: "output_permute"}
 PRECISIONS = {"fp64": PREC_FP64, "bf16x6": PREC_BF16X6, "bf16x3": PREC_BF16X3, "fp32": PREC_FP32,
-              "fp16x3": PREC_FP16X3}
+              "fp16x3": PREC_FP16X3, "fp64e": PREC_FP64E}
 
 # Every symbol declared in include/grafttn.h, with (restype, argtypes).
 _p = C.c_void_p
@@ -51,6 +52,7 @@ SIGNATURES = {
     "gtn_map_apply": (_i, [_p, _p, _p]),
     "gtn_map_apply_prec": (_i, [_p, _i, _p, _p]),
     "gtn_map_apply_host": (_i, [_p, _p, _p]),
+    "gtn_map_set_fp64": (_i, [_p, _p]),
     "gtn_map_apply_profiled": (_i, [_p, _i, _p, _p, _i, _pd, _pi, _pd, _pi]),
     "gtn_map_info": (_i, [_p, _pi64, _pi64, _pd, _pi, _pi64]),
     "gtn_map_apply_batched": (_i, [_i, C.POINTER(_p), C.POINTER(_p), C.POINTER(_p), _i]),

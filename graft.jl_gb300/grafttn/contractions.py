@@ -354,6 +354,13 @@ class EffectiveMap:
             check(st, self.ctx.h, "lanczos")
         return E.value, x, dict(restarts=info[0], matvecs=info[1], converged=bool(info[2]), resid=res.value)
 
+    def set_fp64_map(self, other):
+        """Serve this map's FP64 applications (Rayleigh quotients, refinement residuals) with
+        `other`, an FP64 or "fp64e" map of the same shape (gtn_map_set_fp64); None resets."""
+        check(self.ctx.lib.gtn_map_set_fp64(self.h, other.h if other is not None else None), self.ctx.h,
+              "map_set_fp64")
+        self._fp64_map = other
+
     def vjp(self, x, ybar, slot):
         """Adjoint of operand `slot` (0 = x, 1.. = statics) of y = H_eff x at this x: the
         tensor G with <G, d op_slot> = <ybar, dy> (gtn_contract_vjp), in FP64."""
@@ -433,9 +440,12 @@ class EnvCache:
     (envcache.jl:812-844).  ``max_env_bytes`` bounds the cached bytes with least-recently-
     used eviction (envcache.jl:571-594); evicted environments are recomputed on demand."""
 
-    def __init__(self, topo, max_env_bytes=None):
+    def __init__(self, topo, max_env_bytes=None, precision="fp64"):
+        """``precision`` of the environment contractions: "fp64" (FP64 SIMT kernels) or
+        "fp64e" (the FP64-grade digit products on the tensor cores, about 1e-14)."""
         from collections import OrderedDict
         self.topo = topo
+        self.precision = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
         self.envs = OrderedDict()
         self.max_env_bytes = max_env_bytes
         self.bytes = 0
@@ -445,7 +455,7 @@ class EnvCache:
     def copy(self):
         """A cache holding the same environments (the device tensors are shared: an
         environment is never modified in place, only dropped and rebuilt)."""
-        c = EnvCache(self.topo, self.max_env_bytes)
+        c = EnvCache(self.topo, self.max_env_bytes, self.precision)
         c.envs.update(self.envs)
         c.bytes = self.bytes
         return c
@@ -479,7 +489,7 @@ class EnvCache:
             ops.append(psi.ctx.upload(np.ones((1, 1, 1))))
         ops += [W, A]
         order = choose_order([tuple(o.shape) for o in ops], labels, list(range(len(ops))))
-        E = psi.ctx.contract(ops, labels, conj, order)
+        E = psi.ctx.contract(ops, labels, conj, order, self.precision)
         self.envs[key] = E
         self.bytes += E.numel() * E.element_size()
         self.builds += 1

@@ -29,7 +29,7 @@ def refine_local(h2, E, v, refine_tol, max_outer=8, inner_dim=20, stats=None):
 
 def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10, tol=1e-10,
           krylovdim=20, precision="fp64", rq_fp64=None, lanczos_tol=1e-12, maxiter=100,
-          verbose=False, stats=None, refine="off", refine_tol=1e-8):
+          verbose=False, stats=None, refine="off", refine_tol=1e-8, fp64e=False):
     """Two-site DMRG; returns (psi, energies per sweep).  ``precision`` selects the map
     arithmetic.  With a mixed mode the energy that closes each sweep (the one returned and
     used for the convergence test) is the FP64 Rayleigh quotient of the last local
@@ -39,7 +39,11 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
     ``refine`` ("off", "last" or "all"; mixed modes only) refines the local eigenvectors of
     the sweep-closing solve or of every solve to FP64 accuracy (refine_local): the FP64
     residual |H v - E v| is brought below refine_tol * max(1, |E|), and the energy is the
-    FP64 Rayleigh quotient of the refined vector."""
+    FP64 Rayleigh quotient of the refined vector.
+
+    ``fp64e`` runs the FP64-accurate work of a mixed sweep on the tensor cores: environment
+    updates in GTN_PREC_FP64E, and the Rayleigh quotients and refinement residuals through
+    an FP64E twin of each local map (gtn_map_set_fp64)."""
     if not H.ishermitian:
         raise ValueError("dmrg2: DMRG requires ishermitian(H) == true")
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
@@ -47,7 +51,8 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
         rq_fp64 = prec != _lib.PREC_FP64
     trunc = trunc or TruncationScheme()
     t = psi.topo
-    cache = EnvCache(t)
+    use_e = fp64e and prec != _lib.PREC_FP64
+    cache = EnvCache(t, precision="fp64e" if use_e else "fp64")
     energies = []
     bonds = [n for n in t.postorder() if t.parent[n] >= 0]
     sched = [(n, "m") for n in bonds] + [(n, "n") for n in reversed(bonds)]
@@ -71,10 +76,14 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
             theta = two_site_tensor(psi, n, m)
             tt = mark("t_merge", tt)
             h2 = eff_h2(cache, psi, H, n, m, prec)
-            tt = mark("t_env_and_map", tt)
+            h2e = None
             last = step == len(sched) - 1 or (stats is not None and stats.get("max_steps") is not None
                                                and step == stats["max_steps"] - 1)
             do_refine = prec != _lib.PREC_FP64 and (refine == "all" or (refine == "last" and last))
+            if use_e and (do_refine or (rq_fp64 and last)):
+                h2e = eff_h2(cache, psi, H, n, m, _lib.PREC_FP64E)
+                h2.set_fp64_map(h2e)
+            tt = mark("t_env_and_map", tt)
             E, v, info = h2.lanczos_min(theta, krylovdim=krylovdim, tol=lanczos_tol, maxiter=maxiter,
                                         rq_fp64=rq_fp64 and last and not do_refine)
             tt = mark("t_lanczos", tt)
@@ -86,6 +95,8 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
                 stats["steps"] = stats.get("steps", 0) + 1
                 stats.setdefault("energies", []).append(E)
             h2.close()
+            if h2e is not None:
+                h2e.close()
             cache.invalidate_edge(n, m)
             split_two_site(psi, v, n, m, trunc, center_on)
             tt = mark("t_split", tt)

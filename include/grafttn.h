@@ -44,8 +44,13 @@ typedef enum {
   GTN_PREC_BF16X6 = 1,     /* tcgen05: 3 bf16 slices per operand, 6 products, FP32 accum */
   GTN_PREC_BF16X3 = 2,     /* tcgen05: 2 bf16 slices per operand, 3 products, FP32 accum */
   GTN_PREC_FP32 = 3,       /* complex FP32 SIMT kernels (diagnostic mode) */
-  GTN_PREC_FP16X3 = 4      /* tcgen05: 2 fp16 slices per operand (22 bits, power-of-two row
-                              scales), 3 products, FP32 accum; dense maps only */
+  GTN_PREC_FP16X3 = 4,     /* tcgen05: 2 fp16 slices per operand (22 bits, power-of-two row
+                              scales), 3 products, FP32 accum */
+  GTN_PREC_FP64E = 5       /* FP64-grade on the tensor cores: 7 integer base-128 digits per
+                              operand (power-of-two row scales), the 28 digit products of
+                              level <= 6 summed exactly in FP32 over chunks of 256 k and
+                              combined in double-float; about 1e-14 relative (dense maps and
+                              one-shot contractions) */
 } gtn_precision;
 
 typedef struct gtn_ctx_s* gtn_ctx;
@@ -85,6 +90,12 @@ int gtn_map_destroy(gtn_map map);
 /* y = H_eff x on device buffers (c128), in the map's default precision. */
 int gtn_map_apply(gtn_map map, const void* x, void* y);
 int gtn_map_apply_prec(gtn_map map, int precision, const void* x, void* y);
+/* Route this map's FP64 applications (the Rayleigh quotient of gtn_lanczos_min, the
+ * residuals of gtn_lanczos_refine, gtn_map_apply_prec with GTN_PREC_FP64) to fp64_map, an
+ * FP64 or GTN_PREC_FP64E map of the same shape (e.g. the FP64-grade tensor-core twin of a
+ * mixed map); NULL restores the map's own FP64 plan.  fp64_map is not owned: keep it alive
+ * while it is set.  No counterpart in the reference (its maps are FP64 only). */
+int gtn_map_set_fp64(gtn_map map, gtn_map fp64_map);
 /* Same with HOST buffers: host->device copy, apply, device->host copy (one call). */
 int gtn_map_apply_host(gtn_map map, const void* x_host, void* y_host);
 /* Shape/cost facts: elements of x and y, algorithmic FLOPs per apply (complex MAC = 8),

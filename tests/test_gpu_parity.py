@@ -45,18 +45,20 @@ def test_dmrg_star32_tfi(ctx, precision):
     assert abs(Es[-1] - E0) / abs(E0) < 1e-10
 
 
-@pytest.mark.parametrize("precision", ["fp64", "bf16x6", "fp16x3"])
-def test_dmrg_mps16_heisenberg_d256(ctx, precision):
+@pytest.mark.parametrize("precision,fp64e", [("fp64", False), ("bf16x6", False), ("fp16x3", False),
+                                             ("fp16x3", True)])
+def test_dmrg_mps16_heisenberg_d256(ctx, precision, fp64e):
     # 16-site Heisenberg chain at bond 256 (exact): the centre two-site splits are 512 x 512
     # and go through the Gram-matrix SVD; energy against sparse Lanczos of the full matrix.
     # The mixed modes refine every local eigenvector with FP64 residuals (gtn_lanczos_refine)
-    # and meet the FP64 bound, 1e-10 relative.
+    # and meet the FP64 bound, 1e-10 relative; with fp64e the environments, residuals and
+    # Rayleigh quotients run in the FP64-grade tensor-core precision.
     E0 = O.sparse_ground_energy(O.sparse_hamiltonian(O.heisenberg(O.mps_topology(16))))
     topo = G.mps_topology(16)
     psi = G.random_ttns(np.random.default_rng(3), topo, 2, 256, ctx=ctx)
     W = G.TTNO.from_hamiltonian(G.heisenberg(topo), ctx)
     _, Es = G.dmrg2(psi, W, G.TruncationScheme(maxdim=256), nsweeps=3, precision=precision,
-                    refine="off" if precision == "fp64" else "all")
+                    refine="off" if precision == "fp64" else "all", fp64e=fp64e)
     assert abs(Es[-1] - E0) / abs(E0) < 1e-10, (Es, E0)
     assert abs(psi.norm() - 1.0) < 1e-10
 

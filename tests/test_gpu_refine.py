@@ -78,3 +78,24 @@ def test_dmrg_step_mps63_d256_refined_vs_fp64(ctx):
     assert abs(Er - E64) / abs(E64) <= 1e-10, (Er, E64, Em)
     h64.close()
     hm.close()
+
+
+def test_refinement_with_fp64e_twin_matches_fp64(ctx):
+    # the residuals of the refinement through the FP64-grade tensor-core map (gtn_map_set_fp64)
+    psi, W, cache, n, m = local_problem(ctx, 63, 256, 7)
+    theta = two_site_tensor(psi, n, m)
+    h64 = eff_h2(cache, psi, W, n, m, "fp64")
+    E64, v64, _ = h64.lanczos_min(theta, krylovdim=20, tol=1e-10, maxiter=200)
+    hm = eff_h2(cache, psi, W, n, m, "fp16x3")
+    he = eff_h2(cache, psi, W, n, m, "fp64e")
+    hm.set_fp64_map(he)
+    Em, vm, _ = hm.lanczos_min(theta, krylovdim=20, tol=1e-10, maxiter=200)
+    Er, vr, info = hm.refine(vm, tol=1e-8 * abs(Em), max_outer=8)
+    assert info["converged"]
+    assert abs(Er - E64) / abs(E64) <= 1e-10, (Er, E64)
+    # the FP64E map agrees with the FP64 map on the refined vector
+    y64, ye = ctx.download(h64(vr)), ctx.download(he(vr))
+    assert np.linalg.norm(ye - y64) <= 1e-12 * np.linalg.norm(y64)
+    hm.close()
+    he.close()
+    h64.close()
