@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 namespace {
 
@@ -77,9 +78,19 @@ struct SplitWriter {
 
 // Element offsets of the rows m and columns k of a gather: decomposed through index groups,
 // or read from precomputed tables (dense maps, built once per plan step).
+// GrpOff refers to groups that already live in device-visible kernel parameters; it is built
+// inside a kernel and never passed to one (a host reference would make the device read host
+// memory, which Grace's coherent link allows silently, after the host may have freed it).
 struct GrpOff {
   const GroupSpec& mg;
   const GroupSpec& kg;
+  __device__ int64_t m(int64_t i) const { return decompose(i, mg); }
+  __device__ int64_t k(int64_t i) const { return decompose(i, kg); }
+};
+// The same with the groups held by value: the form a launch passes as a kernel parameter.
+struct GrpOffV {
+  GroupSpec mg;
+  GroupSpec kg;
   __device__ int64_t m(int64_t i) const { return decompose(i, mg); }
   __device__ int64_t k(int64_t i) const { return decompose(i, kg); }
 };
@@ -914,6 +925,7 @@ cudaError_t launch_split_c64(const float2* T, const GroupSpec& mg, const GroupSp
 template <typename Tin, class Off>
 static cudaError_t launch_rowmax(const Tin* T, const Off& off, int m_fast, int64_t M, int64_t K, float* amax,
                                  cudaStream_t s) {
+  static_assert(!std::is_same<Off, GrpOff>::value, "kernel parameters hold index groups by value (GrpOffV)");
   if (M <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(amax, 0, (size_t)M * sizeof(float), s);
   if (e != cudaSuccess || K <= 0) return e;
@@ -932,11 +944,11 @@ static cudaError_t launch_rowmax(const Tin* T, const Off& off, int m_fast, int64
 }
 cudaError_t launch_rowmax_c128(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
                                float* amax, cudaStream_t s) {
-  return launch_rowmax(T, GrpOff{mg, kg}, choose_m_fast(mg, kg) ? 1 : 0, M, K, amax, s);
+  return launch_rowmax(T, GrpOffV{mg, kg}, choose_m_fast(mg, kg) ? 1 : 0, M, K, amax, s);
 }
 cudaError_t launch_rowmax_c64(const float2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
                               float* amax, cudaStream_t s) {
-  return launch_rowmax(T, GrpOff{mg, kg}, choose_m_fast(mg, kg) ? 1 : 0, M, K, amax, s);
+  return launch_rowmax(T, GrpOffV{mg, kg}, choose_m_fast(mg, kg) ? 1 : 0, M, K, amax, s);
 }
 
 // ---- table-driven variants (offsets precomputed per plan step) --------------------------
