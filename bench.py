@@ -649,6 +649,26 @@ def dmrg_segment(ctx, steps, precision, D=1024, refine_tol=1e-8):
                              "matvecs": [r["matvecs"] for r in recs], "total_s": sum(r["s"] for r in recs),
                              "refine_fp64_matvecs": [r["refine_fp64_matvecs"] for r in recs],
                              "refine_mixed_matvecs": [r["refine_mixed_matvecs"] for r in recs]}
+        if prec == precision:
+            # the environment update after the split (the next step's env of the updated
+            # site), on this state in both precisions: time and agreement
+            nb = topo.parent[n0]
+            envs = {}
+            for eprec in ("fp64", "fp64e"):
+                ec = cache.copy()
+                ec.precision = G._lib.PRECISIONS[eprec]
+                ec.env(psi, H, n0, nb).shape  # warm-up (packing, arena growth)
+                ec.invalidate_edge(n0, nb)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                E = ec.env(psi, H, n0, nb)
+                torch.cuda.synchronize()
+                envs[eprec] = (time.perf_counter() - t0, ctx.download(E))
+            e64, ee = envs["fp64"][1], envs["fp64e"][1]
+            out["env_update"] = {"env": f"E({topo.ids[n0]}->{topo.ids[nb]}) [ket, op, bra] = {list(e64.shape)}",
+                                 "fp64_s": envs["fp64"][0], "fp64e_s": envs["fp64e"][0],
+                                 "speedup_fp64e": envs["fp64"][0] / envs["fp64e"][0],
+                                 "rel_diff": float(np.linalg.norm(ee - e64) / np.linalg.norm(e64))}
     r64 = out["runs"]["fp64"]
     rm = out["runs"][precision]
     out["rel_energy_vs_fp64"] = [abs(a - b) / abs(b) for a, b in zip(rm["energies"], r64["energies"])]
@@ -913,6 +933,9 @@ def main():
     ap.add_argument("--no-dmrg-segment", action="store_true",
                     help="leave out the bounded D=1024 dmrg2 segment (mixed vs FP64) of the default line")
     ap.add_argument("--segment-steps", type=int, default=1)
+    ap.add_argument("--tc-tuning", default="measured", choices=["measured", "ladder"],
+                    help="tile shapes of the tcgen05 steps: timed per problem class (default) or the fixed "
+                         "ladder (a fixed launch sequence, for profiler captures)")
     ap.add_argument("--dmrg", action="store_true", help="measure DMRG sweeps instead of map applications")
     ap.add_argument("--dmrg-topology", default="mps", choices=["mps", "binary"])
     ap.add_argument("--dmrg-sites", type=int, default=63)
@@ -941,6 +964,9 @@ def main():
             import torch
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
         dist.init_process_group(backend)
+    if args.impl != "reference" and args.tc_tuning != "measured":
+        from grafttn import _lib as GL
+        GL.tc_tuning(args.tc_tuning)
     try:
         if args.dmrg or args.grad or args.cbe or args.lanczos or args.svd:
             if rank == 0:

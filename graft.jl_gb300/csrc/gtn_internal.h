@@ -101,6 +101,18 @@ cudaError_t launch_split_tab(const void* T, int is64, const GatherTab& t, int64_
                              int nplanes, int64_t pstride, __nv_bfloat16* out, cudaStream_t s);
 cudaError_t launch_split16_tab(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
                                int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s);
+// One pass: row maxima (written to amax) and the slice planes together, a cluster of CTAs
+// per block of rows; *done = false when a row does not fit the clusters' shared memory.
+cudaError_t launch_split16_rows_tab(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                                    int64_t pstride, float* amax, __nv_bfloat16* out, cudaStream_t s, bool* done);
+cudaError_t launch_split16_rows_grp(const void* T, int is64, const GroupSpec& mg, const GroupSpec& kg, int64_t M,
+                                    int64_t K, int64_t Kp, int64_t pstride, float* amax, __nv_bfloat16* out,
+                                    cudaStream_t s, bool* done);
+cudaError_t launch_split_i7_rows_tab(const double2* T, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                                     int64_t pstride, float* amax, __nv_bfloat16* out, cudaStream_t s, bool* done);
+cudaError_t launch_split_i7_rows_grp(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                                     int64_t Kp, int64_t pstride, float* amax, __nv_bfloat16* out, cudaStream_t s,
+                                     bool* done);
 cudaError_t launch_gather_tab_to_c128(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t ldo,
                                       double2* out, cudaStream_t s);
 // fp16 slice planes (2 planes, hi + lo) of a K-major gather, rows scaled by

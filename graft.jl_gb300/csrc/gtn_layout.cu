@@ -5,6 +5,7 @@
 #include "gtn_internal.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 
@@ -279,19 +280,35 @@ __device__ __forceinline__ void split16(double x, __half* h, __half* l) {
 __device__ __forceinline__ float absmax2(float2 v) { return fmaxf(fabsf(v.x), fabsf(v.y)); }
 __device__ __forceinline__ float absmax2(double2 v) { return (float)fmax(fabs(v.x), fabs(v.y)); }
 
+// Element (m, k) as two fp16 planes, the row scaled by fp16_row_scale of its maximum.
+template <typename Tin>
+__device__ __forceinline__ void put16(__half* out, int64_t ld2, int64_t pstride, int64_t m, int64_t k, Tin v,
+                                      float rowmax) {
+  const float s = fp16_row_scale(rowmax);
+  __half2 hi, lo;
+  split16(v.x * s, &hi.x, &lo.x);
+  split16(v.y * s, &hi.y, &lo.y);
+  __half2* row = reinterpret_cast<__half2*>(out + m * ld2 + 2 * k);
+  row[0] = hi;
+  *reinterpret_cast<__half2*>(reinterpret_cast<__half*>(row) + pstride) = lo;
+}
+
 struct Split16Writer {
   __half* out;
   int64_t ld2;      // row pitch in halves (= 2*Kp)
   int64_t pstride;  // plane pitch in halves
   const float* amax;
   template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v) const {
-    const float s = fp16_row_scale(amax[m]);
-    __half2 hi, lo;
-    split16(v.x * s, &hi.x, &lo.x);
-    split16(v.y * s, &hi.y, &lo.y);
-    __half2* row = reinterpret_cast<__half2*>(out + m * ld2 + 2 * k);
-    row[0] = hi;
-    *reinterpret_cast<__half2*>(reinterpret_cast<__half*>(row) + pstride) = lo;
+    put16(out, ld2, pstride, m, k, v, amax[m]);
+  }
+};
+// The same, handed the row maximum (the fused split computes it in shared memory).
+struct Split16RowWriter {
+  __half* out;
+  int64_t ld2;
+  int64_t pstride;
+  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v, float rowmax) const {
+    put16(out, ld2, pstride, m, k, v, rowmax);
   }
 };
 
@@ -332,24 +349,39 @@ __device__ __forceinline__ void i7_digits(double x, int k, __nv_bfloat16* d) {
 }
 __device__ __forceinline__ void i7_digits(float x, int k, __nv_bfloat16* d) { i7_digits((double)x, k, d); }
 
+// Element (m, k) as kF64eSlices digit planes, the row scaled by 2^k of its maximum.
+template <typename Tin>
+__device__ __forceinline__ void put_i7(__nv_bfloat16* out, int64_t ld2, int64_t pstride, int64_t m, int64_t k,
+                                       Tin v, float rowmax) {
+  const int e = f64e_row_exp(rowmax);
+  __nv_bfloat16 dr[kF64eSlices], di[kF64eSlices];
+  i7_digits(v.x, e, dr);
+  i7_digits(v.y, e, di);
+  __nv_bfloat16* row = out + m * ld2 + 2 * k;
+#pragma unroll
+  for (int p = 0; p < kF64eSlices; ++p) {
+    __nv_bfloat162 pr;
+    pr.x = dr[p];
+    pr.y = di[p];
+    *reinterpret_cast<__nv_bfloat162*>(row + p * pstride) = pr;
+  }
+}
+
 struct Int7Writer {
   __nv_bfloat16* out;
   int64_t ld2;      // row pitch (= 2 Kp)
   int64_t pstride;  // plane pitch
   const float* amax;
   template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v) const {
-    const int e = f64e_row_exp(amax[m]);
-    __nv_bfloat16 dr[kF64eSlices], di[kF64eSlices];
-    i7_digits(v.x, e, dr);
-    i7_digits(v.y, e, di);
-    __nv_bfloat16* row = out + m * ld2 + 2 * k;
-#pragma unroll
-    for (int p = 0; p < kF64eSlices; ++p) {
-      __nv_bfloat162 pr;
-      pr.x = dr[p];
-      pr.y = di[p];
-      *reinterpret_cast<__nv_bfloat162*>(row + p * pstride) = pr;
-    }
+    put_i7(out, ld2, pstride, m, k, v, amax[m]);
+  }
+};
+struct Int7RowWriter {
+  __nv_bfloat16* out;
+  int64_t ld2;
+  int64_t pstride;
+  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v, float rowmax) const {
+    put_i7(out, ld2, pstride, m, k, v, rowmax);
   }
 };
 
@@ -733,6 +765,205 @@ __global__ void __launch_bounds__(256) block_rowmax_kernel(const DevGatherJob* _
                             static_cast<float*>(bases.buf[5]) + J.amax_off, m0, k0);
 }
 
+
+// ---- fused split: row maxima and slice planes in one pass over the running tensor --------
+// A cluster of cs CTAs owns TR rows of the K-major view; CTA r of the cluster stages the
+// columns [r kc, (r + 1) kc) of those rows in shared memory (cp.async, every element read
+// from HBM once), reduces its partial row maxima, and reads its peers' partial maxima
+// through distributed shared memory after a cluster barrier.  It then writes its columns
+// of the slice planes, scaled by the full row maxima, and the cluster's rank 0 writes them
+// to amax[] for the GEMM epilogue.  The second cluster barrier (arrive after the peer
+// reads, wait before exit) keeps each CTA's partial maxima alive while peers read them.
+// The barriers are hardware cluster barriers: every CTA of a cluster is co-scheduled and
+// every thread reaches both, so no wait can be left hanging.
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
+__device__ __forceinline__ float ld_peer_f32(const float* p, uint32_t rank) {
+  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
+  uint32_t ra;
+  float v;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(ra) : "memory");
+  return v;
+}
+__device__ __forceinline__ void cp_async_el(float2* dst, const float2* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_el(double2* dst, const double2* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <typename Tin> __host__ __device__ constexpr int split_rows_pitch(int kc) { return kc | 1; }
+template <typename Tin> __host__ __device__ constexpr size_t split_rows_smem(int TR, int kc) {
+  return (size_t)TR * split_rows_pitch<Tin>(kc) * sizeof(Tin) + (size_t)kc * 8 + (size_t)TR * 8 + (size_t)TR * 8;
+}
+
+template <typename Tin, int TR, class Off, class W>
+__global__ void __launch_bounds__(256) split_rows_kernel(const Tin* __restrict__ T, Off off, int64_t M, int64_t K,
+                                                         int64_t Kp, int kc, int cs, int m_fast, W w,
+                                                         float* __restrict__ amax) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int pitch = split_rows_pitch<Tin>(kc);  // odd: the row-strided staging stores spread over banks
+  Tin* tile = reinterpret_cast<Tin*>(smraw);
+  int64_t* offK = reinterpret_cast<int64_t*>(tile + TR * pitch);
+  int64_t* offM = offK + kc;
+  float* pmax = reinterpret_cast<float*>(offM + TR);
+  float* rmax = pmax + TR;
+  const int tid = threadIdx.x;
+  const uint32_t rank = cs > 1 ? cluster_rank() : 0u;
+  const int64_t m0 = (int64_t)(blockIdx.x / cs) * TR;
+  const int64_t k0 = (int64_t)rank * kc;
+  const int kv = (int)max((int64_t)0, min((int64_t)kc, K - k0));   // columns read
+  const int kw = (int)max((int64_t)0, min((int64_t)kc, Kp - k0));  // columns written (zero padding to Kp)
+  for (int i = tid; i < kv; i += 256) offK[i] = off.k(k0 + i);
+  if (tid < TR) offM[tid] = m0 + tid < M ? off.m(m0 + tid) : 0;
+  __syncthreads();
+  if (m_fast) {  // consecutive threads on consecutive rows (the unit-stride index is in M)
+    for (int e = tid; e < TR * kv; e += 256) {
+      const int im = e % TR, ik = e / TR;
+      Tin* d = tile + im * pitch + ik;
+      if (m0 + im < M) cp_async_el(d, T + offM[im] + offK[ik]);
+      else *d = Zero<Tin>::v();
+    }
+  } else {
+    for (int r = 0; r < TR; ++r) {
+      const bool live = m0 + r < M;
+      for (int c = tid; c < kv; c += 256) {
+        Tin* d = tile + r * pitch + c;
+        if (live) cp_async_el(d, T + offM[r] + offK[c]);
+        else *d = Zero<Tin>::v();
+      }
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int r = warp; r < TR; r += 8) {
+    float x = 0.f;
+    for (int c = lane; c < kv; c += 32) x = fmaxf(x, absmax2(tile[r * pitch + c]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (lane == 0) pmax[r] = x;
+  }
+  if (cs > 1) {
+    cluster_sync_all();  // every CTA's partial maxima are in its shared memory
+    if (tid < TR) {
+      float x = 0.f;
+      for (int q = 0; q < cs; ++q) x = fmaxf(x, ld_peer_f32(pmax + tid, (uint32_t)q));
+      rmax[tid] = x;
+    }
+    cluster_arrive_relaxed();  // done reading the peers
+    __syncthreads();
+  } else {
+    __syncthreads();
+    if (tid < TR) rmax[tid] = pmax[tid];
+    __syncthreads();
+  }
+  if (rank == 0 && tid < TR && m0 + tid < M) amax[m0 + tid] = rmax[tid];
+  for (int r = 0; r < TR; ++r) {
+    const int64_t m = m0 + r;
+    if (m >= M) break;
+    const float rm = rmax[r];
+    for (int c = tid; c < kw; c += 256) w(m, k0 + c, c < kv ? tile[r * pitch + c] : Zero<Tin>::v(), rm);
+  }
+  if (cs > 1) cluster_wait();  // peers may read this CTA's maxima until they have arrived
+}
+
+// Rows per cluster, cluster size and columns per CTA of the fused split, or false when a
+// row of the view does not fit in 8 CTAs' shared memory (the two-kernel path runs then).
+// Rows: 32, 16 or 8 (at least 16 when the rows are the unit-stride index, for 128-byte runs);
+// the smallest cluster whose CTAs stay under the budget that lets two CTAs share an SM.
+template <typename Tin>
+bool split_rows_shape(int64_t K, int64_t Kp, int m_fast, int* TR, int* cs, int* kc, size_t* smem) {
+  constexpr size_t kBudget = 112 * 1024;
+  const int trs[3] = {32, 16, 8};
+  for (int t : trs) {
+    if (m_fast && t < 16) break;
+    for (int c = 1; c <= 8; ++c) {
+      const int64_t k = ((Kp + c - 1) / c + 7) / 8 * 8;
+      if (c > 1 && (c - 1) * k >= Kp) break;  // every rank holds columns
+      const size_t b = split_rows_smem<Tin>(t, (int)k);
+      if (b <= kBudget) {
+        *TR = t;
+        *cs = c;
+        *kc = (int)k;
+        *smem = b;
+        return true;
+      }
+    }
+  }
+  return false;
+}
+
+template <typename Tin, int TR, class Off, class W>
+cudaError_t launch_split_rows_t(const Tin* T, const Off& off, int64_t M, int64_t K, int64_t Kp, int kc, int cs,
+                                int m_fast, const W& w, float* amax, size_t smem, cudaStream_t s) {
+  auto kern = split_rows_kernel<Tin, TR, Off, W>;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const int64_t tiles = (M + TR - 1) / TR;
+  if (tiles * cs > 2147483647LL) return cudaErrorInvalidConfiguration;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(tiles * cs), 1, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attrs[1];
+  attrs[0].id = cudaLaunchAttributeClusterDimension;
+  attrs[0].val.clusterDim.x = (unsigned)cs;
+  attrs[0].val.clusterDim.y = 1;
+  attrs[0].val.clusterDim.z = 1;
+  cfg.attrs = attrs;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, T, off, M, K, Kp, kc, cs, m_fast, w, amax);
+}
+
+template <typename Tin, class Off, class W>
+cudaError_t launch_split_rows(const Tin* T, const Off& off, int64_t M, int64_t K, int64_t Kp, int m_fast,
+                              const W& w, float* amax, cudaStream_t s, bool* done) {
+  static_assert(!std::is_same<Off, GrpOff>::value, "kernel parameters hold index groups by value (GrpOffV)");
+  *done = false;
+  const char* env = std::getenv("GTN_FUSED_SPLIT");
+  if ((env && env[0] == '0') || M <= 0 || K <= 0) return cudaSuccess;
+  int TR = 0, cs = 0, kc = 0;
+  size_t smem = 0;
+  if (!split_rows_shape<Tin>(K, Kp, m_fast, &TR, &cs, &kc, &smem)) return cudaSuccess;
+  cudaError_t e;
+  if (TR == 32) e = launch_split_rows_t<Tin, 32>(T, off, M, K, Kp, kc, cs, m_fast, w, amax, smem, s);
+  else if (TR == 16) e = launch_split_rows_t<Tin, 16>(T, off, M, K, Kp, kc, cs, m_fast, w, amax, smem, s);
+  else e = launch_split_rows_t<Tin, 8>(T, off, M, K, Kp, kc, cs, m_fast, w, amax, smem, s);
+  if (e == cudaSuccess) {
+    *done = true;
+    return e;
+  }
+  // a cluster shape the device cannot schedule is a launch-configuration error (nothing ran):
+  // clear it and let the caller take the two-kernel path
+  if (e == cudaErrorInvalidClusterSize || e == cudaErrorInvalidConfiguration || e == cudaErrorInvalidValue) {
+    cudaGetLastError();
+    return cudaSuccess;
+  }
+  return e;
+}
+
 }  // namespace
 
 cudaError_t launch_block_rowmax(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
@@ -970,6 +1201,35 @@ cudaError_t launch_split16_tab(const void* T, int is64, const GatherTab& t, int6
   const Split16Writer w{reinterpret_cast<__half*>(out), 2 * Kp, pstride, amax};
   return is64 ? launch_gather_tab(static_cast<const double2*>(T), t.om, t.ok, M, K, Kp, t.m_fast, w, s)
               : launch_gather_tab(static_cast<const float2*>(T), t.om, t.ok, M, K, Kp, t.m_fast, w, s);
+}
+// Fused one-pass split (row maxima through cluster shared memory), table or group offsets;
+// *done = false when the view's rows do not fit (the caller runs rowmax + split instead).
+cudaError_t launch_split16_rows_tab(const void* T, int is64, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                                    int64_t pstride, float* amax, __nv_bfloat16* out, cudaStream_t s, bool* done) {
+  const Split16RowWriter w{reinterpret_cast<__half*>(out), 2 * Kp, pstride};
+  const TabOff off{t.om, t.ok};
+  return is64 ? launch_split_rows(static_cast<const double2*>(T), off, M, K, Kp, t.m_fast, w, amax, s, done)
+              : launch_split_rows(static_cast<const float2*>(T), off, M, K, Kp, t.m_fast, w, amax, s, done);
+}
+cudaError_t launch_split16_rows_grp(const void* T, int is64, const GroupSpec& mg, const GroupSpec& kg, int64_t M,
+                                    int64_t K, int64_t Kp, int64_t pstride, float* amax, __nv_bfloat16* out,
+                                    cudaStream_t s, bool* done) {
+  const Split16RowWriter w{reinterpret_cast<__half*>(out), 2 * Kp, pstride};
+  const GrpOffV off{mg, kg};
+  const int mf = choose_m_fast(mg, kg) ? 1 : 0;
+  return is64 ? launch_split_rows(static_cast<const double2*>(T), off, M, K, Kp, mf, w, amax, s, done)
+              : launch_split_rows(static_cast<const float2*>(T), off, M, K, Kp, mf, w, amax, s, done);
+}
+cudaError_t launch_split_i7_rows_tab(const double2* T, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
+                                     int64_t pstride, float* amax, __nv_bfloat16* out, cudaStream_t s, bool* done) {
+  return launch_split_rows(T, TabOff{t.om, t.ok}, M, K, Kp, t.m_fast, Int7RowWriter{out, 2 * Kp, pstride}, amax, s,
+                           done);
+}
+cudaError_t launch_split_i7_rows_grp(const double2* T, const GroupSpec& mg, const GroupSpec& kg, int64_t M, int64_t K,
+                                     int64_t Kp, int64_t pstride, float* amax, __nv_bfloat16* out, cudaStream_t s,
+                                     bool* done) {
+  return launch_split_rows(T, GrpOffV{mg, kg}, M, K, Kp, choose_m_fast(mg, kg) ? 1 : 0,
+                           Int7RowWriter{out, 2 * Kp, pstride}, amax, s, done);
 }
 cudaError_t launch_split_i7_tab(const double2* T, const GatherTab& t, int64_t M, int64_t K, int64_t Kp,
                                int64_t pstride, const float* amax, __nv_bfloat16* out, cudaStream_t s) {

@@ -689,19 +689,28 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
         __nv_bfloat16* Apl = static_cast<__nv_bfloat16*>(map->abuf);
         const int64_t pstride = st.M * 2 * st.Kp;
         prof_begin(s);
-        if (st.tab.om) {
-          e = launch_rowmax_tab(cur, 1, st.tab, st.M, st.K, map->amax, s);
-          if (e == cudaSuccess)
-            e = launch_split_i7_tab(static_cast<const double2*>(cur), st.tab, st.M, st.K, st.Kp, pstride, map->amax,
-                                    Apl, s);
-        } else {
-          e = launch_rowmax_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, map->amax, s);
-          if (e == cudaSuccess)
-            e = launch_split_i7_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
-                                     map->amax, Apl, s);
+        bool fused = false;
+        if (st.tab.om)
+          e = launch_split_i7_rows_tab(static_cast<const double2*>(cur), st.tab, st.M, st.K, st.Kp, pstride,
+                                       map->amax, Apl, s, &fused);
+        else
+          e = launch_split_i7_rows_grp(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
+                                       map->amax, Apl, s, &fused);
+        if (e == cudaSuccess && !fused) {  // rows too long for the clusters: maxima first, then the split
+          if (st.tab.om) {
+            e = launch_rowmax_tab(cur, 1, st.tab, st.M, st.K, map->amax, s);
+            if (e == cudaSuccess)
+              e = launch_split_i7_tab(static_cast<const double2*>(cur), st.tab, st.M, st.K, st.Kp, pstride,
+                                      map->amax, Apl, s);
+          } else {
+            e = launch_rowmax_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, map->amax, s);
+            if (e == cudaSuccess)
+              e = launch_split_i7_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
+                                       map->amax, Apl, s);
+          }
         }
         prof_end(s, GTN_KERNEL_SPLIT, 0.0);
-        ctx->launches += 2;
+        ctx->launches += fused ? 1 : 2;
         if (e == cudaSuccess) {
           F64eGemmArgs a;
           a.A = Apl;
@@ -772,38 +781,50 @@ int map_run(gtn_map map, int precision, const double2* x, double2* y) {
         const int64_t pstride = st.M * 2 * st.Kp;
         const bool f16 = is_fp16(precision);
         prof_begin(s);
-        if (st.tab.om) {
-          // offsets from the step's tables
-          if (f16) {
-            e = launch_rowmax_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, map->amax, s);
-            if (e == cudaSuccess)
-              e = launch_split16_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, st.Kp, pstride, map->amax, Apl, s);
+        bool fused = false;
+        if (f16) {  // one pass: row maxima and fp16 planes together
+          if (st.tab.om)
+            e = launch_split16_rows_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, st.Kp, pstride, map->amax, Apl, s,
+                                        &fused);
+          else
+            e = launch_split16_rows_grp(cur, cur64 ? 1 : 0, st.mg, st.kg, st.M, st.K, st.Kp, pstride, map->amax, Apl,
+                                        s, &fused);
+          if (fused) ctx->launches++;
+        }
+        if (e == cudaSuccess && !fused) {  // two passes: row maxima (fp16 planes only), then the split
+          if (st.tab.om) {
+            // offsets from the step's tables
+            if (f16) {
+              e = launch_rowmax_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, map->amax, s);
+              if (e == cudaSuccess)
+                e = launch_split16_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, st.Kp, pstride, map->amax, Apl, s);
+              ctx->launches += 2;
+            } else {
+              e = launch_split_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, st.Kp, P, pstride, Apl, s);
+              ctx->launches++;
+            }
+          } else if (f16) {
+            // fp16 planes: per-row maxima first, then the scaled two-slice split
+            if (cur64)
+              e = launch_rowmax_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, map->amax, s);
+            else
+              e = launch_rowmax_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, map->amax, s);
+            if (e == cudaSuccess && cur64)
+              e = launch_split16_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
+                                      map->amax, Apl, s);
+            else if (e == cudaSuccess)
+              e = launch_split16_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
+                                     map->amax, Apl, s);
             ctx->launches += 2;
+          } else if (cur64) {
+            e = launch_split_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
+                                  pstride, Apl, s);
+            ctx->launches++;
           } else {
-            e = launch_split_tab(cur, cur64 ? 1 : 0, st.tab, st.M, st.K, st.Kp, P, pstride, Apl, s);
+            e = launch_split_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
+                                 pstride, Apl, s);
             ctx->launches++;
           }
-        } else if (f16) {
-          // fp16 planes: per-row maxima first, then the scaled two-slice split
-          if (cur64)
-            e = launch_rowmax_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, map->amax, s);
-          else
-            e = launch_rowmax_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, map->amax, s);
-          if (e == cudaSuccess && cur64)
-            e = launch_split16_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
-                                    map->amax, Apl, s);
-          else if (e == cudaSuccess)
-            e = launch_split16_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, pstride,
-                                   map->amax, Apl, s);
-          ctx->launches += 2;
-        } else if (cur64) {
-          e = launch_split_c128(static_cast<const double2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
-                                pstride, Apl, s);
-          ctx->launches++;
-        } else {
-          e = launch_split_c64(static_cast<const float2*>(cur), st.mg, st.kg, st.M, st.K, st.Kp, P,
-                               pstride, Apl, s);
-          ctx->launches++;
         }
         prof_end(s, GTN_KERNEL_SPLIT, 0.0);
         if (e == cudaSuccess) {
