@@ -475,6 +475,12 @@ def run_ours(args, rank, world):
             segment = dmrg_segment(ctx, args.segment_steps, args.precision)
         except Exception as exc:  # reported, never hides the headline
             segment = {"error": f"{type(exc).__name__}: {exc}"}
+    gradient = None
+    if not args.skip_extra:
+        try:
+            gradient = grad_segment(ctx, args.grad_D, tuple(args.grad_precisions.split(",")))
+        except Exception as exc:  # reported, never hides the headline
+            gradient = {"error": f"{type(exc).__name__}: {exc}"}
 
     extra = {}
     alt = {}
@@ -570,6 +576,8 @@ def run_ours(args, rank, world):
     }
     if segment is not None:
         line["dmrg_segment"] = segment
+    if gradient is not None:
+        line["gradient"] = gradient
     line.update(extra)
     print(json.dumps(line), flush=True)
     if not parity_ok:
@@ -813,55 +821,62 @@ def run_svd(args):
     print(json.dumps(out), flush=True)
 
 
-def run_grad(args):
+def grad_segment(ctx, D=128, precisions=("fp64", "fp16x3")):
     """Gradient workload: XXZ (Delta = 0.7) on binary_topology(4) (31 sites) at bond
-    dimension --grad-D with per-edge couplings theta_e ~ U(0.5, 1.5): wall time of the
-    gradient with respect to every site tensor (one eff_h1 application per node) and every
-    coupling (one two-site expectation per edge), plus the identities <A_n, g_n> = E and
-    sum_e theta_e dE/dtheta_e = E and central finite differences (h = 1e-6) on a sample."""
+    dimension D with per-edge couplings theta_e ~ U(0.5, 1.5): wall time of the gradient with
+    respect to every site tensor (one eff_h1 application per node) and every coupling, the
+    latter both through the adjoint of the TTNO operand (gtn_contract_vjp, chain rule through
+    W(theta)) and as two-site expectation values; the identities <A_n, g_n> = E and
+    sum_e theta_e dE/dtheta_e = E; central finite differences (h = 1e-6) on a sample."""
     import torch
     import grafttn as G
     from grafttn import gradients as GR
-    ctx = G.default_context(0)
     topo = G.binary_topology(4)
     rng = np.random.default_rng(11)
     theta = {e: float(rng.uniform(0.5, 1.5)) for e in topo.edges()}
     S = G.spin_ops()
     terms = {e: [(1.0, S["X"], S["X"]), (1.0, S["Y"], S["Y"]), (0.7, S["Z"], S["Z"])] for e in topo.edges()}
+    dco = {e: [1.0, 1.0, 0.7] for e in topo.edges()}
 
     def ttno(th):
         return G.TTNO.from_hamiltonian(G.xxz(topo, th, 0.7), ctx)
-    H = ttno(theta)
+    Hnn = G.xxz(topo, theta, 0.7)
+    H = G.TTNO.from_hamiltonian(Hnn, ctx)
     bond = {}
     for c in range(topo.nnodes):
         if topo.parent[c] >= 0:
             below = len(topo.subtree_nodes(c, topo.parent[c]))
-            bond[c] = int(min(args.grad_D, 2 ** below, 2 ** (topo.nnodes - below)))
+            bond[c] = int(min(D, 2 ** below, 2 ** (topo.nnodes - below)))
     psi = G.random_ttns(rng, topo, 2, bond, ctx=ctx)
     E = GR.energy(psi, H).real
-    out = {"metric": "gradient time", "unit": "s", "topology": "binary31", "bond_dim": args.grad_D,
-           "model": "XXZ Delta=0.7, theta_e ~ U(0.5,1.5)", "energy": E, "runs": {}}
-    for prec in args.grad_precisions.split(","):
+    out = {"workload": f"binary31 XXZ Delta=0.7, theta_e ~ U(0.5,1.5), D={D}, random normalised state",
+           "energy": E, "site_gradients": {}}
+    for prec in precisions:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         grads = GR.site_gradients(psi, H, precision=prec)
         torch.cuda.synchronize()
         t_sites = time.perf_counter() - t0
         closure = max(abs(ctx.dot(psi.tensors[n], grads[n]) - E) for n in range(topo.nnodes)) / abs(E)
-        out["runs"][prec] = {"site_gradients_s": t_sites, "max_rel_closure": closure}
+        out["site_gradients"][prec] = {"s": t_sites, "max_rel_closure": closure}
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g_adj = GR.coupling_gradients_adjoint(psi, H, Hnn, dco)
+    torch.cuda.synchronize()
+    out["coupling_gradients_adjoint_s"] = time.perf_counter() - t0
     t0 = time.perf_counter()
     g_theta = GR.coupling_gradients(psi, terms)
     torch.cuda.synchronize()
-    out["coupling_gradients_s"] = time.perf_counter() - t0
-    out["linearity_rel_err"] = abs(sum(theta[e] * g_theta[e] for e in theta) - E) / abs(E)
+    out["coupling_gradients_expectation_s"] = time.perf_counter() - t0
+    out["adjoint_vs_expectation_max_rel"] = max(abs(g_adj[e] - g_theta[e]) / max(1.0, abs(g_theta[e])) for e in theta)
+    out["linearity_rel_err"] = abs(sum(theta[e] * g_adj[e] for e in theta) - E) / abs(E)
     h, fd_err = 1e-6, 0.0
     for e in list(topo.edges())[:3]:
         tp, tm = dict(theta), dict(theta)
         tp[e] += h
         tm[e] -= h
         fd = (GR.energy(psi, ttno(tp)).real - GR.energy(psi, ttno(tm)).real) / (2 * h)
-        fd_err = max(fd_err, abs(fd - g_theta[e]) / max(1.0, abs(g_theta[e])))
+        fd_err = max(fd_err, abs(fd - g_adj[e]) / max(1.0, abs(g_adj[e])))
     grads = GR.site_gradients(psi, H)
     for n in [0, topo.nnodes - 1]:
         A = psi.tensors[n]
@@ -873,6 +888,16 @@ def run_grad(args):
         an = 2 * ctx.dot(Dn, grads[n]).real
         fd_err = max(fd_err, abs(fd - an) / max(1.0, abs(an)))
     out["max_fd_rel_err"] = fd_err
+    out["fd_sample"] = "3 couplings (h = 1e-6) and 2 site tensors along random directions"
+    return out
+
+
+def run_grad(args):
+    """The gradient workload alone at --grad-D (see grad_segment)."""
+    import grafttn as G
+    ctx = G.default_context(0)
+    out = {"metric": "gradient time", "unit": "s", "bond_dim": args.grad_D}
+    out.update(grad_segment(ctx, args.grad_D, tuple(args.grad_precisions.split(","))))
     print(json.dumps(out), flush=True)
 
 
@@ -948,7 +973,7 @@ def main():
                     help="time one mid-chain Lanczos solve of mps63 at --dmrg-D against one map application")
     ap.add_argument("--grad", action="store_true", help="measure the gradient workload (bin31 XXZ)")
     ap.add_argument("--grad-D", type=int, default=128)
-    ap.add_argument("--grad-precisions", default="fp64,bf16x6")
+    ap.add_argument("--grad-precisions", default="fp64,fp16x3")
     ap.add_argument("--cbe", action="store_true", help="measure TDVP1_CBE steps (85-site 4-ary TFI)")
     ap.add_argument("--cbe-maxdim", type=int, default=32)
     ap.add_argument("--cbe-steps", type=int, default=5)

@@ -258,6 +258,13 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  // inverse fp16 scales of the tile's complex columns, read once here instead of per output
+  __shared__ float s_binv[BN / 2 > 0 ? BN / 2 : 1];
+  if (sc.bmax)
+    for (int t = threadIdx.x; t < BN / 2; t += blockDim.x) {
+      const int64_t n = (int64_t)(r0 >> 1) + t;
+      s_binv[t] = n < N ? fp16_row_scale_inv(sc.bmax[n]) : 1.0f;
+    }
   fence_before();
   __syncthreads();
   fence_after();
@@ -331,7 +338,7 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
     const uint32_t taddr = tmem_d + ((uint32_t)(warp * 32) << 16);
     bool has_corr = false;
     for (int q = 0; q < prods.n; ++q) has_corr |= !(prods.a[q] == 0 && prods.b[q] == 0);
-    const float ainv = (sc.amax && m < M) ? 1.0f / fp16_row_scale(sc.amax[m]) : 1.0f;
+    const float ainv = (sc.amax && m < M) ? fp16_row_scale_inv(sc.amax[m]) : 1.0f;
 #pragma unroll 1
     for (int c = 0; c < BN; c += 16) {
       uint32_t v[16], w[16];
@@ -348,7 +355,7 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
         for (int j = 0; j < 8; ++j) {
           const int64_t n = nb + j;
           if (n < N) {
-            const float f = sc.bmax ? ainv / fp16_row_scale(sc.bmax[n]) : ainv;
+            const float f = sc.bmax ? ainv * s_binv[(c >> 1) + j] : ainv;
             C[n * M + m] = make_float2((__uint_as_float(v[2 * j]) + __uint_as_float(w[2 * j])) * f,
                                        (__uint_as_float(v[2 * j + 1]) + __uint_as_float(w[2 * j + 1])) * f);
           }
@@ -523,6 +530,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
   }
+  // inverse fp16 scales of the pair's complex columns (every CTA writes all TILE_N columns)
+  __shared__ float s_binv[CF::TILE_N / 2];
+  if (sc.bmax)
+    for (int t = threadIdx.x; t < CF::TILE_N / 2; t += blockDim.x) {
+      const int64_t n = (int64_t)(n0 >> 1) + t;
+      s_binv[t] = n < N ? fp16_row_scale_inv(sc.bmax[n]) : 1.0f;
+    }
   fence_before();
   __syncthreads();
   cluster_sync();  // both CTAs' barriers exist before either side signals the other's
@@ -605,7 +619,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
     const uint32_t taddr = tmem_d + ((uint32_t)(warp * 32) << 16);
     bool has_corr = false;
     for (int q = 0; q < prods.n; ++q) has_corr |= !(prods.a[q] == 0 && prods.b[q] == 0);
-    const float ainv = (sc.amax && m < M) ? 1.0f / fp16_row_scale(sc.amax[m]) : 1.0f;
+    const float ainv = (sc.amax && m < M) ? fp16_row_scale_inv(sc.amax[m]) : 1.0f;
 #pragma unroll 1
     for (int c = 0; c < CF::TILE_N; c += 16) {
       uint32_t v[16], w[16];
@@ -622,7 +636,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
         for (int j = 0; j < 8; ++j) {
           const int64_t n = nb + j;
           if (n < N) {
-            const float f = sc.bmax ? ainv / fp16_row_scale(sc.bmax[n]) : ainv;
+            const float f = sc.bmax ? ainv * s_binv[(c >> 1) + j] : ainv;
             C[n * M + m] = make_float2((__uint_as_float(v[2 * j]) + __uint_as_float(w[2 * j])) * f,
                                        (__uint_as_float(v[2 * j + 1]) + __uint_as_float(w[2 * j + 1])) * f);
           }
@@ -732,6 +746,7 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
   __shared__ __align__(8) uint64_t empty_bar[CF::STAGES];
   __shared__ __align__(8) uint64_t accf_bar[2];
   __shared__ __align__(8) uint64_t acce_bar[2];
+  __shared__ float s_binv[4][BN / 2 > 0 ? BN / 2 : 1];
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
   __shared__ int n_issued, n_consumed;
@@ -862,8 +877,17 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
       const int row = q4 * 32 + lane;
       const int64_t m = (int64_t)m0 + row;
       const uint32_t taddr = tmem_base + (uint32_t)b * 2u * CF::ACC_COLS + ((uint32_t)(q4 * 32) << 16);
-      const float ainv = (g.amax[p] && m < M) ? 1.0f / fp16_row_scale(g.amax[p][m]) : 1.0f;
+      const float ainv = (g.amax[p] && m < M) ? fp16_row_scale_inv(g.amax[p][m]) : 1.0f;
       const float* bmx = g.bmax[p];
+      // this warp's copy of the tile's inverse column scales (read once per tile)
+      float* binv = s_binv[warp - 2];
+      if (bmx) {
+        for (int t = lane; t < BN / 2; t += 32) {
+          const int64_t n = (int64_t)(r0 >> 1) + t;
+          binv[t] = n < N ? fp16_row_scale_inv(bmx[n]) : 1.0f;
+        }
+        __syncwarp();
+      }
 #pragma unroll 1
       for (int c = 0; c < BN; c += 16) {
         uint32_t v[16], w[16];
@@ -880,7 +904,7 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
           for (int j = 0; j < 8; ++j) {
             const int64_t n = nb + j;
             if (n < N) {
-              const float f = bmx ? ainv / fp16_row_scale(bmx[n]) : ainv;
+              const float f = bmx ? ainv * binv[(c >> 1) + j] : ainv;
               C[n * M + m] = make_float2((__uint_as_float(v[2 * j]) + __uint_as_float(w[2 * j])) * f,
                                          (__uint_as_float(v[2 * j + 1]) + __uint_as_float(w[2 * j + 1])) * f);
             }

@@ -248,6 +248,20 @@ __host__ __device__ inline float fp16_row_scale(float mx) {
   memcpy(&r, &o, 4);
   return r;
 }
+// 1 / fp16_row_scale(mx) exactly (a power of two, 2^-127 at the smallest), without a division.
+__host__ __device__ inline float fp16_row_scale_inv(float mx) {
+  uint32_t b;
+  memcpy(&b, &mx, 4);
+  const int e = (int)((b >> 23) & 0xffu);
+  if (e == 0) return 1.0f;
+  int te = 268 - e;
+  te = te < 1 ? 1 : (te > 254 ? 254 : te);
+  const int ie = 254 - te;  // biased exponent of 2^(127 - te)
+  const uint32_t o = ie > 0 ? (uint32_t)ie << 23 : 0x00400000u;
+  float r;
+  memcpy(&r, &o, 4);
+  return r;
+}
 cudaError_t launch_tc_gemm(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why);
 
 // ---- FP64-grade GEMM on the tensor cores (gtn_gemm_f64e.cu) ------------------------------

@@ -277,8 +277,51 @@ __device__ __forceinline__ void split16(double x, __half* h, __half* l) {
   *h = __double2half(x);
   *l = __double2half(x - (double)__half2float(*h));
 }
+// The complex FP64 inputs of the fp16 planes are handled with integer operations on the
+// doubles' bits: on this part FP64 arithmetic and the F64->F32 conversion run far below the
+// integer rate and bounded the c128 splits (one FP64 multiply, two conversions and a
+// subtraction per value).
+// x * 2^shift rounded to float (nearest, ties to even); magnitudes below FLT_MIN become a
+// signed zero (far below the fp16 planes' resolution after the row scaling), NaN stays NaN.
+__device__ __forceinline__ float d2f_scaled_rn(double x, int shift) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned long long mag = b & 0x7fffffffffffffffull;
+  const uint32_t sgn = static_cast<uint32_t>(b >> 32) & 0x80000000u;
+  const int E = static_cast<int>(mag >> 52);
+  const unsigned long long m52 = mag & 0xfffffffffffffull;
+  if (E == 0x7ff) return __uint_as_float(sgn | (m52 ? 0x7fc00000u : 0x7f800000u));
+  if (E == 0) return __uint_as_float(sgn);
+  const int fe = E - 1023 + shift + 127;  // biased float exponent before rounding
+  if (fe < 1) return __uint_as_float(sgn);
+  if (fe > 254) return __uint_as_float(sgn | 0x7f800000u);
+  unsigned long long r = (static_cast<unsigned long long>(fe) << 52) | m52;
+  r += 0x0fffffffull + ((r >> 29) & 1ull);  // round half to even at the 29 dropped bits
+  return __uint_as_float(sgn | static_cast<uint32_t>(r >> 29));  // a carry moves into the exponent
+}
+// The same scaled split as the float overload, for a double and a power-of-two scale s.
+__device__ __forceinline__ void split16_scaled(double x, float s, __half* h, __half* l) {
+  const float xf = d2f_scaled_rn(x, (int)((__float_as_uint(s) >> 23) & 0xffu) - 127);
+  *h = __float2half_rn(xf);
+  *l = __float2half_rn(xf - __half2float(*h));
+}
+__device__ __forceinline__ void split16_scaled(float x, float s, __half* h, __half* l) { split16(x * s, h, l); }
 __device__ __forceinline__ float absmax2(float2 v) { return fmaxf(fabsf(v.x), fabsf(v.y)); }
-__device__ __forceinline__ float absmax2(double2 v) { return (float)fmax(fabs(v.x), fabs(v.y)); }
+// max(|re|, |im|) of a complex double as a float upper bound with the same binary exponent
+// (truncated mantissa), from the bits: NaN entries are ignored like fmax does, a magnitude
+// below FLT_MIN gives FLT_MIN (so the row still gets a scale that resolves it).
+__device__ __forceinline__ float absmax2(double2 v) {
+  constexpr unsigned long long kAbs = 0x7fffffffffffffffull, kInf = 0x7ff0000000000000ull;
+  unsigned long long a = static_cast<unsigned long long>(__double_as_longlong(v.x)) & kAbs;
+  unsigned long long c = static_cast<unsigned long long>(__double_as_longlong(v.y)) & kAbs;
+  if (a > kInf) a = 0;
+  if (c > kInf) c = 0;
+  const unsigned long long m = a > c ? a : c;
+  if (m == 0) return 0.f;
+  const int fe = static_cast<int>(m >> 52) - 1023 + 127;
+  if (fe < 1) return __uint_as_float(0x00800000u);
+  if (fe > 254) return __uint_as_float(0x7f800000u);
+  return __uint_as_float((static_cast<uint32_t>(fe) << 23) | static_cast<uint32_t>((m >> 29) & 0x7fffffu));
+}
 
 // Element (m, k) as two fp16 planes, the row scaled by fp16_row_scale of its maximum.
 template <typename Tin>
@@ -286,8 +329,8 @@ __device__ __forceinline__ void put16(__half* out, int64_t ld2, int64_t pstride,
                                       float rowmax) {
   const float s = fp16_row_scale(rowmax);
   __half2 hi, lo;
-  split16(v.x * s, &hi.x, &lo.x);
-  split16(v.y * s, &hi.y, &lo.y);
+  split16_scaled(v.x, s, &hi.x, &lo.x);
+  split16_scaled(v.y, s, &hi.y, &lo.y);
   __half2* row = reinterpret_cast<__half2*>(out + m * ld2 + 2 * k);
   row[0] = hi;
   *reinterpret_cast<__half2*>(reinterpret_cast<__half*>(row) + pstride) = lo;
@@ -302,13 +345,27 @@ struct Split16Writer {
     put16(out, ld2, pstride, m, k, v, amax[m]);
   }
 };
-// The same, handed the row maximum (the fused split computes it in shared memory).
+// The same, handed the row maximum (the fused split computes it in shared memory), for two
+// adjacent columns k, k + 1 (k even): one 8-byte store per plane.
 struct Split16RowWriter {
   __half* out;
   int64_t ld2;
   int64_t pstride;
-  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v, float rowmax) const {
-    put16(out, ld2, pstride, m, k, v, rowmax);
+  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v0, Tin v1, float rowmax) const {
+    const float s = fp16_row_scale(rowmax);
+    __half2 h0, l0, h1, l1;
+    split16_scaled(v0.x, s, &h0.x, &l0.x);
+    split16_scaled(v0.y, s, &h0.y, &l0.y);
+    split16_scaled(v1.x, s, &h1.x, &l1.x);
+    split16_scaled(v1.y, s, &h1.y, &l1.y);
+    __half* row = out + m * ld2 + 2 * k;
+    uint2 hv, lv;
+    hv.x = *reinterpret_cast<uint32_t*>(&h0);
+    hv.y = *reinterpret_cast<uint32_t*>(&h1);
+    lv.x = *reinterpret_cast<uint32_t*>(&l0);
+    lv.y = *reinterpret_cast<uint32_t*>(&l1);
+    *reinterpret_cast<uint2*>(row) = hv;
+    *reinterpret_cast<uint2*>(row + pstride) = lv;
   }
 };
 
@@ -380,8 +437,9 @@ struct Int7RowWriter {
   __nv_bfloat16* out;
   int64_t ld2;
   int64_t pstride;
-  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v, float rowmax) const {
-    put_i7(out, ld2, pstride, m, k, v, rowmax);
+  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v0, Tin v1, float rowmax) const {
+    put_i7(out, ld2, pstride, m, k, v0, rowmax);
+    put_i7(out, ld2, pstride, m, k + 1, v1, rowmax);
   }
 };
 
@@ -875,35 +933,43 @@ __global__ void __launch_bounds__(256) split_rows_kernel(const Tin* __restrict__
     __syncthreads();
   }
   if (rank == 0 && tid < TR && m0 + tid < M) amax[m0 + tid] = rmax[tid];
+  // columns in pairs (kc, Kp and k0 are even): 8-byte stores per plane
   for (int r = 0; r < TR; ++r) {
     const int64_t m = m0 + r;
     if (m >= M) break;
     const float rm = rmax[r];
-    for (int c = tid; c < kw; c += 256) w(m, k0 + c, c < kv ? tile[r * pitch + c] : Zero<Tin>::v(), rm);
+    for (int c = 2 * tid; c < kw; c += 512)
+      w(m, k0 + c, c < kv ? tile[r * pitch + c] : Zero<Tin>::v(), c + 1 < kv ? tile[r * pitch + c + 1] : Zero<Tin>::v(),
+        rm);
   }
   if (cs > 1) cluster_wait();  // peers may read this CTA's maxima until they have arrived
 }
 
 // Rows per cluster, cluster size and columns per CTA of the fused split, or false when a
-// row of the view does not fit in 8 CTAs' shared memory (the two-kernel path runs then).
-// Rows: 32, 16 or 8 (at least 16 when the rows are the unit-stride index, for 128-byte runs);
-// the smallest cluster whose CTAs stay under the budget that lets two CTAs share an SM.
+// row of the view does not fit in 16 CTAs' shared memory (the two-kernel path runs then).
+// Rows: 32, 16 or 8 (at least 16 when the rows are the unit-stride index, for 128-byte
+// runs).  CTAs of at most 48 KB come first, so that four share an SM and their load,
+// reduce and store phases overlap; the smallest cluster for the most rows within that
+// budget wins, then the same with 112 KB (two per SM).  Columns per CTA: a multiple of 8.
+constexpr int kSplitMaxCluster = 16;
 template <typename Tin>
 bool split_rows_shape(int64_t K, int64_t Kp, int m_fast, int* TR, int* cs, int* kc, size_t* smem) {
-  constexpr size_t kBudget = 112 * 1024;
+  const size_t budgets[2] = {48 * 1024, 112 * 1024};
   const int trs[3] = {32, 16, 8};
-  for (int t : trs) {
-    if (m_fast && t < 16) break;
-    for (int c = 1; c <= 8; ++c) {
-      const int64_t k = ((Kp + c - 1) / c + 7) / 8 * 8;
-      if (c > 1 && (c - 1) * k >= Kp) break;  // every rank holds columns
-      const size_t b = split_rows_smem<Tin>(t, (int)k);
-      if (b <= kBudget) {
-        *TR = t;
-        *cs = c;
-        *kc = (int)k;
-        *smem = b;
-        return true;
+  for (size_t budget : budgets) {
+    for (int t : trs) {
+      if (m_fast && t < 16) break;
+      for (int c = 1; c <= kSplitMaxCluster; ++c) {
+        const int64_t k = ((Kp + c - 1) / c + 7) / 8 * 8;
+        if (c > 1 && (c - 1) * k >= Kp) break;  // every rank holds columns
+        const size_t b = split_rows_smem<Tin>(t, (int)k);
+        if (b <= budget) {
+          *TR = t;
+          *cs = c;
+          *kc = (int)k;
+          *smem = b;
+          return true;
+        }
       }
     }
   }
@@ -917,6 +983,7 @@ cudaError_t launch_split_rows_t(const Tin* T, const Off& off, int64_t M, int64_t
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
     attr = true;
   }
@@ -957,7 +1024,8 @@ cudaError_t launch_split_rows(const Tin* T, const Off& off, int64_t M, int64_t K
   }
   // a cluster shape the device cannot schedule is a launch-configuration error (nothing ran):
   // clear it and let the caller take the two-kernel path
-  if (e == cudaErrorInvalidClusterSize || e == cudaErrorInvalidConfiguration || e == cudaErrorInvalidValue) {
+  if (e == cudaErrorInvalidClusterSize || e == cudaErrorInvalidConfiguration || e == cudaErrorInvalidValue ||
+      e == cudaErrorLaunchOutOfResources) {
     cudaGetLastError();
     return cudaSuccess;
   }

@@ -2,8 +2,8 @@
 planes) against the two-kernel path it replaces (row maxima, then the split): the planes,
 and so the map outputs, are bit-identical.  Covers table-driven maps and one-shot
 contractions, fp16x3 and the FP64-grade digit planes, views whose unit-stride index is a
-row or a column, clusters of one to eight CTAs, row and column tails, and a row too long
-for eight CTAs (the two-kernel path runs)."""
+row or a column, clusters of two to sixteen CTAs, row and column tails, and rows too long
+for the clusters (the two-kernel path runs)."""
 import os
 import sys
 
@@ -57,12 +57,13 @@ def test_fused_split_map_bit_identical(ctx, prec, tol):
 
 @pytest.mark.parametrize("prec", ["fp16x3", "fp64e"])
 @pytest.mark.parametrize("M,K,N,k_major", [
-    (1000, 200, 70, True),     # one CTA per row block, rows contiguous along k
+    (1000, 200, 70, True),     # a small cluster per row block, rows contiguous along k
     (1000, 200, 70, False),    # the unit-stride index is the row
-    (517, 3000, 40, True),     # a cluster of several CTAs per row block, tails in M and K
+    (517, 3000, 40, True),     # a wide cluster, tails in M and K
     (517, 3000, 40, False),
-    (300, 7001, 33, False),    # a long row: the widest cluster
-    (64, 20000, 24, True),     # longer than eight CTAs hold: the two-kernel path
+    (300, 7001, 33, True),     # the widest clusters
+    (300, 7001, 33, False),    # longer than the clusters hold with 16-row blocks: two kernels
+    (64, 20000, 24, True),     # longer than sixteen CTAs hold: the two-kernel path
 ])
 def test_fused_split_contract_bit_identical(ctx, prec, M, K, N, k_major):
     rng = np.random.default_rng(M + K)
