@@ -702,7 +702,13 @@ def run_dmrg(args):
     psi0 = G.random_ttns(np.random.default_rng(7), topo, 2, bond, ctx=ctx)
     out = {"metric": "DMRG sweep time", "unit": "s/sweep", "topology": f"{args.dmrg_topology}{L}", "bond_dim": D,
            "model": "Heisenberg XX+YY+ZZ (Pauli), dense ComplexF64", "krylovdim": 20, "runs": {}}
-    for prec in args.dmrg_precisions.split(","):
+    for label in args.dmrg_precisions.split(","):
+        # "fp16x3+fp64e": the mixed maps with FP64-grade tensor-core environments, Rayleigh
+        # quotients and refinement residuals; "+refine": FP64-residual refinement of every
+        # local eigenvector (gtn_lanczos_refine)
+        prec = label.split("+")[0]
+        fp64e = "+fp64e" in label
+        refine = "all" if ("+refine" in label or fp64e) and prec != "fp64" else "off"
         psi = psi0.copy()
         stats = {"timing": True}
         times, energies = [], []
@@ -710,13 +716,13 @@ def run_dmrg(args):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             _, Es = G.dmrg2(psi, H, G.TruncationScheme(maxdim=D), nsweeps=1, precision=prec, lanczos_tol=1e-10,
-                            stats=stats)
+                            stats=stats, refine=refine, fp64e=fp64e)
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
             energies.append(Es[-1])
-            print(f"dmrg {prec} sweep {sweep + 1}: {times[-1]:.3f} s, E = {Es[-1]:.12f}, "
+            print(f"dmrg {label} sweep {sweep + 1}: {times[-1]:.3f} s, E = {Es[-1]:.12f}, "
                   f"matvecs so far {stats.get('matvecs')}", file=sys.stderr, flush=True)
-        out["runs"][prec] = {"sweep_s": times, "energies": energies, "matvecs": stats.get("matvecs"),
+        out["runs"][label] = {"sweep_s": times, "energies": energies, "matvecs": stats.get("matvecs"),
                              "steps": stats.get("steps"),
                              "phase_s": {k[2:]: round(v, 3) for k, v in stats.items() if k.startswith("t_")}}
     runs = out["runs"]
@@ -958,9 +964,10 @@ def main():
     ap.add_argument("--no-dmrg-segment", action="store_true",
                     help="leave out the bounded D=1024 dmrg2 segment (mixed vs FP64) of the default line")
     ap.add_argument("--segment-steps", type=int, default=1)
-    ap.add_argument("--tc-tuning", default="measured", choices=["measured", "ladder"],
-                    help="tile shapes of the tcgen05 steps: timed per problem class (default) or the fixed "
-                         "ladder (a fixed launch sequence, for profiler captures)")
+    ap.add_argument("--tc-tuning", default="measured",
+                    choices=["measured", "ladder", "ps128", "ps128x2", "ps256", "pair256", "persist128"],
+                    help="tile shapes of the tcgen05 steps: timed per problem class (default), the fixed "
+                         "ladder, or one variant for every step (fixed launch sequences, for profiler captures)")
     ap.add_argument("--dmrg", action="store_true", help="measure DMRG sweeps instead of map applications")
     ap.add_argument("--dmrg-topology", default="mps", choices=["mps", "binary"])
     ap.add_argument("--dmrg-sites", type=int, default=63)
