@@ -312,6 +312,20 @@ def bench_u1(ctx, steps):
     for prec in ("bf16x6", "fp16x3"):
         out[prec]["rel_err_vs_fp64"] = float(np.linalg.norm(ys[prec] - y64) / np.linalg.norm(y64))
         out[prec]["speedup_vs_fp64"] = out[prec]["applies_per_s"] / out["fp64"]["applies_per_s"]
+    # HBM roofline of the block map: the minimal bytes of one application are x read once
+    # and y written once (c128), every intermediate coupled-charge output written and read
+    # once (c64 in the mixed modes), and every static block read once (c128); the problems
+    # are skinny (N of a few to ~200), so bytes, not tensor flops, bound them
+    mkn = out["sector_gemms_mkn_per_step"]
+    inter = sum(m * n for step in mkn[:-1] for m, _, n in step)
+    static_elems = sum(n * k for step in mkn for _, k, n in step)
+    hbm = measured_peaks()[1]
+    for prec in ("bf16x6", "fp16x3", "fp64"):
+        e_mid = 32 if prec == "fp64" else 16
+        nbytes = 16 * xs.size + 16 * plan.y.size + e_mid * inter + 16 * static_elems
+        gbs = nbytes / (out[prec]["ms_per_apply"] * 1e-3) / 1e9
+        out[prec]["hbm_roofline"] = {"algorithmic_bytes": int(nbytes), "achieved_gbs": gbs, "peak_gbs": hbm,
+                                     "frac": gbs / hbm if hbm else None}
     blocks = [U.blocks_from_flat(xs, x)] + [U.blocks_from_flat(T, d) for T, _, d in statics]
     t0 = time.perf_counter()
     y_cpu = U.flat_from_blocks(plan.y, U.ncon_blocks(blocks, labels, order))
@@ -623,16 +637,31 @@ def dmrg_segment(ctx, steps, precision, D=1024, refine_tol=1e-8):
     for prec in (precision, "fp64"):
         psi, cache = psi0.copy(), cache0.copy()
         pcode = G._lib.PRECISIONS[prec]
-        if pcode != G._lib.PREC_FP64:
+        mixed = pcode != G._lib.PREC_FP64
+        if mixed:  # the FP64-accurate work on the tensor cores, as dmrg2(fp64e=True) runs it
             cache.precision = G._lib.PREC_FP64E
+        old_linalg = ctx.linalg_precision(G._lib.PREC_FP64E if mixed else G._lib.PREC_FP64)
         n = n0
         recs = []
+        if pcode != G._lib.PREC_FP64:
+            # a sweep has chosen its tile shapes long before: measure this bond's problem
+            # classes once (a throw-away application of both maps on a copy) before the clock
+            wpsi = psi.copy()
+            wc = cache.copy()
+            move_center(wpsi, n, wc)
+            wth = two_site_tensor(wpsi, n, topo.parent[n])
+            for wp in (pcode, G._lib.PREC_FP64E):
+                wm = eff_h2(wc, wpsi, H, n, topo.parent[n], wp)
+                wm(wth)
+                wm.close()
+            del wpsi, wc, wth
+            torch.cuda.synchronize()
         for _ in range(steps):
             m = topo.parent[n]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             move_center(psi, n, cache)
-            theta = two_site_tensor(psi, n, m)
+            theta = two_site_tensor(psi, n, m, precision=G._lib.PREC_FP64E if mixed else G._lib.PREC_FP64)
             h2 = eff_h2(cache, psi, H, n, m, pcode)
             h2e = None
             if pcode != G._lib.PREC_FP64:
@@ -653,6 +682,7 @@ def dmrg_segment(ctx, steps, precision, D=1024, refine_tol=1e-8):
                          "refine_fp64_matvecs": rstats.get("refine_fp64_matvecs", 0),
                          "refine_mixed_matvecs": rstats.get("refine_mixed_matvecs", 0)})
             n = m
+        ctx.linalg_precision(old_linalg)
         out["runs"][prec] = {"step_s": [r["s"] for r in recs], "energies": [r["energy"] for r in recs],
                              "matvecs": [r["matvecs"] for r in recs], "total_s": sum(r["s"] for r in recs),
                              "refine_fp64_matvecs": [r["refine_fp64_matvecs"] for r in recs],

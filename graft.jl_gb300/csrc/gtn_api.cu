@@ -131,6 +131,18 @@ int gtn_ctx_set_stream(gtn_ctx ctx, void* stream) {
 
 void* gtn_ctx_stream(gtn_ctx ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
 
+int gtn_ctx_set_linalg_precision(gtn_ctx ctx, int precision) {
+  if (!ctx) return GTN_ERR_INVALID;
+  if (precision != GTN_PREC_FP64 && precision != GTN_PREC_FP64E)
+    return set_err(ctx, GTN_ERR_INVALID, "linalg precision: GTN_PREC_FP64 or GTN_PREC_FP64E");
+  if (precision == GTN_PREC_FP64E && !tc_gemm_supported(ctx->cc_major, ctx->cc_minor))
+    return set_err(ctx, GTN_ERR_UNSUPPORTED, "GTN_PREC_FP64E needs an sm_10x device");
+  ctx->linalg_prec = precision;
+  return GTN_OK;
+}
+
+int gtn_ctx_linalg_precision(gtn_ctx ctx) { return ctx ? ctx->linalg_prec : -1; }
+
 const char* gtn_last_error(gtn_ctx ctx) {
   if (!ctx) return "null context";
   if (t_err_ctx == ctx) return t_err.c_str();

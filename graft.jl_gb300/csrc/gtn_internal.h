@@ -52,6 +52,9 @@ struct gtn_ctx_s {
   char* carena = nullptr;
   size_t carena_cap = 0, carena_need = 0;
   void* cusolver = nullptr;
+  // precision of the GEMMs inside the factorisations (Gram SVD route): GTN_PREC_FP64 or
+  // GTN_PREC_FP64E (gtn_ctx_set_linalg_precision)
+  int linalg_prec = 0;
 };
 
 // ---- status helpers -------------------------------------------------------------

@@ -127,6 +127,34 @@ int64_t trunc_rank(const std::vector<double>& hs, int64_t maxdim, double atol, d
   return std::max<int64_t>(r, 1);
 }
 
+// C[n][m] = sum_k X[m][k] Y'[n][k] for row-major X (M x K) and Y (N x K), Y' = conj(Y) when
+// conj_y: FP64 SIMT, or the FP64-grade tensor-core GEMM (a one-shot contraction) when the
+// context's linear-algebra precision is GTN_PREC_FP64E.  tmp (M x K when conj_y, SIMT only)
+// holds conj(Y).
+int linalg_gemm(gtn_ctx ctx, const double2* X, const double2* Y, double2* C, int64_t M, int64_t N, int64_t K,
+                bool conj_y, double2* tmp) {
+  cudaStream_t s = ctx->stream;
+  if (ctx->linalg_prec == GTN_PREC_FP64E) {
+    const int ranks[2] = {2, 2};
+    const int64_t dims[4] = {M, K, N, K};
+    const int labels[4] = {-2, 1, -1, 1};
+    const int conj[2] = {0, conj_y ? 1 : 0};
+    const int order[2] = {0, 1};
+    const void* ops[2] = {X, Y};
+    return gtn_contract(ctx, 2, ranks, dims, labels, conj, order, ops, C, GTN_PREC_FP64E);
+  }
+  const double2* Yc = Y;
+  if (conj_y) {
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(tmp, Y, N * K * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    GTN_CUDA_TRY(ctx, launch_conj_inplace(tmp, N * K, s));
+    ctx->launches++;
+    Yc = tmp;
+  }
+  GTN_CUDA_TRY(ctx, launch_zgemm_simt(X, Yc, C, M, N, K, s));
+  ctx->launches++;
+  return GTN_OK;
+}
+
 // Thin SVD of a wide row-major m x n matrix (m <= n) through its Gram matrix:
 // G = A A^H (FP64 GEMM), G = W diag(w) W^H (cuSOLVER Zheevd), U = W reversed (descending),
 // S = sqrt(w), Vh = S^-1 U^H A (FP64 GEMM).  Used above the size where LAPACK-style
@@ -155,10 +183,10 @@ int svd_gram(gtn_ctx ctx, cusolverDnHandle_t h, int64_t m, int64_t n, const doub
   double2* Ut = reinterpret_cast<double2*>(p); p += bUt;
   int* dinfo = reinterpret_cast<int*>(p);
   // G (column-major) : C[j][i] = sum_l A[i][l] conj(A[j][l]) = G[i][j]
-  GTN_CUDA_TRY(ctx, cudaMemcpyAsync(conjA, A, m * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-  GTN_CUDA_TRY(ctx, launch_conj_inplace(conjA, m * n, s));
-  GTN_CUDA_TRY(ctx, launch_zgemm_simt(A, conjA, G, m, m, n, s));
-  ctx->launches += 2;
+  {
+    const int st = linalg_gemm(ctx, A, A, G, m, m, n, true, conjA);
+    if (st != GTN_OK) return st;
+  }
   if (sv.heevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)m, reinterpret_cast<cuDoubleComplex*>(G),
                (int)m, w, reinterpret_cast<cuDoubleComplex*>(work), lwork, dinfo) != CUSOLVER_STATUS_SUCCESS)
     return set_err(ctx, GTN_ERR_CUDA, "cusolverDnZheevd failed");
@@ -190,7 +218,10 @@ int svd_gram(gtn_ctx ctx, cusolverDnHandle_t h, int64_t m, int64_t n, const doub
   GTN_CUDA_TRY(ctx, launch_conj_inplace(Ut, r * m, s));
   // Vh[i][l] = sum_a Ut[i][a] A[a][l]: C[nn=i][mm=l] = sum_k X[l][k] Y[i][k], X = A^T, Y = Ut
   GTN_CUDA_TRY(ctx, launch_transpose_c128(A, m, n, At, s));
-  GTN_CUDA_TRY(ctx, launch_zgemm_simt(At, Ut, Vh, n, r, m, s));
+  {
+    const int st = linalg_gemm(ctx, At, Ut, Vh, n, r, m, false, nullptr);
+    if (st != GTN_OK) return st;
+  }
   // s_i = ||A^H u_i|| (absolute accuracy ~ eps * s_max instead of the eigenvalues'
   // sqrt(eps) * s_max, so singular values of a rank-deficient A come out near zero)
   double* dnorm = reinterpret_cast<double*>(conjA);  // conjA is no longer needed

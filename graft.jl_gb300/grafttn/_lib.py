@@ -47,6 +47,8 @@ SIGNATURES = {
     "gtn_last_error": (C.c_char_p, [_p]),
     "gtn_ctx_launch_count": (_i64, [_p]),
     "gtn_ctx_sync": (_i, [_p]),
+    "gtn_ctx_set_linalg_precision": (_i, [_p, _i]),
+    "gtn_ctx_linalg_precision": (_i, [_p]),
     "gtn_map_create": (_i, [_p, _i, _pi, _pi64, _pi, _pi, _pi, C.POINTER(_p), _i, C.POINTER(_p)]),
     "gtn_map_destroy": (_i, [_p]),
     "gtn_map_apply": (_i, [_p, _p, _p]),

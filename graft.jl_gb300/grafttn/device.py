@@ -55,6 +55,16 @@ class Context:
     def sync(self):
         check(self.lib.gtn_ctx_sync(self.h), self.h, "sync")
 
+    def linalg_precision(self, precision=None):
+        """The precision of the matrix products inside the factorisations (GTN_PREC_FP64 or
+        GTN_PREC_FP64E, gtn_ctx_set_linalg_precision); sets it when given (None leaves it) and
+        returns the previous value."""
+        old = int(self.lib.gtn_ctx_linalg_precision(self.h))
+        if precision is not None:
+            prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+            check(self.lib.gtn_ctx_set_linalg_precision(self.h, prec), self.h, "set_linalg_precision")
+        return old
+
     # ---- tensors -------------------------------------------------------------------
     def empty(self, shape):
         return torch.empty(tuple(int(s) for s in shape), dtype=CDT, device=f"cuda:{self.device}")

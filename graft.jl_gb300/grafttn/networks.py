@@ -166,8 +166,9 @@ def random_ttns(rng, topo: TreeTopology, d, bond, center=None, ctx=None):
     return normalize(psi)
 
 
-def two_site_tensor(psi: TTNS, n, m):
-    """Θ: A_n's codomain legs, then A_m's legs except slot k (effective.jl:827-843)."""
+def two_site_tensor(psi: TTNS, n, m, precision=None):
+    """Θ: A_n's codomain legs, then A_m's legs except slot k (effective.jl:827-843).
+    ``precision``: GTN_PREC_FP64 (default) or GTN_PREC_FP64E for the contraction."""
     t = psi.topo
     if t.parent[n] != m:
         raise ValueError("two_site_tensor: m must be the parent of n")
@@ -183,7 +184,9 @@ def two_site_tensor(psi: TTNS, n, m):
         else:
             pos += 1
             labB.append(-pos)
-    return psi.ctx.contract([A, B], [labA, labB])
+    if precision is None:
+        return psi.ctx.contract([A, B], [labA, labB])
+    return psi.ctx.contract([A, B], [labA, labB], precision=precision)
 
 
 def split_two_site(psi: TTNS, theta, n, m, trunc: TruncationScheme | None = None, center_on="n"):

@@ -42,8 +42,9 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
     FP64 Rayleigh quotient of the refined vector.
 
     ``fp64e`` runs the FP64-accurate work of a mixed sweep on the tensor cores: environment
-    updates in GTN_PREC_FP64E, and the Rayleigh quotients and refinement residuals through
-    an FP64E twin of each local map (gtn_map_set_fp64)."""
+    updates and two-site merges in GTN_PREC_FP64E, the Gram-matrix products of the truncated
+    SVD (gtn_ctx_set_linalg_precision), and the Rayleigh quotients and refinement residuals
+    through an FP64E twin of each local map (gtn_map_set_fp64)."""
     if not H.ishermitian:
         raise ValueError("dmrg2: DMRG requires ishermitian(H) == true")
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
@@ -53,6 +54,18 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
     t = psi.topo
     use_e = fp64e and prec != _lib.PREC_FP64
     cache = EnvCache(t, precision="fp64e" if use_e else "fp64")
+    merge_prec = _lib.PREC_FP64E if use_e else _lib.PREC_FP64
+    old_linalg = psi.ctx.linalg_precision(_lib.PREC_FP64E if use_e else None)
+    try:
+        return _dmrg2_sweeps(psi, H, trunc, nsweeps, tol, krylovdim, prec, rq_fp64, lanczos_tol, maxiter,
+                             verbose, stats, refine, refine_tol, use_e, cache, merge_prec)
+    finally:
+        psi.ctx.linalg_precision(old_linalg)
+
+
+def _dmrg2_sweeps(psi, H, trunc, nsweeps, tol, krylovdim, prec, rq_fp64, lanczos_tol, maxiter, verbose, stats,
+                  refine, refine_tol, use_e, cache, merge_prec):
+    t = psi.topo
     energies = []
     bonds = [n for n in t.postorder() if t.parent[n] >= 0]
     sched = [(n, "m") for n in bonds] + [(n, "n") for n in reversed(bonds)]
@@ -73,7 +86,7 @@ def dmrg2(psi: TTNS, H: TTNO, trunc: TruncationScheme | None = None, nsweeps=10,
             tt = time.perf_counter()
             move_center(psi, n, cache)
             tt = mark("t_gauge", tt)
-            theta = two_site_tensor(psi, n, m)
+            theta = two_site_tensor(psi, n, m, precision=merge_prec)
             tt = mark("t_merge", tt)
             h2 = eff_h2(cache, psi, H, n, m, prec)
             h2e = None

@@ -69,6 +69,13 @@ const char* gtn_last_error(gtn_ctx ctx);
 int64_t gtn_ctx_launch_count(gtn_ctx ctx);
 /* Wait for the stream and report (then clear) any device-side error flag. */
 int gtn_ctx_sync(gtn_ctx ctx);
+/* Precision of the matrix products inside the factorisations of this context (the Gram
+ * matrix and the right factor of the truncated SVD's Gram route, gtn_svd_trunc):
+ * GTN_PREC_FP64 (default, FP64 SIMT) or GTN_PREC_FP64E (the FP64-grade tensor-core GEMM,
+ * about 1e-14 relative to sum |a||b|).  The eigen- and QR decompositions stay cuSOLVER FP64.
+ * No counterpart in the reference (its factorisations are LAPACK calls on the host). */
+int gtn_ctx_set_linalg_precision(gtn_ctx ctx, int precision);
+int gtn_ctx_linalg_precision(gtn_ctx ctx);
 
 /* ---- effective maps: replaces Planning.EffectiveMap / execute / contract_pair ------
  * lib/GraftPlanning/src/Planning/types.jl:410-445 (EffectiveMap callable),

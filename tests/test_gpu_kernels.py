@@ -135,16 +135,22 @@ def test_lanczos_and_expm(ctx):
     hm.close()
 
 
+@pytest.mark.parametrize("linalg", ["fp64", "fp64e"])
 @pytest.mark.parametrize("m,n", [(500, 700), (700, 500), (512, 512)])
-def test_svd_gram_path_large(ctx, m, n):
-    # above the Gram threshold: FP64 GEMM + Zheevd; decaying spectrum down to 1e-7
+def test_svd_gram_path_large(ctx, m, n, linalg):
+    # above the Gram threshold: Gram matrix (FP64 SIMT or FP64-grade tensor-core GEMM, the
+    # context's linear-algebra precision) + Zheevd; decaying spectrum down to 1e-7
     rng = np.random.default_rng(8)
     k = min(m, n)
     U0, _ = np.linalg.qr(crandn(rng, (m, k)))
     V0, _ = np.linalg.qr(crandn(rng, (n, k)))
     s0 = np.logspace(0, -7, k)
     a = (U0 * s0) @ V0.conj().T
-    U, S, Vh, disc = ctx.svd_trunc(ctx.upload(a), maxdim=300)
+    old = ctx.linalg_precision(linalg)
+    try:
+        U, S, Vh, disc = ctx.svd_trunc(ctx.upload(a), maxdim=300)
+    finally:
+        ctx.linalg_precision(old)
     U, Vh = ctx.download(U), ctx.download(Vh)
     assert len(S) == 300
     # the Gram path resolves sigma to ~eps * s_max^2 / sigma: ~1e-12 absolute here
