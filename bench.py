@@ -455,7 +455,8 @@ def run_ours(args, rank, world):
     executed = tc[2] * PRODUCTS[args.precision] / (tc[1] / 1000.0) / 1e12
     traffic = profile_traffic("tc_gemm", args.workload)
 
-    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    # end to end through the C ABI with host buffers (page-locked): every step moves x from
+    # and y to host memory inside the timed region
     xh = torch.from_numpy(theta.copy()).pin_memory()
     yh = torch.empty(hm.y_shape, dtype=torch.complex128).pin_memory()
     import ctypes as C
@@ -583,7 +584,8 @@ def run_ours(args, rank, world):
                          "sample": f"{cpu_n} eff_h2 application(s) of the same workload, {cpu_el:.1f} s"},
         "e2e": {"value": e2e_rate, "unit": "applies/s", "h2d_bytes_per_step": int(theta.size * 16),
                 "d2h_bytes_per_step": int(np.prod(hm.y_shape) * 16),
-                "path": "gtn_map_apply_host (C ABI, pinned host buffers)"},
+                "path": "gtn_map_apply_host (C ABI) with page-locked host buffers, which the map's first and "
+                        "last kernels read and write in place"},
         "gpu_launches": launches,
         "clocks": clocks,
         "tc_tile_choices": tuning,

@@ -825,18 +825,15 @@ __global__ void __launch_bounds__(256) block_rowmax_kernel(const DevGatherJob* _
 
 
 // ---- fused split: row maxima and slice planes in one pass over the running tensor --------
-// A cluster of cs CTAs owns blocks of TR rows of the K-major view; CTA r of the cluster
-// holds the columns [r kc, (r + 1) kc).  The clusters are persistent: cluster c takes the
-// row blocks c, c + (number of clusters), ...  For each block a CTA stages its columns with
-// cp.async (every element read from HBM once), reduces partial row maxima, reads its peers'
-// through distributed shared memory after a cluster barrier, and writes its columns of the
-// slice planes scaled by the full row maxima; the cluster's rank 0 writes the maxima to
-// amax[] for the GEMM epilogue.  Two staging buffers: the copies of block i + 1 are in
-// flight while block i is reduced and written.  The partial maxima are double-buffered too:
-// a peer reads block i's maxima before it arrives at block i + 1's barrier, and they are
-// overwritten only at block i + 2.  The barriers are hardware cluster barriers: every CTA
-// of a cluster runs the same blocks, every thread reaches every barrier, and a last barrier
-// keeps each CTA's shared memory alive until its peers are done with it.
+// A cluster of cs CTAs owns TR rows of the K-major view; CTA r of the cluster stages the
+// columns [r kc, (r + 1) kc) of those rows in shared memory (cp.async, every element read
+// from HBM once), reduces its partial row maxima, and reads its peers' partial maxima
+// through distributed shared memory after a cluster barrier.  It then writes its columns
+// of the slice planes, scaled by the full row maxima, and the cluster's rank 0 writes them
+// to amax[] for the GEMM epilogue.  The second cluster barrier (arrive after the peer
+// reads, wait before exit) keeps each CTA's partial maxima alive while peers read them.
+// The barriers are hardware cluster barriers: every CTA of a cluster is co-scheduled and
+// every thread reaches both, so no wait can be left hanging.
 __device__ __forceinline__ uint32_t cluster_rank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -845,6 +842,10 @@ __device__ __forceinline__ uint32_t cluster_rank() {
 __device__ __forceinline__ void cluster_sync_all() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
 __device__ __forceinline__ float ld_peer_f32(const float* p, uint32_t rank) {
   const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
   uint32_t ra;
@@ -863,15 +864,11 @@ __device__ __forceinline__ void cp_async_el(double2* dst, const double2* src) {
                "l"(src)
                : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 template <typename Tin> __host__ __device__ constexpr int split_rows_pitch(int kc) { return kc | 1; }
-// staging buffers, column offsets, row offsets (x2), partial maxima (x2), row maxima
 template <typename Tin> __host__ __device__ constexpr size_t split_rows_smem(int TR, int kc) {
-  return 2 * (size_t)TR * split_rows_pitch<Tin>(kc) * sizeof(Tin) + (size_t)kc * 8 + 2 * (size_t)TR * 8 +
-         3 * (size_t)TR * 4;
+  return (size_t)TR * split_rows_pitch<Tin>(kc) * sizeof(Tin) + (size_t)kc * 8 + (size_t)TR * 8 + (size_t)TR * 8;
 }
 
 template <typename Tin, int TR, class Off, class W>
@@ -880,119 +877,99 @@ __global__ void __launch_bounds__(256) split_rows_kernel(const Tin* __restrict__
                                                          float* __restrict__ amax) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int pitch = split_rows_pitch<Tin>(kc);  // odd: the row-strided staging stores spread over banks
-  Tin* tiles = reinterpret_cast<Tin*>(smraw);   // [2][TR * pitch]
-  int64_t* offK = reinterpret_cast<int64_t*>(tiles + 2 * TR * pitch);
-  int64_t* offM = offK + kc;                    // [2][TR]
-  float* pmax = reinterpret_cast<float*>(offM + 2 * TR);  // [2][TR]
-  float* rmax = pmax + 2 * TR;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  Tin* tile = reinterpret_cast<Tin*>(smraw);
+  int64_t* offK = reinterpret_cast<int64_t*>(tile + TR * pitch);
+  int64_t* offM = offK + kc;
+  float* pmax = reinterpret_cast<float*>(offM + TR);
+  float* rmax = pmax + TR;
+  const int tid = threadIdx.x;
   const uint32_t rank = cs > 1 ? cluster_rank() : 0u;
+  const int64_t m0 = (int64_t)(blockIdx.x / cs) * TR;
   const int64_t k0 = (int64_t)rank * kc;
   const int kv = (int)max((int64_t)0, min((int64_t)kc, K - k0));   // columns read
   const int kw = (int)max((int64_t)0, min((int64_t)kc, Kp - k0));  // columns written (zero padding to Kp)
-  const int64_t nblocks = (M + TR - 1) / TR;
-  const int64_t nclusters = gridDim.x / cs;
   for (int i = tid; i < kv; i += 256) offK[i] = off.k(k0 + i);
-
-  auto set_rows = [&](int64_t rb, int b) {
-    if (tid < TR) offM[b * TR + tid] = rb * TR + tid < M ? off.m(rb * TR + tid) : 0;
-  };
-  auto issue = [&](int64_t rb, int b) {
-    Tin* tile = tiles + b * TR * pitch;
-    const int64_t* om = offM + b * TR;
-    const int64_t m0 = rb * TR;
-    if (m_fast) {  // consecutive threads on consecutive rows (the unit-stride index is in M)
-      for (int e = tid; e < TR * kv; e += 256) {
-        const int im = e % TR, ik = e / TR;
-        Tin* d = tile + im * pitch + ik;
-        if (m0 + im < M) cp_async_el(d, T + om[im] + offK[ik]);
+  if (tid < TR) offM[tid] = m0 + tid < M ? off.m(m0 + tid) : 0;
+  __syncthreads();
+  if (m_fast) {  // consecutive threads on consecutive rows (the unit-stride index is in M)
+    for (int e = tid; e < TR * kv; e += 256) {
+      const int im = e % TR, ik = e / TR;
+      Tin* d = tile + im * pitch + ik;
+      if (m0 + im < M) cp_async_el(d, T + offM[im] + offK[ik]);
+      else *d = Zero<Tin>::v();
+    }
+  } else {
+    for (int r = 0; r < TR; ++r) {
+      const bool live = m0 + r < M;
+      for (int c = tid; c < kv; c += 256) {
+        Tin* d = tile + r * pitch + c;
+        if (live) cp_async_el(d, T + offM[r] + offK[c]);
         else *d = Zero<Tin>::v();
       }
-    } else {
-      for (int r = 0; r < TR; ++r) {
-        const bool live = m0 + r < M;
-        for (int c = tid; c < kv; c += 256) {
-          Tin* d = tile + r * pitch + c;
-          if (live) cp_async_el(d, T + om[r] + offK[c]);
-          else *d = Zero<Tin>::v();
-        }
-      }
-    }
-  };
-
-  int64_t rb = (int64_t)(blockIdx.x / cs);
-  if (rb < nblocks) set_rows(rb, 0);
-  __syncthreads();
-  if (rb < nblocks) issue(rb, 0);
-  cp_async_commit();
-  for (int it = 0; rb < nblocks; rb += nclusters, ++it) {
-    const int b = it & 1;
-    const int64_t nb = rb + nclusters;
-    if (nb < nblocks) set_rows(nb, b ^ 1);
-    __syncthreads();  // the other buffer's rows are set and its previous block fully written
-    if (nb < nblocks) issue(nb, b ^ 1);
-    cp_async_commit();
-    cp_async_wait_prev();  // this block's copies have landed (the next block's may be in flight)
-    __syncthreads();
-    const Tin* tile = tiles + b * TR * pitch;
-    float* pm = pmax + b * TR;
-    for (int r = warp; r < TR; r += 8) {
-      float x = 0.f;
-      for (int c = lane; c < kv; c += 32) x = fmaxf(x, absmax2(tile[r * pitch + c]));
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
-      if (lane == 0) pm[r] = x;
-    }
-    if (cs > 1) {
-      cluster_sync_all();  // every CTA's partial maxima of this block are in its shared memory
-      if (tid < TR) {
-        float x = 0.f;
-        for (int q = 0; q < cs; ++q) x = fmaxf(x, ld_peer_f32(pm + tid, (uint32_t)q));
-        rmax[tid] = x;
-      }
-    } else {
-      __syncthreads();
-      if (tid < TR) rmax[tid] = pm[tid];
-    }
-    __syncthreads();
-    const int64_t m0 = rb * TR;
-    if (rank == 0 && tid < TR && m0 + tid < M) amax[m0 + tid] = rmax[tid];
-    // columns in pairs (kc, Kp and k0 are even): 8-byte stores per plane
-    for (int r = 0; r < TR; ++r) {
-      const int64_t m = m0 + r;
-      if (m >= M) break;
-      const float rm = rmax[r];
-      for (int c = 2 * tid; c < kw; c += 512)
-        w(m, k0 + c, c < kv ? tile[r * pitch + c] : Zero<Tin>::v(),
-          c + 1 < kv ? tile[r * pitch + c + 1] : Zero<Tin>::v(), rm);
     }
   }
   cp_async_wait_all();
-  if (cs > 1) cluster_sync_all();  // peers may read this CTA's last maxima until they arrive here
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int r = warp; r < TR; r += 8) {
+    float x = 0.f;
+    for (int c = lane; c < kv; c += 32) x = fmaxf(x, absmax2(tile[r * pitch + c]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (lane == 0) pmax[r] = x;
+  }
+  if (cs > 1) {
+    cluster_sync_all();  // every CTA's partial maxima are in its shared memory
+    if (tid < TR) {
+      float x = 0.f;
+      for (int q = 0; q < cs; ++q) x = fmaxf(x, ld_peer_f32(pmax + tid, (uint32_t)q));
+      rmax[tid] = x;
+    }
+    cluster_arrive_relaxed();  // done reading the peers
+    __syncthreads();
+  } else {
+    __syncthreads();
+    if (tid < TR) rmax[tid] = pmax[tid];
+    __syncthreads();
+  }
+  if (rank == 0 && tid < TR && m0 + tid < M) amax[m0 + tid] = rmax[tid];
+  // columns in pairs (kc, Kp and k0 are even): 8-byte stores per plane
+  for (int r = 0; r < TR; ++r) {
+    const int64_t m = m0 + r;
+    if (m >= M) break;
+    const float rm = rmax[r];
+    for (int c = 2 * tid; c < kw; c += 512)
+      w(m, k0 + c, c < kv ? tile[r * pitch + c] : Zero<Tin>::v(), c + 1 < kv ? tile[r * pitch + c + 1] : Zero<Tin>::v(),
+        rm);
+  }
+  if (cs > 1) cluster_wait();  // peers may read this CTA's maxima until they have arrived
 }
 
 // Rows per cluster, cluster size and columns per CTA of the fused split, or false when a
 // row of the view does not fit in 16 CTAs' shared memory (the two-kernel path runs then).
 // Rows: 32, 16 or 8 (at least 16 when the rows are the unit-stride index, for 128-byte
-// runs).  Each CTA holds two staging buffers within 112 KB (two CTAs per SM); the most rows
-// with the smallest cluster win.  Columns per CTA: a multiple of 8.
+// runs).  CTAs of at most 48 KB come first, so that four share an SM and their load,
+// reduce and store phases overlap; the smallest cluster for the most rows within that
+// budget wins, then the same with 112 KB (two per SM).  Columns per CTA: a multiple of 8.
 constexpr int kSplitMaxCluster = 16;
 template <typename Tin>
 bool split_rows_shape(int64_t K, int64_t Kp, int m_fast, int* TR, int* cs, int* kc, size_t* smem) {
-  constexpr size_t kBudget = 112 * 1024;
+  const size_t budgets[2] = {48 * 1024, 112 * 1024};
   const int trs[3] = {32, 16, 8};
-  for (int t : trs) {
-    if (m_fast && t < 16) break;
-    for (int c = 1; c <= kSplitMaxCluster; ++c) {
-      const int64_t k = ((Kp + c - 1) / c + 7) / 8 * 8;
-      if (c > 1 && (c - 1) * k >= Kp) break;  // every rank holds columns
-      const size_t b = split_rows_smem<Tin>(t, (int)k);
-      if (b <= kBudget) {
-        *TR = t;
-        *cs = c;
-        *kc = (int)k;
-        *smem = b;
-        return true;
+  for (size_t budget : budgets) {
+    for (int t : trs) {
+      if (m_fast && t < 16) break;
+      for (int c = 1; c <= kSplitMaxCluster; ++c) {
+        const int64_t k = ((Kp + c - 1) / c + 7) / 8 * 8;
+        if (c > 1 && (c - 1) * k >= Kp) break;  // every rank holds columns
+        const size_t b = split_rows_smem<Tin>(t, (int)k);
+        if (b <= budget) {
+          *TR = t;
+          *cs = c;
+          *kc = (int)k;
+          *smem = b;
+          return true;
+        }
       }
     }
   }
@@ -1010,7 +987,10 @@ cudaError_t launch_split_rows_t(const Tin* T, const Off& off, int64_t M, int64_t
     if (e != cudaSuccess) return e;
     attr = true;
   }
+  const int64_t tiles = (M + TR - 1) / TR;
+  if (tiles * cs > 2147483647LL) return cudaErrorInvalidConfiguration;
   cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(tiles * cs), 1, 1);
   cfg.blockDim = dim3(256, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
@@ -1021,17 +1001,6 @@ cudaError_t launch_split_rows_t(const Tin* T, const Off& off, int64_t M, int64_t
   attrs[0].val.clusterDim.z = 1;
   cfg.attrs = attrs;
   cfg.numAttrs = 1;
-  // persistent clusters: as many as can be resident at once (at most one per row block)
-  const int64_t nblocks = (M + TR - 1) / TR;
-  cfg.gridDim = dim3((unsigned)cs, 1, 1);
-  int fit = 0;
-  if (cudaOccupancyMaxActiveClusters(&fit, kern, &cfg) != cudaSuccess || fit < 1) {
-    cudaGetLastError();
-    fit = 1;
-  }
-  const int64_t nclusters = std::min<int64_t>(nblocks, fit);
-  if (nclusters * cs > 2147483647LL) return cudaErrorInvalidConfiguration;
-  cfg.gridDim = dim3((unsigned)(nclusters * cs), 1, 1);
   return cudaLaunchKernelEx(&cfg, kern, T, off, M, K, Kp, kc, cs, m_fast, w, amax);
 }
 
