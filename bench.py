@@ -584,8 +584,7 @@ def run_ours(args, rank, world):
                          "sample": f"{cpu_n} eff_h2 application(s) of the same workload, {cpu_el:.1f} s"},
         "e2e": {"value": e2e_rate, "unit": "applies/s", "h2d_bytes_per_step": int(theta.size * 16),
                 "d2h_bytes_per_step": int(np.prod(hm.y_shape) * 16),
-                "path": "gtn_map_apply_host (C ABI) with page-locked host buffers, which the map's first and "
-                        "last kernels read and write in place"},
+                "path": "gtn_map_apply_host (C ABI), page-locked host buffers: H2D copy, apply, D2H copy"},
         "gpu_launches": launches,
         "clocks": clocks,
         "tc_tile_choices": tuning,

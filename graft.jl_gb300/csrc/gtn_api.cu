@@ -227,36 +227,11 @@ int gtn_map_apply_profiled(gtn_map map, int precision, const void* x, void* y, i
                           kind, flops, count);
 }
 
-// The device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister), or
-// null for pageable memory.
-static void* pinned_device_ptr(const void* p) {
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
-}
-
 int gtn_map_apply_host(gtn_map map, const void* x_host, void* y_host) {
   if (!map || !x_host || !y_host) return GTN_ERR_INVALID;
   MapUse use(map);
   if (!use.ok) return map_busy_error(map);
   gtn_ctx ctx = map->ctx;
-  // Page-locked buffers: the map's first step reads x and its output permutation writes y
-  // in host memory directly (over NVLink-C2C on Grace), with no staging copies in HBM.
-  // GTN_HOST_DIRECT=0 keeps the staged copies.
-  static const bool direct_ok = [] {
-    const char* e = std::getenv("GTN_HOST_DIRECT");
-    return !(e && e[0] == '0');
-  }();
-  void* dxp = direct_ok ? pinned_device_ptr(x_host) : nullptr;
-  void* dyp = direct_ok ? pinned_device_ptr(y_host) : nullptr;
-  if (dxp && dyp) {
-    const int st = map_run(map, map->precision, static_cast<const double2*>(dxp), static_cast<double2*>(dyp));
-    if (st != GTN_OK) return st;
-    return gtn_ctx_sync(ctx);
-  }
   if (!map->dx) {
     if (cudaMalloc(&map->dx, map->x_elems * sizeof(double2)) != cudaSuccess ||
         cudaMalloc(&map->dy, map->y_elems * sizeof(double2)) != cudaSuccess)

@@ -866,6 +866,21 @@ __device__ __forceinline__ void cp_async_el(double2* dst, const double2* src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// q = floor(i / d) for i < 2^31 by a multiply and a shift (Granlund and Montgomery's
+// round-up method, as in decompose_fast); the magic number is made once per CTA.
+struct FastDiv {
+  uint32_t d, mag, sh;
+};
+__device__ __forceinline__ FastDiv make_fastdiv(uint32_t d) {
+  if (d <= 1) return FastDiv{1u, 0u, 0u};
+  uint32_t l = 0;
+  while ((1u << l) < d) ++l;
+  return FastDiv{d, (uint32_t)((1ull << (31 + l)) / d + 1ull), l - 1};
+}
+__device__ __forceinline__ uint32_t fast_div(uint32_t i, const FastDiv& f) {
+  return f.d == 1u ? i : (__umulhi(i, f.mag) >> f.sh);
+}
+
 template <typename Tin> __host__ __device__ constexpr int split_rows_pitch(int kc) { return kc | 1; }
 template <typename Tin> __host__ __device__ constexpr size_t split_rows_smem(int TR, int kc) {
   return (size_t)TR * split_rows_pitch<Tin>(kc) * sizeof(Tin) + (size_t)kc * 8 + (size_t)TR * 8 + (size_t)TR * 8;
@@ -898,14 +913,13 @@ __global__ void __launch_bounds__(256) split_rows_kernel(const Tin* __restrict__
       if (m0 + im < M) cp_async_el(d, T + offM[im] + offK[ik]);
       else *d = Zero<Tin>::v();
     }
-  } else {
-    for (int r = 0; r < TR; ++r) {
-      const bool live = m0 + r < M;
-      for (int c = tid; c < kv; c += 256) {
-        Tin* d = tile + r * pitch + c;
-        if (live) cp_async_el(d, T + offM[r] + offK[c]);
-        else *d = Zero<Tin>::v();
-      }
+  } else {  // consecutive threads along a row, all threads busy however short the rows
+    const FastDiv dkv = make_fastdiv((uint32_t)(kv > 0 ? kv : 1));
+    for (int e = tid; e < TR * kv; e += 256) {
+      const int r = (int)fast_div((uint32_t)e, dkv), c = e - r * kv;
+      Tin* d = tile + r * pitch + c;
+      if (m0 + r < M) cp_async_el(d, T + offM[r] + offK[c]);
+      else *d = Zero<Tin>::v();
     }
   }
   cp_async_wait_all();
@@ -933,14 +947,15 @@ __global__ void __launch_bounds__(256) split_rows_kernel(const Tin* __restrict__
     __syncthreads();
   }
   if (rank == 0 && tid < TR && m0 + tid < M) amax[m0 + tid] = rmax[tid];
-  // columns in pairs (kc, Kp and k0 are even): 8-byte stores per plane
-  for (int r = 0; r < TR; ++r) {
-    const int64_t m = m0 + r;
-    if (m >= M) break;
-    const float rm = rmax[r];
-    for (int c = 2 * tid; c < kw; c += 512)
-      w(m, k0 + c, c < kv ? tile[r * pitch + c] : Zero<Tin>::v(), c + 1 < kv ? tile[r * pitch + c + 1] : Zero<Tin>::v(),
-        rm);
+  // columns in pairs (kc, Kp and k0 are even): 8-byte stores per plane; (row, pair) indices
+  // run jointly over the threads, so short rows still keep every thread busy
+  const int hw = kw / 2;
+  const FastDiv dhw = make_fastdiv((uint32_t)(hw > 0 ? hw : 1));
+  const int nrows = (int)min((int64_t)TR, M - m0);
+  for (int e = tid; e < nrows * hw; e += 256) {
+    const int r = (int)fast_div((uint32_t)e, dhw), c = 2 * (e - r * hw);
+    w(m0 + r, k0 + c, c < kv ? tile[r * pitch + c] : Zero<Tin>::v(),
+      c + 1 < kv ? tile[r * pitch + c + 1] : Zero<Tin>::v(), rmax[r]);
   }
   if (cs > 1) cluster_wait();  // peers may read this CTA's maxima until they have arrived
 }

@@ -103,10 +103,9 @@ int gtn_map_apply_prec(gtn_map map, int precision, const void* x, void* y);
  * mixed map); NULL restores the map's own FP64 plan.  fp64_map is not owned: keep it alive
  * while it is set.  No counterpart in the reference (its maps are FP64 only). */
 int gtn_map_set_fp64(gtn_map map, gtn_map fp64_map);
-/* Same with HOST buffers (one call): pageable buffers go through host->device and
- * device->host copies; page-locked buffers (cudaHostAlloc / cudaHostRegister, e.g. a
- * Julia Mem.pin'ed array) are read and written in place by the map's first and last
- * kernels, with no staging copy in device memory. */
+/* Same with HOST buffers (one call): host->device copy into a staging buffer the map
+ * keeps, apply, device->host copy.  Page-locked buffers (cudaHostAlloc / cudaHostRegister,
+ * e.g. a Julia Mem.pin'ed array) make both copies DMA transfers at the link's rate. */
 int gtn_map_apply_host(gtn_map map, const void* x_host, void* y_host);
 /* Shape/cost facts: elements of x and y, algorithmic FLOPs per apply (complex MAC = 8),
  * number of pair steps, and device workspace bytes held by the map. */

@@ -66,9 +66,9 @@ def test_map_apply_host_matches_device_and_oracle(ctx, headline_small, precision
 
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp16x3", 2e-5)])
-def test_map_apply_host_page_locked_in_place(ctx, headline_small, precision, tol):
-    # page-locked host buffers are read and written in place by the map's kernels (no
-    # staging copies): the result equals the device apply bit for bit, twice in a row
+def test_map_apply_host_page_locked(ctx, headline_small, precision, tol):
+    # page-locked host buffers (the binding's fast path): the result equals the device
+    # apply bit for bit, twice in a row
     import ctypes as C
     import torch
     x_shape, labels, order, statics, theta, ref = headline_small
