@@ -929,6 +929,15 @@ def grad_segment(ctx, D=128, precisions=("fp64", "fp16x3")):
     return out
 
 
+def run_u1(args):
+    """The U(1) block-sparse map alone (see bench_u1)."""
+    import grafttn as G
+    ctx = G.default_context(0)
+    out = {"metric": "U(1) eff_h2 applies/s", "unit": "applies/s"}
+    out.update(bench_u1(ctx, args.steps))
+    print(json.dumps(out), flush=True)
+
+
 def run_grad(args):
     """The gradient workload alone at --grad-D (see grad_segment)."""
     import grafttn as G
@@ -1012,6 +1021,8 @@ def main():
     ap.add_argument("--grad", action="store_true", help="measure the gradient workload (bin31 XXZ)")
     ap.add_argument("--grad-D", type=int, default=128)
     ap.add_argument("--grad-precisions", default="fp64,fp16x3")
+    ap.add_argument("--u1", action="store_true",
+                    help="measure only the U(1) block-sparse eff_h2 map (bin63-derived block tree, D=1024)")
     ap.add_argument("--cbe", action="store_true", help="measure TDVP1_CBE steps (85-site 4-ary TFI)")
     ap.add_argument("--cbe-maxdim", type=int, default=32)
     ap.add_argument("--cbe-steps", type=int, default=5)
@@ -1031,10 +1042,10 @@ def main():
         from grafttn import _lib as GL
         GL.tc_tuning(args.tc_tuning)
     try:
-        if args.dmrg or args.grad or args.cbe or args.lanczos or args.svd:
+        if args.dmrg or args.grad or args.cbe or args.lanczos or args.svd or args.u1:
             if rank == 0:
                 (run_dmrg if args.dmrg else run_lanczos if args.lanczos else run_svd if args.svd
-                 else run_grad if args.grad else run_cbe)(args)
+                 else run_grad if args.grad else run_u1 if args.u1 else run_cbe)(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:

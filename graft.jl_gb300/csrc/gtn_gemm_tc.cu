@@ -201,6 +201,10 @@ __device__ __forceinline__ void tc_tile(const CUtensorMap* tmA, const CUtensorMa
 constexpr int BKE2 = 32;
 // CPS = CTAs resident per SM: with 2, one CTA's epilogue overlaps the other's mainloop
 // (short-K steps, where the prologue and epilogue of a one-tile CTA dominate).
+// Threads of a split-plane tile CTA: warps 0-3 hold the TMA, MMA and TMEM-allocation roles
+// (one lane each), and all 8 warps drain the accumulators (two per TMEM lane quarter).
+constexpr int kPsThreads = 256;
+
 template <int BN, int P, int CPS = 1> struct Cfg2 {
   static constexpr int A_PLANE = BM * BKE2 * 2;   // 8 KB
   static constexpr int B_PLANE = BN * BKE2 * 2;
@@ -333,14 +337,16 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
   __syncwarp();
   fence_after();
   if (ok) {
-    const int row = warp * 32 + lane;
+    // 8 warps: warp w drains TMEM lane quarter w % 4, columns of half w / 4 of the tile
+    const int q4 = warp & 3, c0 = (warp >> 2) * (BN / 2);
+    const int row = q4 * 32 + lane;
     const int64_t m = (int64_t)m0 + row;
-    const uint32_t taddr = tmem_d + ((uint32_t)(warp * 32) << 16);
+    const uint32_t taddr = tmem_d + ((uint32_t)(q4 * 32) << 16);
     bool has_corr = false;
     for (int q = 0; q < prods.n; ++q) has_corr |= !(prods.a[q] == 0 && prods.b[q] == 0);
     const float ainv = (sc.amax && m < M) ? fp16_row_scale_inv(sc.amax[m]) : 1.0f;
 #pragma unroll 1
-    for (int c = 0; c < BN; c += 16) {
+    for (int c = c0; c < c0 + BN / 2; c += 16) {
       uint32_t v[16], w[16];
       tmem_ld16(taddr + (uint32_t)c, v);
       if (has_corr) {
@@ -381,7 +387,7 @@ __device__ __forceinline__ void tc_tile_ps(const CUtensorMap* tmA, const CUtenso
 }
 
 template <int BN, int P, int CPS>
-__global__ void __launch_bounds__(128, CPS)
+__global__ void __launch_bounds__(kPsThreads, CPS)
     tc_gemm_ps_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       float2* __restrict__ C, int64_t M, int64_t N, int nkb, ProdList prods,
                       int* __restrict__ errflag, PlaneScales sc, int tiles_n) {
@@ -693,7 +699,7 @@ struct GroupedTc {
 };
 
 template <int BN, int P>
-__global__ void __launch_bounds__(128, 1) tc_gemm_grouped_ps_kernel(const __grid_constant__ GroupedTc g,
+__global__ void __launch_bounds__(kPsThreads, 1) tc_gemm_grouped_ps_kernel(const __grid_constant__ GroupedTc g,
                                                                     int* __restrict__ errflag) {
   constexpr int CPS = 1;
   const int b = blockIdx.x;
@@ -713,7 +719,9 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_grouped_ps_kernel(const __grid
 //   warp 0 (one lane) : TMA producer over the CTA's (tile, k-block) sequence, one ring of
 //                       stages shared by all its tiles (no pipeline drain between tiles)
 //   warp 1 (one lane) : MMA issuer; warp 1 also allocates and frees TMEM
-//   warps 2-5         : epilogue; warp w reads TMEM lanes 32 (w % 4) .. + 31
+//   warps 2-9         : epilogue; warp w reads TMEM lanes 32 (w % 4) .. + 31 and one half of
+//                       the tile's columns (two warps per lane quarter keep twice the
+//                       TMEM loads and stores in flight)
 // With 128-wide (or narrower) tiles TMEM holds two accumulator sets (lead + corrections
 // each), so the epilogue of tile i runs while the MMAs of tile i + 1 proceed; 256-wide tiles
 // fill TMEM with one set.  Accumulator hand-off: full barriers (one MMA commit) and empty
@@ -734,9 +742,12 @@ __device__ __forceinline__ int find_problem(const GroupedTc& g, int t) {
   return p;
 }
 
+constexpr int kPersistEpiWarps = 8;
+constexpr int kPersistThreads = 32 * (2 + kPersistEpiWarps);
+
 template <int BN, int P>
-__global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_constant__ GroupedTc g,
-                                                                 int* __restrict__ errflag) {
+__global__ void __launch_bounds__(kPersistThreads, 1) tc_gemm_persist_kernel(const __grid_constant__ GroupedTc g,
+                                                                             int* __restrict__ errflag) {
   using CF = CfgPersist<BN, P>;
   using B2 = Cfg2<BN, P, 1>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -746,7 +757,7 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
   __shared__ __align__(8) uint64_t empty_bar[CF::STAGES];
   __shared__ __align__(8) uint64_t accf_bar[2];
   __shared__ __align__(8) uint64_t acce_bar[2];
-  __shared__ float s_binv[4][BN / 2 > 0 ? BN / 2 : 1];
+  __shared__ float s_binv[kPersistEpiWarps][BN / 4 > 0 ? BN / 4 : 1];
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
   __shared__ int n_issued, n_consumed;
@@ -760,7 +771,7 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf_bar[b], 1);
-      mbar_init(&acce_bar[b], 4);
+      mbar_init(&acce_bar[b], kPersistEpiWarps);
     }
     abort_flag = 0;
     n_issued = 0;
@@ -852,7 +863,8 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
     }
     n_consumed = gk;
   } else if (warp >= 2) {
-    const int q4 = warp & 3;  // TMEM lane quarter of this warp
+    const int q4 = warp & 3;                // TMEM lane quarter of this warp
+    const int c0 = ((warp - 2) >> 2) * (BN / 2);  // its half of the tile's columns
     int i = 0;
     bool has_corr = false;
     for (int q = 0; q < g.prods.n; ++q) has_corr |= !(g.prods.a[q] == 0 && g.prods.b[q] == 0);
@@ -879,17 +891,17 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
       const uint32_t taddr = tmem_base + (uint32_t)b * 2u * CF::ACC_COLS + ((uint32_t)(q4 * 32) << 16);
       const float ainv = (g.amax[p] && m < M) ? fp16_row_scale_inv(g.amax[p][m]) : 1.0f;
       const float* bmx = g.bmax[p];
-      // this warp's copy of the tile's inverse column scales (read once per tile)
+      // this warp's copy of its columns' inverse scales (read once per tile)
       float* binv = s_binv[warp - 2];
       if (bmx) {
-        for (int t = lane; t < BN / 2; t += 32) {
-          const int64_t n = (int64_t)(r0 >> 1) + t;
+        for (int t = lane; t < BN / 4; t += 32) {
+          const int64_t n = (int64_t)((r0 + c0) >> 1) + t;
           binv[t] = n < N ? fp16_row_scale_inv(bmx[n]) : 1.0f;
         }
         __syncwarp();
       }
 #pragma unroll 1
-      for (int c = 0; c < BN; c += 16) {
+      for (int c = c0; c < c0 + BN / 2; c += 16) {
         uint32_t v[16], w[16];
         tmem_ld16(taddr + (uint32_t)c, v);
         if (has_corr) {
@@ -904,7 +916,7 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
           for (int j = 0; j < 8; ++j) {
             const int64_t n = nb + j;
             if (n < N) {
-              const float f = bmx ? ainv * binv[(c >> 1) + j] : ainv;
+              const float f = bmx ? ainv * binv[((c - c0) >> 1) + j] : ainv;
               C[n * M + m] = make_float2((__uint_as_float(v[2 * j]) + __uint_as_float(w[2 * j])) * f,
                                          (__uint_as_float(v[2 * j + 1]) + __uint_as_float(w[2 * j + 1])) * f);
             }
@@ -1001,7 +1013,7 @@ cudaError_t launch_ps(const TcGemmArgs& a, int* errflag, cudaStream_t s, std::st
   const int64_t gy = (2 * a.N + BN - 1) / BN;
   if (gx * gy > 2147483647LL) return cudaErrorInvalidConfiguration;
   const PlaneScales sc{a.a_max, a.b_max, a.fp16};
-  tc_gemm_ps_kernel<BN, P, CPS><<<(unsigned)(gx * gy), 128, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb, pl, errflag, sc,
+  tc_gemm_ps_kernel<BN, P, CPS><<<(unsigned)(gx * gy), kPsThreads, CF::SMEM, s>>>(tmA, tmB, a.C, a.M, a.N, nkb, pl, errflag, sc,
                                                                      (int)gy);
   return cudaGetLastError();
 }
@@ -1019,7 +1031,7 @@ int device_sm_count() {
 }
 
 // Grouped problems, at most kTcGroupMax per launch.  Persist: one persistent launch of
-// min(tiles, SM count) CTAs of 192 threads (tc_gemm_persist_kernel); otherwise one CTA per
+// min(tiles, SM count) CTAs of 320 threads (tc_gemm_persist_kernel); otherwise one CTA per
 // tile (tc_gemm_grouped_ps_kernel).
 template <int BN, int P, bool Persist>
 cudaError_t launch_grouped_ps(const TcGemmArgs* probs, int nprob, int* errflag, cudaStream_t s, std::string* why) {
@@ -1062,9 +1074,9 @@ cudaError_t launch_grouped_ps(const TcGemmArgs* probs, int nprob, int* errflag, 
     }
     if (tiles == 0) continue;
     if (Persist)
-      tc_gemm_persist_kernel<BN, P><<<std::min(tiles, device_sm_count()), 192, CF::SMEM, s>>>(g, errflag);
+      tc_gemm_persist_kernel<BN, P><<<std::min(tiles, device_sm_count()), kPersistThreads, CF::SMEM, s>>>(g, errflag);
     else
-      tc_gemm_grouped_ps_kernel<BN, P><<<tiles, 128, CF::SMEM, s>>>(g, errflag);
+      tc_gemm_grouped_ps_kernel<BN, P><<<tiles, kPsThreads, CF::SMEM, s>>>(g, errflag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
