@@ -10,21 +10,39 @@
 #include "gtn_internal.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <new>
+#include <utility>
 
 struct BMStep {
   DevGatherJob* jobs = nullptr;  // device table
-  int* tiles = nullptr;          // device prefix sums
+  int2* tiles = nullptr;         // (job, tile within the job) of every CTA
   int njobs = 0, ntiles = 0;
   DevGatherJob* mjobs = nullptr; // fp16 row-maxima pass (before the split)
-  int* mtiles = nullptr;
+  int2* mtiles = nullptr;
   int nmjobs = 0, nmtiles = 0;
   int64_t amax_elems = 0;        // row maxima zeroed before that pass
   int src_is64 = 0;
   std::vector<TcGemmArgs> tcp;   // tcgen05 problems (addresses fixed at creation)
   std::vector<GemmJob> simt;     // SIMT problems
   std::vector<GemmJob> skinny;   // SIMT problems with N <= 32
+  DevBand* bands = nullptr;      // fused gather + product of the few-column problems
+  DevBandWork* bwork = nullptr;  // CTA work items over the bands
+  DevBandCol* cols = nullptr;
+  int64_t* rstr = nullptr;
+  int nbands = 0, nbwork = 0, band_maxn = 0;
+  size_t band_smem = 0;
+};
+
+// Bands of a step on the host, before upload.
+struct BandSet {
+  std::vector<DevBand> bands;
+  std::vector<DevBandCol> cols;
+  std::vector<int64_t> rstr;
+  int maxn = 0;
+  size_t smem = 0;
 };
 
 struct gtn_blockmap_s {
@@ -86,36 +104,189 @@ void set_prods(TcGemmArgs& a, int P) {
 }
 
 // Upload a job table with its tile prefix sums.
-cudaError_t upload_table(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, DevGatherJob** djobs, int** dtiles,
+cudaError_t upload_table(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, DevGatherJob** djobs, int2** dtiles,
                          int* njobs, int* ntiles);
 
 cudaError_t upload_jobs(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, BMStep* st) {
   return upload_table(bm, jobs, &st->jobs, &st->tiles, &st->njobs, &st->ntiles);
 }
 
-cudaError_t upload_table(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, DevGatherJob** djobs, int** dtiles,
+cudaError_t upload_table(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, DevGatherJob** djobs, int2** dtiles,
                          int* njobs, int* ntiles) {
-  std::vector<int> start(jobs.size() + 1, 0);
-  int tiles = 0;
+  std::vector<int2> map;
   for (size_t i = 0; i < jobs.size(); ++i) {
     finish_dev_gather_job(&jobs[i]);
-    start[i] = tiles;
-    if (jobs[i].M > 0 && jobs[i].Kw > 0)
-      tiles += jobs[i].tiles_m * (int)((jobs[i].Kw + (1 << jobs[i].tks) - 1) >> jobs[i].tks);
+    if (jobs[i].M > 0 && jobs[i].Kw > 0) {
+      const int nt = jobs[i].tiles_m * (int)((jobs[i].Kw + (1 << jobs[i].tks) - 1) >> jobs[i].tks);
+      for (int t = 0; t < nt; ++t) map.push_back(make_int2((int)i, t));
+    }
   }
-  start[jobs.size()] = tiles;
+  const int tiles = (int)map.size();
   *njobs = (int)jobs.size();
   *ntiles = tiles;
   if (jobs.empty()) return cudaSuccess;
   cudaError_t e = cudaMalloc(djobs, jobs.size() * sizeof(DevGatherJob));
   if (e != cudaSuccess) return e;
   bm->owned.push_back(*djobs);
-  e = cudaMalloc(dtiles, start.size() * sizeof(int));
+  e = cudaMalloc(dtiles, std::max<size_t>(map.size(), 1) * sizeof(int2));
   if (e != cudaSuccess) return e;
   bm->owned.push_back(*dtiles);
   e = cudaMemcpy(*djobs, jobs.data(), jobs.size() * sizeof(DevGatherJob), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return e;
-  return cudaMemcpy(*dtiles, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess || map.empty()) return e;
+  return cudaMemcpy(*dtiles, map.data(), map.size() * sizeof(int2), cudaMemcpyHostToDevice);
+}
+
+// Upload the bands of a step with their work items, column table and row strides.  A work
+// item is 1 to 8 passes of one CTA over a band's rows (a pass covers 256 / G rows, G threads
+// per row), about 16384 loads, so that each CTA's set-up (band, B_q, strides, columns) is
+// paid once over several passes while the grid keeps every SM busy.
+cudaError_t upload_bands(gtn_blockmap bm, const BandSet& bs, BMStep* st) {
+  std::vector<DevBandWork> work;
+  const int64_t rb = block_band_rows_per_pass(bs.maxn);
+  for (size_t i = 0; i < bs.bands.size(); ++i) {
+    const int64_t M = bs.bands[i].M;
+    const int64_t passes = std::min<int64_t>(8, std::max<int64_t>(1, 16384 / (rb * std::max(bs.bands[i].ncol, 1))));
+    const int64_t per = rb * passes;
+    for (int64_t m = 0; m < M; m += per) {
+      DevBandWork w;
+      w.band = (int)i;
+      w.nrows = (int)std::min<int64_t>(per, M - m);
+      w.m0 = m;
+      work.push_back(w);
+    }
+  }
+  st->nbands = (int)bs.bands.size();
+  st->nbwork = (int)work.size();
+  st->band_maxn = bs.maxn;
+  st->band_smem = bs.smem;
+  if (bs.bands.empty()) return cudaSuccess;
+  auto put = [&](void** dst, const void* src, size_t bytes) {
+    cudaError_t e = cudaMalloc(dst, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return e;
+    bm->owned.push_back(*dst);
+    return bytes ? cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+  };
+  cudaError_t e = put(reinterpret_cast<void**>(&st->bands), bs.bands.data(), bs.bands.size() * sizeof(DevBand));
+  if (e == cudaSuccess) e = put(reinterpret_cast<void**>(&st->bwork), work.data(), work.size() * sizeof(DevBandWork));
+  if (e == cudaSuccess) e = put(reinterpret_cast<void**>(&st->cols), bs.cols.data(), bs.cols.size() * sizeof(DevBandCol));
+  if (e == cudaSuccess) e = put(reinterpret_cast<void**>(&st->rstr), bs.rstr.data(), bs.rstr.size() * sizeof(int64_t));
+  return e;
+}
+
+int64_t host_decompose(int64_t i, int n, const int64_t* dim, const int64_t* str) {
+  int64_t off = 0;
+  for (int j = n - 1; j >= 0; --j) {
+    const int64_t q = i / dim[j];
+    off += (i - q * dim[j]) * str[j];
+    i = q;
+  }
+  return off;
+}
+
+// The bands of one few-column problem: its gathers grouped by first row.  Returns false
+// (the problem then takes the staged path) when a band cannot be read in place: rectangles
+// of one band with different rows or sources, row groups with no common refinement, more
+// than kBandMaxRects rectangles, or more than kBandMaxGroups common groups.
+bool plan_bands(const gtn_block_gemm& g, const std::vector<const gtn_block_gather*>& gs, const void* Bq, int fp64,
+                BandSet* out) {
+  std::map<int64_t, std::vector<const gtn_block_gather*>> by_row;
+  for (const gtn_block_gather* d : gs) by_row[d->row_off].push_back(d);
+  BandSet loc;
+  for (const auto& kv : by_row) {
+    const int64_t M = kv.second[0]->M;
+    if (M <= 0 || M >= (int64_t(1) << 31)) return false;
+    std::vector<const gtn_block_gather*> present;
+    for (const gtn_block_gather* d : kv.second) {
+      if (d->M != M) return false;
+      if (d->K > 0) present.push_back(d);
+    }
+    if ((int)present.size() > kBandMaxRects) return false;
+    // common refinement of the rectangles' row groups: the union of their cumulative
+    // products from the fastest group, each dividing the next
+    std::vector<int64_t> bounds{1, M};
+    for (const gtn_block_gather* d : present) {
+      int64_t c = 1;
+      for (int j = d->ng_m - 1; j >= 0; --j) {
+        if (d->m_dim[j] < 1) return false;
+        c *= d->m_dim[j];
+        bounds.push_back(c);
+      }
+      if (c != M) return false;
+    }
+    std::sort(bounds.begin(), bounds.end());
+    bounds.erase(std::unique(bounds.begin(), bounds.end()), bounds.end());
+    for (size_t t = 1; t < bounds.size(); ++t)
+      if (bounds[t] % bounds[t - 1] != 0) return false;
+    const int ng = (int)bounds.size() - 1;
+    if (ng > kBandMaxGroups) return false;
+    DevBand D;
+    std::memset(&D, 0, sizeof(D));
+    D.M = M;
+    D.c_off = g.c_off + kv.first;
+    D.ldc = g.M;
+    D.B = Bq;
+    D.N = (int)g.N;
+    D.Kq = (int)g.K;
+    D.c_buf = g.c_buf;
+    D.src_buf = present.empty() ? 0 : present[0]->src_buf;
+    D.ng = ng;
+    for (int t = 0; t < ng; ++t) {  // group t (slowest first) spans cumulative [bounds[u], bounds[u + 1])
+      const int u = ng - 1 - t;
+      const int64_t d = bounds[u + 1] / bounds[u];
+      D.dim[t] = (uint32_t)d;
+      int l = 0;
+      while ((int64_t(1) << l) < d) ++l;
+      D.mag[t] = d == 1 ? 0u : (uint32_t)(((uint64_t)1 << (31 + l)) / (uint64_t)d + 1);
+      D.sh[t] = d == 1 ? 0u : (uint32_t)(l - 1);
+    }
+    D.rs0 = (int)(out->rstr.size() + loc.rstr.size());
+    D.nrect = (int)present.size();
+    D.col0 = (int)(out->cols.size() + loc.cols.size());
+    const gtn_block_gather* widest = nullptr;
+    for (size_t r = 0; r < present.size(); ++r) {
+      const gtn_block_gather* d = present[r];
+      if (d->src_buf != D.src_buf) return false;
+      for (int t = 0; t < ng; ++t) {  // the rectangle's stride of common group t
+        const int u = ng - 1 - t;
+        int64_t c = 1, st = 0;
+        for (int j = d->ng_m - 1; j >= 0; --j) {
+          const int64_t c2 = c * d->m_dim[j];
+          if (bounds[u] >= c && bounds[u + 1] <= c2) {
+            st = d->m_str[j] * (bounds[u] / c);
+            break;
+          }
+          c = c2;
+        }
+        loc.rstr.push_back(st);
+      }
+      for (int64_t k = 0; k < d->K; ++k) {
+        DevBandCol cc;
+        cc.src = d->src_off + host_decompose(k, d->ng_k, d->k_dim, d->k_str);
+        cc.rect = (int32_t)r;
+        cc.bcol = (int32_t)(d->col_off + k);
+        loc.cols.push_back(cc);
+      }
+      if (!widest || d->K > widest->K) widest = d;
+    }
+    D.ncol = (int)(out->cols.size() + loc.cols.size()) - D.col0;
+    if (widest) {  // load along rows when the widest block's rows are nearer in memory than its columns
+      int64_t rmin = INT64_MAX, kmin = INT64_MAX;
+      for (int j = 0; j < widest->ng_m; ++j)
+        if (widest->m_dim[j] > 1) rmin = std::min<int64_t>(rmin, std::abs(widest->m_str[j]));
+      for (int j = 0; j < widest->ng_k; ++j)
+        if (widest->k_dim[j] > 1) kmin = std::min<int64_t>(kmin, std::abs(widest->k_str[j]));
+      D.m_fast = rmin < kmin ? 1 : 0;
+    }
+    loc.maxn = std::max(loc.maxn, D.N);
+    loc.smem = std::max(loc.smem, block_band_smem(D.N, D.Kq, D.nrect, D.ng, fp64));
+    loc.bands.push_back(D);
+  }
+  out->bands.insert(out->bands.end(), loc.bands.begin(), loc.bands.end());
+  out->cols.insert(out->cols.end(), loc.cols.begin(), loc.cols.end());
+  out->rstr.insert(out->rstr.end(), loc.rstr.begin(), loc.rstr.end());
+  out->maxn = std::max(out->maxn, loc.maxn);
+  out->smem = std::max(out->smem, loc.smem);
+  return true;
 }
 
 int run(gtn_blockmap bm, const double2* x, double2* y) {
@@ -136,12 +307,14 @@ int run(gtn_blockmap bm, const double2* x, double2* y) {
     const BMStep& st = bm->steps[si];
     if (st.nmjobs > 0) {
       e = cudaMemsetAsync(bm->amax, 0, (size_t)st.amax_elems * sizeof(float), s);
-      if (e == cudaSuccess) e = launch_block_rowmax(st.mjobs, st.mtiles, st.nmjobs, st.nmtiles, bases, st.src_is64, s);
+      if (e == cudaSuccess) e = launch_block_rowmax(st.mjobs, st.mtiles, st.nmtiles, bases, st.src_is64, s);
       ctx->launches++;
       if (e != cudaSuccess) break;
     }
-    e = launch_block_gather(st.jobs, st.tiles, st.njobs, st.ntiles, bases, st.src_is64, s);
-    ctx->launches++;
+    if (st.ntiles > 0) {
+      e = launch_block_gather(st.jobs, st.tiles, st.ntiles, bases, st.src_is64, s);
+      ctx->launches++;
+    }
     if (e == cudaSuccess && !st.tcp.empty()) {
       e = launch_tc_gemm_grouped(st.tcp.data(), (int)st.tcp.size(), ctx->d_errflag, s, &why);
       ctx->launches += (int64_t)((st.tcp.size() + 55) / 56);
@@ -154,9 +327,14 @@ int run(gtn_blockmap bm, const double2* x, double2* y) {
       e = launch_gemm_skinny_grouped(st.skinny.data(), (int)st.skinny.size(), fp64 ? 1 : 0, s);
       ctx->launches += (int64_t)((st.skinny.size() + kGemmJobMax - 1) / kGemmJobMax);
     }
+    if (e == cudaSuccess && st.nbwork > 0) {
+      e = launch_block_band(st.bands, st.bwork, st.nbwork, st.cols, st.rstr, bases, st.src_is64, fp64 ? 1 : 0,
+                            st.band_maxn, st.band_smem, s);
+      ctx->launches++;
+    }
   }
   if (e == cudaSuccess) {
-    e = launch_block_gather(bm->fin.jobs, bm->fin.tiles, bm->fin.njobs, bm->fin.ntiles, bases, bm->fin.src_is64, s);
+    e = launch_block_gather(bm->fin.jobs, bm->fin.tiles, bm->fin.ntiles, bases, bm->fin.src_is64, s);
     ctx->launches++;
   }
   if (e != cudaSuccess) return set_err(ctx, GTN_ERR_CUDA, "block map: " + why + " " + cudaGetErrorString(e));
@@ -249,6 +427,8 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
   const bool tc = is_tc_p(precision);
   const bool f16 = precision == GTN_PREC_FP16X3;
   const int P = tc ? planes_p(precision) : 0;
+  const char* band_env = std::getenv("GTN_BLOCK_BANDS");
+  const bool bands_on = !(band_env && band_env[0] == '0');
   auto fail = [&](int code, const std::string& msg) {
     cudaStreamSynchronize(ctx->stream);
     bm_free(bm);
@@ -316,22 +496,43 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
   std::vector<std::vector<int64_t>> step_mbase;  // fp16: first row-maximum slot of each problem
   std::vector<int64_t> step_mrows;
   int64_t amax_need = 0;
+  std::vector<BandSet> step_bands(nsteps);
+  int64_t gv = 0;
   for (int s = 0; s < nsteps; ++s) {
     std::vector<gtn_block_gemm> gm(gemms + mo, gemms + mo + step_ngemm[s]);
     mo += step_ngemm[s];
+    for (const gtn_block_gemm& g : gm)
+      if (g.b_index < 0 || g.b_index >= nstatics || g.c_buf < 2 || g.c_buf > 3 || bm->bN[g.b_index] != g.N ||
+          bm->bK[g.b_index] != g.K || g.M <= 0)
+        return fail(GTN_ERR_INVALID, "bad GEMM descriptor in step " + std::to_string(s));
+    std::vector<std::vector<const gtn_block_gather*>> per_q(gm.size());
+    for (int i = 0; i < step_ngather[s]; ++i) {
+      const gtn_block_gather& d = gathers[gv + i];
+      if (d.dst_index < 0 || d.dst_index >= (int)gm.size() || d.ng_m < 0 || d.ng_k < 0 ||
+          d.ng_m > GTN_BLOCK_MAXG || d.ng_k > GTN_BLOCK_MAXG || (d.src_buf != 0 && d.src_buf != 2 && d.src_buf != 3))
+        return fail(GTN_ERR_INVALID, "bad gather descriptor in step " + std::to_string(s));
+      const gtn_block_gemm& g = gm[d.dst_index];
+      if (d.M < 0 || d.K < 0 || d.Kw < d.K || d.row_off < 0 || d.col_off < 0 || d.row_off + d.M > g.M ||
+          d.col_off + d.Kw > g.K)
+        return fail(GTN_ERR_INVALID, "gather rectangle outside its problem in step " + std::to_string(s));
+      per_q[d.dst_index].push_back(&d);
+    }
+    gv += step_ngather[s];
     std::vector<size_t> aoff;
     std::vector<int64_t> kp;
     std::vector<char> use_tc;
     size_t off = 0;
-    for (const gtn_block_gemm& g : gm) {
-      if (g.b_index < 0 || g.b_index >= nstatics || g.c_buf < 2 || g.c_buf > 3 || bm->bN[g.b_index] != g.N ||
-          bm->bK[g.b_index] != g.K || g.M <= 0)
-        return fail(GTN_ERR_INVALID, "bad GEMM descriptor in step " + std::to_string(s));
+    for (size_t q = 0; q < gm.size(); ++q) {
+      const gtn_block_gemm& g = gm[q];
       const bool t = tc && g.K >= kTcMinK && g.N >= kTcMinN;
-      use_tc.push_back(t ? 1 : 0);
+      const void* Bq = fp64 ? static_cast<const void*>(bm->b64[g.b_index]) : static_cast<const void*>(bm->b32[g.b_index]);
+      const bool band = !t && bands_on && block_band_fits(g.N, g.K, fp64 ? 1 : 0) &&
+                        plan_bands(g, per_q[q], Bq, fp64 ? 1 : 0, &step_bands[s]);
+      use_tc.push_back(t ? 1 : band ? 2 : 0);
       const int64_t k = t ? ((g.K + 31) / 32) * 32 : g.K;
       kp.push_back(k);
       aoff.push_back(off);
+      if (band) continue;  // read straight from the running tensor: no staged operand
       off += t ? (size_t)P * g.M * 2 * k * sizeof(__nv_bfloat16) : (size_t)g.M * g.K * te;
       off = (off + 255) / 256 * 256;
     }
@@ -340,7 +541,7 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
     std::vector<int64_t> mbase;
     for (size_t q = 0; q < gm.size(); ++q) {
       mbase.push_back(mrows);
-      if (use_tc[q]) mrows += gm[q].M;
+      if (use_tc[q] == 1) mrows += gm[q].M;
     }
     step_mbase.push_back(mbase);
     step_mrows.push_back(mrows);
@@ -371,11 +572,9 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
     const auto& gm = step_gemms[s];
     std::vector<DevGatherJob> jobs, mjobs;
     for (int i = 0; i < step_ngather[s]; ++i) {
-      const gtn_block_gather& d = gathers[go + i];
-      if (d.dst_index < 0 || d.dst_index >= (int)gm.size() || d.ng_m > GTN_BLOCK_MAXG || d.ng_k > GTN_BLOCK_MAXG ||
-          (d.src_buf != 0 && d.src_buf != 2 && d.src_buf != 3))
-        return fail(GTN_ERR_INVALID, "bad gather descriptor in step " + std::to_string(s));
+      const gtn_block_gather& d = gathers[go + i];  // validated above
       const int q = d.dst_index;
+      if (step_tc[s][q] == 2) continue;  // read in place by its problem's bands
       DevGatherJob J;
       std::memset(&J, 0, sizeof(J));
       to_groups(d, &J.mg, &J.kg);
@@ -405,6 +604,10 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
     go += step_ngather[s];
     for (size_t q = 0; q < gm.size(); ++q) {
       const gtn_block_gemm& g = gm[q];
+      if (step_tc[s][q] == 2) {
+        bm->n_problems++;
+        continue;
+      }
       if (step_tc[s][q]) {
         if (step_kp[s][q] > g.K) {  // zero the K padding of the operand planes
           DevGatherJob J;
@@ -459,6 +662,7 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
     std::stable_sort(st.tcp.begin(), st.tcp.end(), [](const TcGemmArgs& a, const TcGemmArgs& b) { return a.Kp > b.Kp; });
     st.src_is64 = (s == 0 || fp64) ? 1 : 0;
     if (upload_jobs(bm, jobs, &st) != cudaSuccess) return fail(GTN_ERR_CUDA, "job table upload");
+    if (upload_bands(bm, step_bands[s], &st) != cudaSuccess) return fail(GTN_ERR_CUDA, "band table upload");
     st.amax_elems = step_mrows[s];
     if (!mjobs.empty() &&
         upload_table(bm, mjobs, &st.mjobs, &st.mtiles, &st.nmjobs, &st.nmtiles) != cudaSuccess)

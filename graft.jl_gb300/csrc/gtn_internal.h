@@ -177,10 +177,46 @@ struct DevGatherJob {
   uint32_t m_sh[GTN_MAXG];
 };
 void finish_dev_gather_job(DevGatherJob* J);
-cudaError_t launch_block_rowmax(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
-                                const BlockBases& bases, int src_is64, cudaStream_t s);
-cudaError_t launch_block_gather(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
-                                const BlockBases& bases, int src_is64, cudaStream_t s);
+// tile_map[b] = (job, tile within the job) of CTA b: one load instead of a search.
+cudaError_t launch_block_rowmax(const DevGatherJob* jobs, const int2* tile_map, int ntiles, const BlockBases& bases,
+                                int src_is64, cudaStream_t s);
+cudaError_t launch_block_gather(const DevGatherJob* jobs, const int2* tile_map, int ntiles, const BlockBases& bases,
+                                int src_is64, cudaStream_t s);
+// Fused gather + product for coupled-charge problems with few output columns (block maps):
+// a band is the rows [row_off, row_off + M) of A_q, read straight from the running tensor,
+// C_q[n][row_off + m] = sum_j A_q[row_off + m][bcol_j] * B_q[n][bcol_j] over the band's
+// present columns j, with no staged copy of A_q.  Column j lives at
+// src_j + sum_t digit_t(m) * rstr[rect_j][t]: the digits of m in the band's common row
+// groups (the refinement of every rectangle's row groups) and the strides of column j's
+// rectangle (source block) in those groups.
+struct DevBandCol {
+  int64_t src;   // element offset of the column in bases.buf[src_buf] (block offset + column offset)
+  int32_t rect;  // its rectangle within the band
+  int32_t bcol;  // its column of B_q
+};
+struct DevBand {
+  int64_t M;       // rows of the band
+  int64_t c_off;   // element offset of C_q[0][row_off] in bases.buf[c_buf]
+  int64_t ldc;     // M_q: the pitch between output columns n
+  const void* B;   // B_q [N][Kq] in the compute type
+  int N, Kq, c_buf, src_buf;
+  int col0, ncol;  // present columns: cols[col0, col0 + ncol)
+  int rs0, nrect;  // row strides: rstr[rs0 + rect * ng + t]
+  int ng, m_fast;  // common row groups (slowest first); loads run along rows when m_fast
+  uint32_t dim[GTN_MAXG], mag[GTN_MAXG], sh[GTN_MAXG];  // group sizes and their division magic
+};
+// A CTA's share of a band: the rows [m0, m0 + nrows).
+struct DevBandWork {
+  int band, nrows;
+  int64_t m0;
+};
+constexpr int kBandMaxRects = 64, kBandMaxGroups = 6;
+bool block_band_fits(int64_t N, int64_t Kq, int fp64);
+int block_band_rows_per_pass(int maxn);  // rows a CTA covers per pass (256 / threads per row)
+size_t block_band_smem(int N, int Kq, int nrect, int ng, int fp64);
+cudaError_t launch_block_band(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
+                              const int64_t* rstr, const BlockBases& bases, int src_is64, int fp64, int maxn,
+                              size_t smem, cudaStream_t s);
 cudaError_t launch_small_grouped(const SmallJob* jobs, int njobs, int is64, cudaStream_t s);
 
 // C[n][m] = sum_k T[offM(m) + offK(k)] * B[n][k]   (small K; B in shared memory)

@@ -27,8 +27,32 @@ template <typename T> struct Zero;
 template <> struct Zero<double2> { __device__ static double2 v() { return make_double2(0.0, 0.0); } };
 template <> struct Zero<float2> { __device__ static float2 v() { return make_float2(0.f, 0.f); } };
 
+// Complex FP64 inputs of FP32 copies and of the fp16 and bf16 slice planes are converted with
+// integer operations on the doubles' bits: on this part FP64 arithmetic and the F64->F32
+// conversion run far below the integer rate and bounded the c128 splits (a multiply,
+// conversions and subtractions per value).
+// x * 2^shift rounded to float (nearest, ties to even); magnitudes below FLT_MIN become a
+// signed zero (far below the fp16 planes' resolution after the row scaling, and 2^-126 of any
+// FP32 or bf16 operand of practical size), NaN stays NaN.
+__device__ __forceinline__ float d2f_scaled_rn(double x, int shift) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned long long mag = b & 0x7fffffffffffffffull;
+  const uint32_t sgn = static_cast<uint32_t>(b >> 32) & 0x80000000u;
+  const int E = static_cast<int>(mag >> 52);
+  const unsigned long long m52 = mag & 0xfffffffffffffull;
+  if (E == 0x7ff) return __uint_as_float(sgn | (m52 ? 0x7fc00000u : 0x7f800000u));
+  if (E == 0) return __uint_as_float(sgn);
+  const int fe = E - 1023 + shift + 127;  // biased float exponent before rounding
+  if (fe < 1) return __uint_as_float(sgn);
+  if (fe > 254) return __uint_as_float(sgn | 0x7f800000u);
+  unsigned long long r = (static_cast<unsigned long long>(fe) << 52) | m52;
+  r += 0x0fffffffull + ((r >> 29) & 1ull);  // round half to even at the 29 dropped bits
+  return __uint_as_float(sgn | static_cast<uint32_t>(r >> 29));  // a carry moves into the exponent
+}
 __device__ __forceinline__ double2 cvt(double2 a, double2*) { return a; }
-__device__ __forceinline__ float2 cvt(double2 a, float2*) { return make_float2((float)a.x, (float)a.y); }
+__device__ __forceinline__ float2 cvt(double2 a, float2*) {
+  return make_float2(d2f_scaled_rn(a.x, 0), d2f_scaled_rn(a.y, 0));
+}
 __device__ __forceinline__ float2 cvt(float2 a, float2*) { return a; }
 __device__ __forceinline__ double2 cvt(float2 a, double2*) { return make_double2(a.x, a.y); }
 
@@ -41,14 +65,8 @@ template <typename Tout> struct ComplexWriter {
   }
 };
 
-// Splits x into up to 3 bf16 slices x ~ s0 + s1 + s2 (round-to-nearest each step).
-__device__ __forceinline__ void split3(double x, __nv_bfloat16* s) {
-  __nv_bfloat16 a = __double2bfloat16(x);
-  double r = x - (double)__bfloat162float(a);
-  __nv_bfloat16 b = __double2bfloat16(r);
-  r -= (double)__bfloat162float(b);
-  s[0] = a; s[1] = b; s[2] = __double2bfloat16(r);
-}
+// Splits x into 3 bf16 slices x = s0 + s1 + s2 (round-to-nearest each step; exact for a float,
+// whose 24 significant bits the three 8-bit slices hold).
 __device__ __forceinline__ void split3(float x, __nv_bfloat16* s) {
   __nv_bfloat16 a = __float2bfloat16_rn(x);
   float r = x - __bfloat162float(a);
@@ -56,6 +74,9 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16* s) {
   r -= __bfloat162float(b);
   s[0] = a; s[1] = b; s[2] = __float2bfloat16_rn(r);
 }
+// A double is first rounded to float (nearest, from its bits): the slices then hold x to a
+// relative 2^-25, below the dropped products of the six-product bf16 GEMM.
+__device__ __forceinline__ void split3(double x, __nv_bfloat16* s) { split3(d2f_scaled_rn(x, 0), s); }
 
 // Writer for bf16 slice planes.
 struct SplitWriter {
@@ -272,31 +293,6 @@ __global__ void pack_b_planes_kernel(const double2* __restrict__ B, int64_t N, i
 __device__ __forceinline__ void split16(float x, __half* h, __half* l) {
   *h = __float2half_rn(x);
   *l = __float2half_rn(x - __half2float(*h));
-}
-__device__ __forceinline__ void split16(double x, __half* h, __half* l) {
-  *h = __double2half(x);
-  *l = __double2half(x - (double)__half2float(*h));
-}
-// The complex FP64 inputs of the fp16 planes are handled with integer operations on the
-// doubles' bits: on this part FP64 arithmetic and the F64->F32 conversion run far below the
-// integer rate and bounded the c128 splits (one FP64 multiply, two conversions and a
-// subtraction per value).
-// x * 2^shift rounded to float (nearest, ties to even); magnitudes below FLT_MIN become a
-// signed zero (far below the fp16 planes' resolution after the row scaling), NaN stays NaN.
-__device__ __forceinline__ float d2f_scaled_rn(double x, int shift) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
-  const unsigned long long mag = b & 0x7fffffffffffffffull;
-  const uint32_t sgn = static_cast<uint32_t>(b >> 32) & 0x80000000u;
-  const int E = static_cast<int>(mag >> 52);
-  const unsigned long long m52 = mag & 0xfffffffffffffull;
-  if (E == 0x7ff) return __uint_as_float(sgn | (m52 ? 0x7fc00000u : 0x7f800000u));
-  if (E == 0) return __uint_as_float(sgn);
-  const int fe = E - 1023 + shift + 127;  // biased float exponent before rounding
-  if (fe < 1) return __uint_as_float(sgn);
-  if (fe > 254) return __uint_as_float(sgn | 0x7f800000u);
-  unsigned long long r = (static_cast<unsigned long long>(fe) << 52) | m52;
-  r += 0x0fffffffull + ((r >> 29) & 1ull);  // round half to even at the 29 dropped bits
-  return __uint_as_float(sgn | static_cast<uint32_t>(r >> 29));  // a carry moves into the exponent
 }
 // The same scaled split as the float overload, for a double and a power-of-two scale s.
 __device__ __forceinline__ void split16_scaled(double x, float s, __half* h, __half* l) {
@@ -547,15 +543,15 @@ __global__ void pack_b_planes_f16_kernel(const double2* __restrict__ B, int64_t 
     const int64_t row = idx / Kp;
     const int64_t k = idx - row * Kp;
     const int64_t n = row >> 1;
-    const double s = (double)fp16_row_scale(bmax[n]);
+    const float s = fp16_row_scale(bmax[n]);
     double v0 = 0.0, v1 = 0.0;
     if (k < K) {
       const double2 b = B[n * K + k];
       if ((row & 1) == 0) { v0 = b.x; v1 = -b.y; } else { v0 = b.y; v1 = b.x; }
     }
     __half2 hi, lo;
-    split16(v0 * s, &hi.x, &lo.x);
-    split16(v1 * s, &hi.y, &lo.y);
+    split16_scaled(v0, s, &hi.x, &lo.x);
+    split16_scaled(v1, s, &hi.y, &lo.y);
     *reinterpret_cast<__half2*>(out + row * (2 * Kp) + 2 * k) = hi;
     *reinterpret_cast<__half2*>(out + pstride + row * (2 * Kp) + 2 * k) = lo;
   }
@@ -775,16 +771,10 @@ __device__ __forceinline__ void rowmax_tile_adaptive(const Tin* __restrict__ T, 
 // and destinations are (buffer id, element offset) resolved against the launch's bases.
 template <typename Tin>
 __global__ void __launch_bounds__(256) block_gather_kernel(const DevGatherJob* __restrict__ jobs,
-                                                           const int* __restrict__ tile_start, int njobs,
-                                                           BlockBases bases) {
-  const int b = blockIdx.x;
-  int lo = 0, hi = njobs - 1;  // last job with tile_start <= b
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (tile_start[mid] <= b) lo = mid; else hi = mid - 1;
-  }
-  const DevGatherJob& J = jobs[lo];
-  const int t = b - tile_start[lo];
+                                                           const int2* __restrict__ tile_map, BlockBases bases) {
+  const int2 jt = tile_map[blockIdx.x];
+  const DevGatherJob& J = jobs[jt.x];
+  const int t = jt.y;
   const int64_t m0 = (int64_t)(t % J.tiles_m) * (1024 >> J.tks), k0 = (int64_t)(t / J.tiles_m) << J.tks;
   const Tin* src = static_cast<const Tin*>(bases.buf[J.src_buf]) + J.src_off;
   __shared__ SmemA<Tin> sm;
@@ -804,20 +794,100 @@ __global__ void __launch_bounds__(256) block_gather_kernel(const DevGatherJob* _
   }
 }
 
+// Fused gather + product of a block map's few-column problems.  A CTA takes a range of rows
+// of one band; G threads share a row (thread g owns the output columns n = g, g + G, ...),
+// each computes its row's offset in every rectangle from the row's digits in the band's
+// common groups and reads the row's present columns straight from the running tensor, eight
+// (c64) or four (c128) loads in flight before they are used.  B_q, the column table and the rectangles' strides
+// live in shared memory; the loop has no barrier.
+constexpr int kBandMaxN64 = 32, kBandMaxN32 = 64, kBandMaxSmem = 96 * 1024;
+
+template <typename Tin, typename T, int NPT, int G>
+__global__ void __launch_bounds__(256, 3) block_band_kernel(const DevBand* __restrict__ bands,
+                                                            const DevBandWork* __restrict__ work,
+                                                            const DevBandCol* __restrict__ cols,
+                                                            const int64_t* __restrict__ rstr, BlockBases bases) {
+  constexpr int RB = 256 / G, LB = sizeof(Tin) == 16 ? 4 : 8;  // rows per pass, loads in flight
+  extern __shared__ __align__(16) unsigned char band_smem[];
+  const DevBandWork W = work[blockIdx.x];
+  const DevBand& D = bands[W.band];
+  const int N = D.N, Kq = D.Kq, ng = D.ng, nrect = D.nrect, ncol = D.ncol;
+  T* Bs = reinterpret_cast<T*>(band_smem);                               // [N][Kq]
+  int64_t* rs = reinterpret_cast<int64_t*>(Bs + (size_t)N * Kq);        // [nrect][ng]
+  DevBandCol* cc = reinterpret_cast<DevBandCol*>(rs + nrect * ng);      // [ncol]
+  __shared__ uint32_t sdim[kBandMaxGroups], smag[kBandMaxGroups], ssh[kBandMaxGroups];
+  const int tid = threadIdx.x, r = tid % RB, g = tid / RB;
+  const T* __restrict__ B = static_cast<const T*>(D.B);
+  for (int i = tid; i < N * Kq; i += 256) Bs[i] = B[i];
+  for (int i = tid; i < nrect * ng; i += 256) rs[i] = rstr[D.rs0 + i];
+  for (int i = tid; i < ncol; i += 256) cc[i] = cols[D.col0 + i];
+  if (tid < ng) {
+    sdim[tid] = D.dim[tid];
+    smag[tid] = D.mag[tid];
+    ssh[tid] = D.sh[tid];
+  }
+  __syncthreads();
+  const Tin* __restrict__ src = static_cast<const Tin*>(bases.buf[D.src_buf]);
+  T* __restrict__ C = static_cast<T*>(bases.buf[D.c_buf]) + D.c_off;
+  for (int64_t mr = r; mr < W.nrows; mr += RB) {
+    const int64_t m = W.m0 + mr;
+    if (m >= D.M) break;
+    int dig[kBandMaxGroups];
+    {
+      uint32_t i = (uint32_t)m;
+#pragma unroll
+      for (int t = kBandMaxGroups - 1; t >= 0; --t) {
+        dig[t] = 0;
+        if (t < ng) {
+          const uint32_t q = sdim[t] == 1u ? i : (__umulhi(i, smag[t]) >> ssh[t]);
+          dig[t] = (int)(i - q * sdim[t]);
+          i = q;
+        }
+      }
+    }
+    T acc[NPT];
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) acc[j] = Zero<T>::v();
+    for (int j0 = 0; j0 < ncol; j0 += LB) {
+      Tin v[LB];
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        v[u] = Zero<Tin>::v();
+        if (j0 + u < ncol) {
+          const DevBandCol c = cc[j0 + u];
+          const int64_t* st = rs + c.rect * ng;
+          int64_t o = c.src;
+#pragma unroll
+          for (int t = 0; t < kBandMaxGroups; ++t)
+            if (t < ng) o += (int64_t)dig[t] * st[t];
+          v[u] = src[o];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        if (j0 + u < ncol) {
+          const T a = cvt(v[u], (T*)nullptr);
+          const T* bcol = Bs + cc[j0 + u].bcol;
+#pragma unroll
+          for (int j = 0; j < NPT; ++j)
+            if (g + G * j < N) cfma(acc[j], a, bcol[(g + G * j) * Kq]);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < NPT; ++j)
+      if (g + G * j < N) C[(int64_t)(g + G * j) * D.ldc + m] = acc[j];
+  }
+}
+
 // Row maxima of the jobs of a table (fp16 split of block maps), a kernel of its own so
 // that the block moves keep their shared-memory footprint.
 template <typename Tin>
 __global__ void __launch_bounds__(256) block_rowmax_kernel(const DevGatherJob* __restrict__ jobs,
-                                                           const int* __restrict__ tile_start, int njobs,
-                                                           BlockBases bases) {
-  const int b = blockIdx.x;
-  int lo = 0, hi = njobs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (tile_start[mid] <= b) lo = mid; else hi = mid - 1;
-  }
-  const DevGatherJob& J = jobs[lo];
-  const int t = b - tile_start[lo];
+                                                           const int2* __restrict__ tile_map, BlockBases bases) {
+  const int2 jt = tile_map[blockIdx.x];
+  const DevGatherJob& J = jobs[jt.x];
+  const int t = jt.y;
   const int64_t m0 = (int64_t)(t % J.tiles_m) * (1024 >> J.tks), k0 = (int64_t)(t / J.tiles_m) << J.tks;
   rowmax_tile_adaptive<Tin>(static_cast<const Tin*>(bases.buf[J.src_buf]) + J.src_off, J,
                             static_cast<float*>(bases.buf[5]) + J.amax_off, m0, k0);
@@ -1049,13 +1119,13 @@ cudaError_t launch_split_rows(const Tin* T, const Off& off, int64_t M, int64_t K
 
 }  // namespace
 
-cudaError_t launch_block_rowmax(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
-                                const BlockBases& bases, int src_is64, cudaStream_t s) {
+cudaError_t launch_block_rowmax(const DevGatherJob* jobs, const int2* tile_map, int ntiles, const BlockBases& bases,
+                                int src_is64, cudaStream_t s) {
   if (ntiles <= 0) return cudaSuccess;
   if (src_is64)
-    block_rowmax_kernel<double2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+    block_rowmax_kernel<double2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_map, bases);
   else
-    block_rowmax_kernel<float2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+    block_rowmax_kernel<float2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_map, bases);
   return cudaGetLastError();
 }
 
@@ -1084,14 +1154,66 @@ void finish_dev_gather_job(DevGatherJob* J) {
   }
 }
 
-cudaError_t launch_block_gather(const DevGatherJob* jobs, const int* tile_start, int njobs, int ntiles,
-                                const BlockBases& bases, int src_is64, cudaStream_t s) {
+cudaError_t launch_block_gather(const DevGatherJob* jobs, const int2* tile_map, int ntiles, const BlockBases& bases,
+                                int src_is64, cudaStream_t s) {
   if (ntiles <= 0) return cudaSuccess;
   if (src_is64)
-    block_gather_kernel<double2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+    block_gather_kernel<double2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_map, bases);
   else
-    block_gather_kernel<float2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_start, njobs, bases);
+    block_gather_kernel<float2><<<ntiles, dim3(32, 8), 0, s>>>(jobs, tile_map, bases);
   return cudaGetLastError();
+}
+
+size_t block_band_smem(int N, int Kq, int nrect, int ng, int fp64) {
+  const size_t e = fp64 ? sizeof(double2) : sizeof(float2);
+  return (size_t)N * Kq * e + (size_t)nrect * ng * sizeof(int64_t) + (size_t)Kq * sizeof(DevBandCol);
+}
+
+int block_band_rows_per_pass(int maxn) { return maxn <= 8 ? 256 : maxn <= 16 ? 128 : maxn <= 32 ? 64 : 32; }
+
+bool block_band_fits(int64_t N, int64_t Kq, int fp64) {
+  return N >= 1 && Kq >= 1 && N <= (fp64 ? kBandMaxN64 : kBandMaxN32) && Kq <= 4096 &&
+         block_band_smem((int)N, (int)Kq, kBandMaxRects, kBandMaxGroups, fp64) <= (size_t)kBandMaxSmem;
+}
+
+namespace {
+template <typename Tin, typename T, int NPT, int G>
+cudaError_t launch_band_t(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
+                          const int64_t* rstr, const BlockBases& bases, size_t smem, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(block_band_kernel<Tin, T, NPT, G>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kBandMaxSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  block_band_kernel<Tin, T, NPT, G><<<nwork, 256, smem, s>>>(bands, work, cols, rstr, bases);
+  return cudaGetLastError();
+}
+
+// Up to 8 outputs per thread: one thread per row for N <= 8, else G = N / 8 threads per row.
+template <typename Tin, typename T>
+cudaError_t launch_band_n(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
+                          const int64_t* rstr, const BlockBases& bases, int maxn, size_t smem, cudaStream_t s) {
+  if (maxn <= 1) return launch_band_t<Tin, T, 1, 1>(bands, work, nwork, cols, rstr, bases, smem, s);
+  if (maxn <= 2) return launch_band_t<Tin, T, 2, 1>(bands, work, nwork, cols, rstr, bases, smem, s);
+  if (maxn <= 4) return launch_band_t<Tin, T, 4, 1>(bands, work, nwork, cols, rstr, bases, smem, s);
+  if (maxn <= 8) return launch_band_t<Tin, T, 8, 1>(bands, work, nwork, cols, rstr, bases, smem, s);
+  if (maxn <= 16) return launch_band_t<Tin, T, 8, 2>(bands, work, nwork, cols, rstr, bases, smem, s);
+  if (maxn <= 32) return launch_band_t<Tin, T, 8, 4>(bands, work, nwork, cols, rstr, bases, smem, s);
+  if (maxn <= 64) return launch_band_t<Tin, T, 8, 8>(bands, work, nwork, cols, rstr, bases, smem, s);
+  return cudaErrorInvalidValue;
+}
+}  // namespace
+
+cudaError_t launch_block_band(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
+                              const int64_t* rstr, const BlockBases& bases, int src_is64, int fp64, int maxn,
+                              size_t smem, cudaStream_t s) {
+  if (nwork <= 0) return cudaSuccess;
+  if (smem > (size_t)kBandMaxSmem || maxn > (fp64 ? kBandMaxN64 : kBandMaxN32)) return cudaErrorInvalidValue;
+  if (fp64) return launch_band_n<double2, double2>(bands, work, nwork, cols, rstr, bases, maxn, smem, s);
+  if (src_is64) return launch_band_n<double2, float2>(bands, work, nwork, cols, rstr, bases, maxn, smem, s);
+  return launch_band_n<float2, float2>(bands, work, nwork, cols, rstr, bases, maxn, smem, s);
 }
 
 template <typename Tin, typename Tout>

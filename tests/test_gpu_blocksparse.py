@@ -50,3 +50,24 @@ def test_block_map_graph_replay(ctx):
         ctx.sync()
         assert np.linalg.norm(ctx.download(dy) - ref) <= 1e-5 * np.linalg.norm(ref)
     bm.close()
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-14), ("bf16x6", 1e-6), ("fp16x3", 1e-6)])
+def test_block_map_bands_match_staged_products(ctx, prec, tol, monkeypatch):
+    """The few-column problems read straight from the running tensor (fused row bands) give
+    the products of the staged-operand path (GTN_BLOCK_BANDS=0) and the dense oracle."""
+    xs, labels, order, statics, x = h2_u1_case(5, "n3_1", 128, seed=5)
+    plan = B.BlockPlan(xs, labels[0], statics, order)
+    ref = dense_reference(xs, labels, order, statics, x)
+    outs, launches = [], []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("GTN_BLOCK_BANDS", flag)
+        bm = B.BlockEffectiveMap(ctx, plan, prec)
+        l0 = ctx.launches
+        outs.append(ctx.download(bm(ctx.upload(x))))
+        launches.append(ctx.launches - l0)
+        bm.close()
+    assert np.linalg.norm(outs[0] - outs[1]) <= tol * np.linalg.norm(outs[1])
+    got = plan.y.to_dense(outs[0])
+    assert np.linalg.norm(got - ref) <= RTOL[prec] * np.linalg.norm(ref)
+    assert launches[0] <= launches[1]
