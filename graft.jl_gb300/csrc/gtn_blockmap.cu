@@ -34,6 +34,12 @@ struct BMStep {
   int64_t* rstr = nullptr;
   int nbands = 0, nbwork = 0, band_maxn = 0;
   size_t band_smem = 0;
+  DevBand* sbands = nullptr;     // split bands of the tensor-core problems with Kp <= 128
+  DevBandWork* swork = nullptr;
+  DevBandCol* scols = nullptr;
+  int64_t* srstr = nullptr;
+  int nsbands = 0, nswork = 0;
+  size_t split_smem = 0;
 };
 
 // Bands of a step on the host, before upload.
@@ -42,7 +48,6 @@ struct BandSet {
   std::vector<DevBandCol> cols;
   std::vector<int64_t> rstr;
   int maxn = 0;
-  size_t smem = 0;
 };
 
 struct gtn_blockmap_s {
@@ -74,6 +79,8 @@ struct gtn_blockmap_s {
 };
 
 namespace {
+
+constexpr int64_t kBandMinCtas = 6 * 152;
 
 // Coupled-charge problems with K < 16 or N < 16 run on the SIMT GEMMs (FP32 in the mixed
 // modes): padding them to the tcgen05 tile costs more than their arithmetic.
@@ -137,15 +144,19 @@ cudaError_t upload_table(gtn_blockmap bm, std::vector<DevGatherJob>& jobs, DevGa
 }
 
 // Upload the bands of a step with their work items, column table and row strides.  A work
-// item is 1 to 8 passes of one CTA over a band's rows (a pass covers 256 / G rows, G threads
-// per row), about 16384 loads, so that each CTA's set-up (band, B_q, strides, columns) is
-// paid once over several passes while the grid keeps every SM busy.
-cudaError_t upload_bands(gtn_blockmap bm, const BandSet& bs, BMStep* st) {
+// item is 1 to 8 passes of one CTA over a band's rows (256 rows a pass, one thread per row),
+// about 16384 loads, so that each CTA's set-up (band, B_q, strides, columns) is paid once
+// over several passes; fewer passes when that would leave the launch with less than
+// kBandMinCtas CTAs (six per SM).
+cudaError_t upload_bands(gtn_blockmap bm, const BandSet& bs, int fp64, BMStep* st) {
   std::vector<DevBandWork> work;
   const int64_t rb = block_band_rows_per_pass(bs.maxn);
+  int64_t rows = 0;
+  for (const DevBand& D : bs.bands) rows += D.M;
+  const int64_t pmax = std::max<int64_t>(1, std::min<int64_t>(8, rows / (rb * kBandMinCtas)));
   for (size_t i = 0; i < bs.bands.size(); ++i) {
     const int64_t M = bs.bands[i].M;
-    const int64_t passes = std::min<int64_t>(8, std::max<int64_t>(1, 16384 / (rb * std::max(bs.bands[i].ncol, 1))));
+    const int64_t passes = std::min<int64_t>(pmax, std::max<int64_t>(1, 16384 / (rb * std::max(bs.bands[i].ncol, 1))));
     const int64_t per = rb * passes;
     for (int64_t m = 0; m < M; m += per) {
       DevBandWork w;
@@ -158,7 +169,9 @@ cudaError_t upload_bands(gtn_blockmap bm, const BandSet& bs, BMStep* st) {
   st->nbands = (int)bs.bands.size();
   st->nbwork = (int)work.size();
   st->band_maxn = bs.maxn;
-  st->band_smem = bs.smem;
+  st->band_smem = 0;  // the launch's padding and rows per pass follow its largest N
+  for (const DevBand& D : bs.bands)
+    st->band_smem = std::max(st->band_smem, block_band_smem(bs.maxn, D.Kq, D.nrect, D.ng, fp64));
   if (bs.bands.empty()) return cudaSuccess;
   auto put = [&](void** dst, const void* src, size_t bytes) {
     cudaError_t e = cudaMalloc(dst, std::max<size_t>(bytes, 16));
@@ -170,6 +183,45 @@ cudaError_t upload_bands(gtn_blockmap bm, const BandSet& bs, BMStep* st) {
   if (e == cudaSuccess) e = put(reinterpret_cast<void**>(&st->bwork), work.data(), work.size() * sizeof(DevBandWork));
   if (e == cudaSuccess) e = put(reinterpret_cast<void**>(&st->cols), bs.cols.data(), bs.cols.size() * sizeof(DevBandCol));
   if (e == cudaSuccess) e = put(reinterpret_cast<void**>(&st->rstr), bs.rstr.data(), bs.rstr.size() * sizeof(int64_t));
+  return e;
+}
+
+// The split bands of a step: work items of 1 to 8 passes of TR rows (about 8192 loads;
+// TR = 32 rows, fewer for rows longer than 128 columns), fewer passes when that would leave
+// the launch with less than kBandMinCtas CTAs.
+cudaError_t upload_split_bands(gtn_blockmap bm, const BandSet& bs, BMStep* st) {
+  std::vector<DevBandWork> work;
+  st->split_smem = 0;
+  int64_t elems = 0;
+  for (const DevBand& D : bs.bands) elems += D.M * D.Kp;
+  const int64_t emax = std::max<int64_t>(1, elems / kBandMinCtas);  // elements per CTA for enough CTAs
+  for (size_t i = 0; i < bs.bands.size(); ++i) {
+    const DevBand& D = bs.bands[i];
+    const int64_t tr = block_split_band_rows(D.Kp, st->src_is64);
+    const int64_t passes = std::min<int64_t>(std::max<int64_t>(1, emax / (tr * D.Kp)),
+                                             std::min<int64_t>(8, std::max<int64_t>(1, 8192 / (tr * std::max(D.ncol, 1)))));
+    for (int64_t m = 0; m < D.M; m += tr * passes) {
+      DevBandWork w;
+      w.band = (int)i;
+      w.nrows = (int)std::min<int64_t>(tr * passes, D.M - m);
+      w.m0 = m;
+      work.push_back(w);
+    }
+    st->split_smem = std::max(st->split_smem, block_split_band_smem(D.Kp, D.nrect, D.ng, D.ncol, st->src_is64));
+  }
+  st->nsbands = (int)bs.bands.size();
+  st->nswork = (int)work.size();
+  if (bs.bands.empty()) return cudaSuccess;
+  auto put = [&](void** dst, const void* src, size_t bytes) {
+    cudaError_t e = cudaMalloc(dst, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return e;
+    bm->owned.push_back(*dst);
+    return bytes ? cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+  };
+  cudaError_t e = put(reinterpret_cast<void**>(&st->sbands), bs.bands.data(), bs.bands.size() * sizeof(DevBand));
+  if (e == cudaSuccess) e = put(reinterpret_cast<void**>(&st->swork), work.data(), work.size() * sizeof(DevBandWork));
+  if (e == cudaSuccess) e = put(reinterpret_cast<void**>(&st->scols), bs.cols.data(), bs.cols.size() * sizeof(DevBandCol));
+  if (e == cudaSuccess) e = put(reinterpret_cast<void**>(&st->srstr), bs.rstr.data(), bs.rstr.size() * sizeof(int64_t));
   return e;
 }
 
@@ -222,6 +274,7 @@ bool plan_bands(const gtn_block_gemm& g, const std::vector<const gtn_block_gathe
     DevBand D;
     std::memset(&D, 0, sizeof(D));
     D.M = M;
+    D.row_off = kv.first;
     D.c_off = g.c_off + kv.first;
     D.ldc = g.M;
     D.B = Bq;
@@ -278,14 +331,12 @@ bool plan_bands(const gtn_block_gemm& g, const std::vector<const gtn_block_gathe
       D.m_fast = rmin < kmin ? 1 : 0;
     }
     loc.maxn = std::max(loc.maxn, D.N);
-    loc.smem = std::max(loc.smem, block_band_smem(D.N, D.Kq, D.nrect, D.ng, fp64));
     loc.bands.push_back(D);
   }
   out->bands.insert(out->bands.end(), loc.bands.begin(), loc.bands.end());
   out->cols.insert(out->cols.end(), loc.cols.begin(), loc.cols.end());
   out->rstr.insert(out->rstr.end(), loc.rstr.begin(), loc.rstr.end());
   out->maxn = std::max(out->maxn, loc.maxn);
-  out->smem = std::max(out->smem, loc.smem);
   return true;
 }
 
@@ -313,6 +364,11 @@ int run(gtn_blockmap bm, const double2* x, double2* y) {
     }
     if (st.ntiles > 0) {
       e = launch_block_gather(st.jobs, st.tiles, st.ntiles, bases, st.src_is64, s);
+      ctx->launches++;
+    }
+    if (e == cudaSuccess && st.nswork > 0) {
+      e = launch_block_split_band(st.sbands, st.swork, st.nswork, st.scols, st.srstr, bases, st.src_is64,
+                                  bm->precision == GTN_PREC_FP16X3 ? 1 : 0, st.split_smem, s);
       ctx->launches++;
     }
     if (e == cudaSuccess && !st.tcp.empty()) {
@@ -496,7 +552,7 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
   std::vector<std::vector<int64_t>> step_mbase;  // fp16: first row-maximum slot of each problem
   std::vector<int64_t> step_mrows;
   int64_t amax_need = 0;
-  std::vector<BandSet> step_bands(nsteps);
+  std::vector<BandSet> step_bands(nsteps), step_sbands(nsteps);
   int64_t gv = 0;
   for (int s = 0; s < nsteps; ++s) {
     std::vector<gtn_block_gemm> gm(gemms + mo, gemms + mo + step_ngemm[s]);
@@ -528,8 +584,19 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
       const void* Bq = fp64 ? static_cast<const void*>(bm->b64[g.b_index]) : static_cast<const void*>(bm->b32[g.b_index]);
       const bool band = !t && bands_on && block_band_fits(g.N, g.K, fp64 ? 1 : 0) &&
                         plan_bands(g, per_q[q], Bq, fp64 ? 1 : 0, &step_bands[s]);
-      use_tc.push_back(t ? 1 : band ? 2 : 0);
       const int64_t k = t ? ((g.K + 31) / 32) * 32 : g.K;
+      const size_t sb0 = step_sbands[s].bands.size();
+      const bool split = t && bands_on && k <= kSplitBandMaxKp &&
+                         plan_bands(g, per_q[q], nullptr, fp64 ? 1 : 0, &step_sbands[s]);
+      for (size_t b = sb0; b < step_sbands[s].bands.size(); ++b) {  // plane layout (row maxima below)
+        DevBand& D = step_sbands[s].bands[b];
+        D.a_off = (int64_t)(off / sizeof(__nv_bfloat16));
+        D.pstride = g.M * 2 * k;
+        D.Kp = (int)k;
+        D.nplanes = P;
+        D.amax_off = (int64_t)q;  // the problem's index until its row-maxima base is known
+      }
+      use_tc.push_back(split ? 3 : t ? 1 : band ? 2 : 0);
       kp.push_back(k);
       aoff.push_back(off);
       if (band) continue;  // read straight from the running tensor: no staged operand
@@ -541,8 +608,9 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
     std::vector<int64_t> mbase;
     for (size_t q = 0; q < gm.size(); ++q) {
       mbase.push_back(mrows);
-      if (use_tc[q] == 1) mrows += gm[q].M;
+      if (use_tc[q] == 1 || use_tc[q] == 3) mrows += gm[q].M;
     }
+    for (DevBand& D : step_sbands[s].bands) D.amax_off = mbase[(size_t)D.amax_off] + D.row_off;
     step_mbase.push_back(mbase);
     step_mrows.push_back(mrows);
     amax_need = std::max(amax_need, mrows);
@@ -574,7 +642,7 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
     for (int i = 0; i < step_ngather[s]; ++i) {
       const gtn_block_gather& d = gathers[go + i];  // validated above
       const int q = d.dst_index;
-      if (step_tc[s][q] == 2) continue;  // read in place by its problem's bands
+      if (step_tc[s][q] == 2 || step_tc[s][q] == 3) continue;  // read in place by its problem's bands
       DevGatherJob J;
       std::memset(&J, 0, sizeof(J));
       to_groups(d, &J.mg, &J.kg);
@@ -609,7 +677,7 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
         continue;
       }
       if (step_tc[s][q]) {
-        if (step_kp[s][q] > g.K) {  // zero the K padding of the operand planes
+        if (step_tc[s][q] == 1 && step_kp[s][q] > g.K) {  // zero the K padding of the operand planes
           DevGatherJob J;
           std::memset(&J, 0, sizeof(J));
           J.src_buf = 4;
@@ -662,7 +730,9 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
     std::stable_sort(st.tcp.begin(), st.tcp.end(), [](const TcGemmArgs& a, const TcGemmArgs& b) { return a.Kp > b.Kp; });
     st.src_is64 = (s == 0 || fp64) ? 1 : 0;
     if (upload_jobs(bm, jobs, &st) != cudaSuccess) return fail(GTN_ERR_CUDA, "job table upload");
-    if (upload_bands(bm, step_bands[s], &st) != cudaSuccess) return fail(GTN_ERR_CUDA, "band table upload");
+    if (upload_bands(bm, step_bands[s], fp64 ? 1 : 0, &st) != cudaSuccess ||
+        upload_split_bands(bm, step_sbands[s], &st) != cudaSuccess)
+      return fail(GTN_ERR_CUDA, "band table upload");
     st.amax_elems = step_mrows[s];
     if (!mjobs.empty() &&
         upload_table(bm, mjobs, &st.mjobs, &st.mtiles, &st.nmjobs, &st.nmtiles) != cudaSuccess)

@@ -194,26 +194,39 @@ struct DevBandCol {
   int32_t rect;  // its rectangle within the band
   int32_t bcol;  // its column of B_q
 };
+constexpr int kBandMaxRects = 24, kBandMaxGroups = 6;
 struct DevBand {
   int64_t M;       // rows of the band
-  int64_t c_off;   // element offset of C_q[0][row_off] in bases.buf[c_buf]
-  int64_t ldc;     // M_q: the pitch between output columns n
-  const void* B;   // B_q [N][Kq] in the compute type
-  int N, Kq, c_buf, src_buf;
+  int64_t row_off; // its first row in A_q
+  int64_t c_off;   // product bands: element offset of C_q[0][row_off] in bases.buf[c_buf]
+  int64_t ldc;     // product bands: M_q, the pitch between output columns n
+  const void* B;   // product bands: B_q [N][Kq] in the compute type
+  int64_t a_off;   // split bands: element offset (halves) of A_q's plane 0 in bases.buf[4]
+  int64_t pstride; // split bands: plane pitch (halves)
+  int64_t amax_off;  // split bands, fp16: row maxima of A_q at (float*)bases.buf[5] + amax_off
+  int N, Kq, Kp, nplanes, c_buf, src_buf;
   int col0, ncol;  // present columns: cols[col0, col0 + ncol)
   int rs0, nrect;  // row strides: rstr[rs0 + rect * ng + t]
   int ng, m_fast;  // common row groups (slowest first); loads run along rows when m_fast
-  uint32_t dim[GTN_MAXG], mag[GTN_MAXG], sh[GTN_MAXG];  // group sizes and their division magic
+  uint32_t dim[kBandMaxGroups], mag[kBandMaxGroups], sh[kBandMaxGroups];  // group sizes, division magic
 };
 // A CTA's share of a band: the rows [m0, m0 + nrows).
 struct DevBandWork {
   int band, nrows;
   int64_t m0;
 };
-constexpr int kBandMaxRects = 64, kBandMaxGroups = 6;
 bool block_band_fits(int64_t N, int64_t Kq, int fp64);
-int block_band_rows_per_pass(int maxn);  // rows a CTA covers per pass (256 / threads per row)
-size_t block_band_smem(int N, int Kq, int nrect, int ng, int fp64);
+int block_band_rows_per_pass(int maxn);  // rows a CTA covers per pass (one thread per row)
+size_t block_band_smem(int maxn, int Kq, int nrect, int ng, int fp64);
+// Split bands: the slice planes of a tensor-core problem's A_q built band by band (rows of
+// up to 1024 columns staged whole, row maxima reduced in the CTA for fp16), replacing the
+// row-maxima pass, the block moves and the K padding of that problem.
+constexpr int kSplitBandMaxKp = 1024;
+int block_split_band_rows(int Kp, int src_is64);  // rows per pass
+size_t block_split_band_smem(int Kp, int nrect, int ng, int ncol, int src_is64);
+cudaError_t launch_block_split_band(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
+                                    const int64_t* rstr, const BlockBases& bases, int src_is64, int fp16,
+                                    size_t smem, cudaStream_t s);
 cudaError_t launch_block_band(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
                               const int64_t* rstr, const BlockBases& bases, int src_is64, int fp64, int maxn,
                               size_t smem, cudaStream_t s);

@@ -795,45 +795,52 @@ __global__ void __launch_bounds__(256) block_gather_kernel(const DevGatherJob* _
 }
 
 // Fused gather + product of a block map's few-column problems.  A CTA takes a range of rows
-// of one band; G threads share a row (thread g owns the output columns n = g, g + G, ...),
-// each computes its row's offset in every rectangle from the row's digits in the band's
-// common groups and reads the row's present columns straight from the running tensor, eight
-// (c64) or four (c128) loads in flight before they are used.  B_q, the column table and the rectangles' strides
-// live in shared memory; the loop has no barrier.
-constexpr int kBandMaxN64 = 32, kBandMaxN32 = 64, kBandMaxSmem = 96 * 1024;
+// of one band, one thread per row.  Per pass each thread computes its row's base offset in
+// every rectangle once (digits of the row in the band's common groups times the
+// rectangle's strides, kept in shared memory for its own row only), then, for each chunk of
+// NPT output columns, reads the row's present columns straight from the running tensor,
+// eight (c64) or four (c128) loads in flight before they are used (chunks after the first
+// find the row in L1).  B_q is held transposed and zero-padded to a multiple of NPT columns
+// so that the products need no predicates.
+constexpr int kBandMaxN64 = 32, kBandMaxN32 = 64, kBandMaxSmem = 96 * 1024, kBandRows = 256;
+__host__ __device__ constexpr int band_npt(int maxn) { return maxn <= 1 ? 1 : maxn <= 2 ? 2 : maxn <= 4 ? 4 : 8; }
+__host__ __device__ constexpr int band_npad(int n, int npt) { return (n + npt - 1) / npt * npt; }
 
-template <typename Tin, typename T, int NPT, int G>
-__global__ void __launch_bounds__(256, 3) block_band_kernel(const DevBand* __restrict__ bands,
+template <typename Tin, typename T, int NPT>
+__global__ void __launch_bounds__(256, 4) block_band_kernel(const DevBand* __restrict__ bands,
                                                             const DevBandWork* __restrict__ work,
                                                             const DevBandCol* __restrict__ cols,
                                                             const int64_t* __restrict__ rstr, BlockBases bases) {
-  constexpr int RB = 256 / G, LB = sizeof(Tin) == 16 ? 4 : 8;  // rows per pass, loads in flight
+  constexpr int LB = sizeof(Tin) == 16 ? 4 : 8;  // loads in flight
   extern __shared__ __align__(16) unsigned char band_smem[];
   const DevBandWork W = work[blockIdx.x];
   const DevBand& D = bands[W.band];
-  const int N = D.N, Kq = D.Kq, ng = D.ng, nrect = D.nrect, ncol = D.ncol;
-  T* Bs = reinterpret_cast<T*>(band_smem);                               // [N][Kq]
-  int64_t* rs = reinterpret_cast<int64_t*>(Bs + (size_t)N * Kq);        // [nrect][ng]
-  DevBandCol* cc = reinterpret_cast<DevBandCol*>(rs + nrect * ng);      // [ncol]
+  const int N = D.N, Kq = D.Kq, ng = D.ng, nrect = D.nrect, ncol = D.ncol, NPAD = band_npad(N, NPT);
+  T* Bt = reinterpret_cast<T*>(band_smem);                                // [Kq][NPAD]
+  int64_t* rs = reinterpret_cast<int64_t*>(Bt + (size_t)Kq * NPAD);      // [nrect][ng]
+  int64_t* base = rs + nrect * ng;                                        // [nrect][kBandRows]
+  DevBandCol* cc = reinterpret_cast<DevBandCol*>(base + nrect * kBandRows);  // [ncol]
   __shared__ uint32_t sdim[kBandMaxGroups], smag[kBandMaxGroups], ssh[kBandMaxGroups];
-  const int tid = threadIdx.x, r = tid % RB, g = tid / RB;
+  const int r = threadIdx.x;
   const T* __restrict__ B = static_cast<const T*>(D.B);
-  for (int i = tid; i < N * Kq; i += 256) Bs[i] = B[i];
-  for (int i = tid; i < nrect * ng; i += 256) rs[i] = rstr[D.rs0 + i];
-  for (int i = tid; i < ncol; i += 256) cc[i] = cols[D.col0 + i];
-  if (tid < ng) {
-    sdim[tid] = D.dim[tid];
-    smag[tid] = D.mag[tid];
-    ssh[tid] = D.sh[tid];
+  for (int i = r; i < Kq * NPAD; i += 256) {
+    const int k = i / NPAD, n = i - k * NPAD;
+    Bt[i] = n < N ? B[(size_t)n * Kq + k] : Zero<T>::v();
+  }
+  for (int i = r; i < nrect * ng; i += 256) rs[i] = rstr[D.rs0 + i];
+  for (int i = r; i < ncol; i += 256) cc[i] = cols[D.col0 + i];
+  if (r < ng) {
+    sdim[r] = D.dim[r];
+    smag[r] = D.mag[r];
+    ssh[r] = D.sh[r];
   }
   __syncthreads();
   const Tin* __restrict__ src = static_cast<const Tin*>(bases.buf[D.src_buf]);
   T* __restrict__ C = static_cast<T*>(bases.buf[D.c_buf]) + D.c_off;
-  for (int64_t mr = r; mr < W.nrows; mr += RB) {
+  for (int64_t mr = r; mr < W.nrows; mr += kBandRows) {
     const int64_t m = W.m0 + mr;
-    if (m >= D.M) break;
-    int dig[kBandMaxGroups];
     {
+      int dig[kBandMaxGroups];
       uint32_t i = (uint32_t)m;
 #pragma unroll
       for (int t = kBandMaxGroups - 1; t >= 0; --t) {
@@ -844,39 +851,185 @@ __global__ void __launch_bounds__(256, 3) block_band_kernel(const DevBand* __res
           i = q;
         }
       }
-    }
-    T acc[NPT];
+      for (int q = 0; q < nrect; ++q) {
+        const int64_t* st = rs + q * ng;
+        int64_t o = 0;
 #pragma unroll
-    for (int j = 0; j < NPT; ++j) acc[j] = Zero<T>::v();
-    for (int j0 = 0; j0 < ncol; j0 += LB) {
-      Tin v[LB];
-#pragma unroll
-      for (int u = 0; u < LB; ++u) {
-        v[u] = Zero<Tin>::v();
-        if (j0 + u < ncol) {
-          const DevBandCol c = cc[j0 + u];
-          const int64_t* st = rs + c.rect * ng;
-          int64_t o = c.src;
-#pragma unroll
-          for (int t = 0; t < kBandMaxGroups; ++t)
-            if (t < ng) o += (int64_t)dig[t] * st[t];
-          v[u] = src[o];
-        }
+        for (int t = 0; t < kBandMaxGroups; ++t)
+          if (t < ng) o += (int64_t)dig[t] * st[t];
+        base[q * kBandRows + r] = o;
       }
+    }
+    for (int n0 = 0; n0 < N; n0 += NPT) {
+      T acc[NPT];
 #pragma unroll
-      for (int u = 0; u < LB; ++u) {
-        if (j0 + u < ncol) {
+      for (int j = 0; j < NPT; ++j) acc[j] = Zero<T>::v();
+      for (int j0 = 0; j0 < ncol; j0 += LB) {
+        Tin v[LB];
+        int bc[LB];
+#pragma unroll
+        for (int u = 0; u < LB; ++u) {
+          v[u] = Zero<Tin>::v();
+          bc[u] = 0;
+          if (j0 + u < ncol) {
+            const DevBandCol c = cc[j0 + u];
+            bc[u] = c.bcol;
+            v[u] = src[c.src + base[c.rect * kBandRows + r]];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < LB; ++u) {
           const T a = cvt(v[u], (T*)nullptr);
-          const T* bcol = Bs + cc[j0 + u].bcol;
+          const T* bp = Bt + (size_t)bc[u] * NPAD + n0;
 #pragma unroll
-          for (int j = 0; j < NPT; ++j)
-            if (g + G * j < N) cfma(acc[j], a, bcol[(g + G * j) * Kq]);
+          for (int j = 0; j < NPT; ++j) cfma(acc[j], a, bp[j]);
         }
       }
-    }
 #pragma unroll
-    for (int j = 0; j < NPT; ++j)
-      if (g + G * j < N) C[(int64_t)(g + G * j) * D.ldc + m] = acc[j];
+      for (int j = 0; j < NPT; ++j)
+        if (n0 + j < N) C[(int64_t)(n0 + j) * D.ldc + m] = acc[j];
+    }
+  }
+}
+
+// bf16 slice planes of two adjacent columns k, k + 1 (k even): one 8-byte store per plane.
+struct SplitRowWriter {
+  __nv_bfloat16* out;
+  int64_t ld2;
+  int64_t pstride;
+  int nplanes;
+  template <typename Tin> __device__ void operator()(int64_t m, int64_t k, Tin v0, Tin v1, float) const {
+    __nv_bfloat16 r0[3], i0[3], r1[3], i1[3];
+    split3(v0.x, r0);
+    split3(v0.y, i0);
+    split3(v1.x, r1);
+    split3(v1.y, i1);
+    __nv_bfloat16* row = out + m * ld2 + 2 * k;
+    for (int p = 0; p < nplanes; ++p) {
+      __nv_bfloat162 a, b;
+      a.x = r0[p];
+      a.y = i0[p];
+      b.x = r1[p];
+      b.y = i1[p];
+      uint2 w;
+      w.x = *reinterpret_cast<uint32_t*>(&a);
+      w.y = *reinterpret_cast<uint32_t*>(&b);
+      *reinterpret_cast<uint2*>(row + p * pstride) = w;
+    }
+  }
+};
+
+// Split bands of the tensor-core problems (Kp <= 1024): a CTA stages TR whole rows of A_q
+// (every present column read straight from the running tensor, absent blocks and the K
+// padding zero), reduces the fp16 row maxima over the staged rows, and writes the rows'
+// slice planes with one 8-byte store per plane and column pair.  The values and the split
+// functions are those of the block moves, so the planes equal the staged path's.
+// Rows staged per pass: as many as fit 33 KB of the tile, at most 32.
+__host__ __device__ inline int split_band_tr(int Kp, int elem) {
+  int tr = 32;
+  while (tr > 1 && (size_t)tr * (Kp + 1) * elem > 33 * 1024) tr >>= 1;
+  return tr;
+}
+
+template <typename Tin, bool F16>
+__global__ void __launch_bounds__(256) block_split_band_kernel(const DevBand* __restrict__ bands,
+                                                               const DevBandWork* __restrict__ work,
+                                                               const DevBandCol* __restrict__ cols,
+                                                               const int64_t* __restrict__ rstr, BlockBases bases) {
+  extern __shared__ __align__(16) unsigned char band_smem[];
+  const DevBandWork W = work[blockIdx.x];
+  const DevBand& D = bands[W.band];
+  const int Kp = D.Kp, P = Kp + 1, ng = D.ng, nrect = D.nrect, ncol = D.ncol;
+  const int TR = split_band_tr(Kp, (int)sizeof(Tin));
+  Tin* tile = reinterpret_cast<Tin*>(band_smem);                           // [TR][Kp + 1]
+  int64_t* rs = reinterpret_cast<int64_t*>(tile + TR * P);                // [nrect][ng]
+  int64_t* base = rs + nrect * ng;                                        // [nrect][TR]
+  DevBandCol* cc = reinterpret_cast<DevBandCol*>(base + nrect * TR);     // [ncol]
+  __shared__ float rmax[32];
+  __shared__ uint32_t sdim[kBandMaxGroups], smag[kBandMaxGroups], ssh[kBandMaxGroups];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < nrect * ng; i += 256) rs[i] = rstr[D.rs0 + i];
+  for (int i = tid; i < ncol; i += 256) cc[i] = cols[D.col0 + i];
+  if (tid < ng) {
+    sdim[tid] = D.dim[tid];
+    smag[tid] = D.mag[tid];
+    ssh[tid] = D.sh[tid];
+  }
+  const Tin* __restrict__ src = static_cast<const Tin*>(bases.buf[D.src_buf]);
+  __half* out = reinterpret_cast<__half*>(bases.buf[4]) + D.a_off;
+  const int64_t ld2 = 2 * (int64_t)Kp;
+  for (int p0 = 0; p0 < W.nrows; p0 += TR) {
+    const int rows = W.nrows - p0 < TR ? W.nrows - p0 : TR;
+    const int64_t m0 = W.m0 + p0;
+    __syncthreads();  // (first pass: strides, columns, groups; then the previous pass's tile)
+    for (int e = tid; e < TR * P; e += 256) tile[e] = Zero<Tin>::v();
+    for (int e = tid; e < TR * nrect; e += 256) {  // row i's base offset in rectangle q
+      const int i = e % TR, q = e / TR;
+      uint32_t x = (uint32_t)(m0 + (i < rows ? i : 0));
+      int64_t o = 0;
+      for (int t = ng - 1; t >= 0; --t) {
+        const uint32_t qq = sdim[t] == 1u ? x : (__umulhi(x, smag[t]) >> ssh[t]);
+        o += (int64_t)(x - qq * sdim[t]) * rs[q * ng + t];
+        x = qq;
+      }
+      base[q * TR + i] = o;
+    }
+    __syncthreads();
+    // every present column of the staged rows, eight loads in flight per thread
+    for (int e0 = 0; e0 < TR * ncol; e0 += 8 * 256) {
+      int64_t off[8];
+      int slot[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + u * 256 + tid;
+        int i, j;
+        if (D.m_fast) {
+          i = e % TR;
+          j = e / TR;
+        } else {
+          j = e % ncol;
+          i = e / ncol;
+        }
+        slot[u] = -1;
+        off[u] = 0;
+        if (e < TR * ncol && i < rows) {
+          const DevBandCol c = cc[j];
+          slot[u] = i * P + c.bcol;
+          off[u] = c.src + base[c.rect * TR + i];
+        }
+      }
+      Tin v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = slot[u] >= 0 ? src[off[u]] : Zero<Tin>::v();
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (slot[u] >= 0) tile[slot[u]] = v[u];
+    }
+    __syncthreads();
+    if (F16) {  // row maxima, one warp per row
+      for (int i = warp; i < rows; i += 8) {
+        float mx = 0.f;
+        for (int k = lane; k < Kp; k += 32) mx = fmaxf(mx, absmax2(tile[i * P + k]));
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) {
+          rmax[i] = mx;
+          static_cast<float*>(bases.buf[5])[D.amax_off + m0 + i] = mx;
+        }
+      }
+      __syncthreads();
+    }
+    const int hw = Kp / 2;
+    for (int e = tid; e < rows * hw; e += 256) {
+      const int i = e / hw, c = 2 * (e - i * hw);
+      const int64_t m = D.row_off + m0 + i;
+      if (F16) {
+        Split16RowWriter w{out, ld2, D.pstride};
+        w(m, c, tile[i * P + c], tile[i * P + c + 1], rmax[i]);
+      } else {
+        SplitRowWriter w{reinterpret_cast<__nv_bfloat16*>(out), ld2, D.pstride, D.nplanes};
+        w(m, c, tile[i * P + c], tile[i * P + c + 1], 0.f);
+      }
+    }
   }
 }
 
@@ -1164,45 +1317,46 @@ cudaError_t launch_block_gather(const DevGatherJob* jobs, const int2* tile_map, 
   return cudaGetLastError();
 }
 
-size_t block_band_smem(int N, int Kq, int nrect, int ng, int fp64) {
+size_t block_band_smem(int maxn, int Kq, int nrect, int ng, int fp64) {
   const size_t e = fp64 ? sizeof(double2) : sizeof(float2);
-  return (size_t)N * Kq * e + (size_t)nrect * ng * sizeof(int64_t) + (size_t)Kq * sizeof(DevBandCol);
+  return (size_t)Kq * band_npad(maxn, band_npt(maxn)) * e + (size_t)nrect * ng * sizeof(int64_t) +
+         (size_t)nrect * kBandRows * sizeof(int64_t) + (size_t)Kq * sizeof(DevBandCol);
 }
 
-int block_band_rows_per_pass(int maxn) { return maxn <= 8 ? 256 : maxn <= 16 ? 128 : maxn <= 32 ? 64 : 32; }
+int block_band_rows_per_pass(int) { return kBandRows; }
 
+// Whatever the largest N of its launch (which sets the padding of B), the problem's shared
+// memory stays within the launch's budget.
 bool block_band_fits(int64_t N, int64_t Kq, int fp64) {
-  return N >= 1 && Kq >= 1 && N <= (fp64 ? kBandMaxN64 : kBandMaxN32) && Kq <= 4096 &&
-         block_band_smem((int)N, (int)Kq, kBandMaxRects, kBandMaxGroups, fp64) <= (size_t)kBandMaxSmem;
+  const int nmax = fp64 ? kBandMaxN64 : kBandMaxN32;
+  if (N < 1 || Kq < 1 || N > nmax || Kq > 4096) return false;
+  return block_band_smem(nmax, (int)Kq, kBandMaxRects, kBandMaxGroups, fp64) <= (size_t)kBandMaxSmem;
 }
 
 namespace {
-template <typename Tin, typename T, int NPT, int G>
+template <typename Tin, typename T, int NPT>
 cudaError_t launch_band_t(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
                           const int64_t* rstr, const BlockBases& bases, size_t smem, cudaStream_t s) {
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(block_band_kernel<Tin, T, NPT, G>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kBandMaxSmem);
+    cudaError_t e = cudaFuncSetAttribute(block_band_kernel<Tin, T, NPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kBandMaxSmem);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  block_band_kernel<Tin, T, NPT, G><<<nwork, 256, smem, s>>>(bands, work, cols, rstr, bases);
+  block_band_kernel<Tin, T, NPT><<<nwork, 256, smem, s>>>(bands, work, cols, rstr, bases);
   return cudaGetLastError();
 }
 
-// Up to 8 outputs per thread: one thread per row for N <= 8, else G = N / 8 threads per row.
 template <typename Tin, typename T>
 cudaError_t launch_band_n(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
                           const int64_t* rstr, const BlockBases& bases, int maxn, size_t smem, cudaStream_t s) {
-  if (maxn <= 1) return launch_band_t<Tin, T, 1, 1>(bands, work, nwork, cols, rstr, bases, smem, s);
-  if (maxn <= 2) return launch_band_t<Tin, T, 2, 1>(bands, work, nwork, cols, rstr, bases, smem, s);
-  if (maxn <= 4) return launch_band_t<Tin, T, 4, 1>(bands, work, nwork, cols, rstr, bases, smem, s);
-  if (maxn <= 8) return launch_band_t<Tin, T, 8, 1>(bands, work, nwork, cols, rstr, bases, smem, s);
-  if (maxn <= 16) return launch_band_t<Tin, T, 8, 2>(bands, work, nwork, cols, rstr, bases, smem, s);
-  if (maxn <= 32) return launch_band_t<Tin, T, 8, 4>(bands, work, nwork, cols, rstr, bases, smem, s);
-  if (maxn <= 64) return launch_band_t<Tin, T, 8, 8>(bands, work, nwork, cols, rstr, bases, smem, s);
-  return cudaErrorInvalidValue;
+  switch (band_npt(maxn)) {
+    case 1: return launch_band_t<Tin, T, 1>(bands, work, nwork, cols, rstr, bases, smem, s);
+    case 2: return launch_band_t<Tin, T, 2>(bands, work, nwork, cols, rstr, bases, smem, s);
+    case 4: return launch_band_t<Tin, T, 4>(bands, work, nwork, cols, rstr, bases, smem, s);
+    default: return launch_band_t<Tin, T, 8>(bands, work, nwork, cols, rstr, bases, smem, s);
+  }
 }
 }  // namespace
 
@@ -1214,6 +1368,43 @@ cudaError_t launch_block_band(const DevBand* bands, const DevBandWork* work, int
   if (fp64) return launch_band_n<double2, double2>(bands, work, nwork, cols, rstr, bases, maxn, smem, s);
   if (src_is64) return launch_band_n<double2, float2>(bands, work, nwork, cols, rstr, bases, maxn, smem, s);
   return launch_band_n<float2, float2>(bands, work, nwork, cols, rstr, bases, maxn, smem, s);
+}
+
+int block_split_band_rows(int Kp, int src_is64) { return split_band_tr(Kp, src_is64 ? 16 : 8); }
+
+size_t block_split_band_smem(int Kp, int nrect, int ng, int ncol, int src_is64) {
+  const int tr = block_split_band_rows(Kp, src_is64);
+  const size_t e = src_is64 ? sizeof(double2) : sizeof(float2);
+  return (size_t)tr * (Kp + 1) * e + (size_t)nrect * ng * sizeof(int64_t) + (size_t)nrect * tr * sizeof(int64_t) +
+         (size_t)ncol * sizeof(DevBandCol);
+}
+
+namespace {
+template <typename Tin, bool F16>
+cudaError_t launch_split_band_t(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
+                                const int64_t* rstr, const BlockBases& bases, size_t smem, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(block_split_band_kernel<Tin, F16>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kBandMaxSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  block_split_band_kernel<Tin, F16><<<nwork, 256, smem, s>>>(bands, work, cols, rstr, bases);
+  return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_block_split_band(const DevBand* bands, const DevBandWork* work, int nwork, const DevBandCol* cols,
+                                    const int64_t* rstr, const BlockBases& bases, int src_is64, int fp16,
+                                    size_t smem, cudaStream_t s) {
+  if (nwork <= 0) return cudaSuccess;
+  if (smem > (size_t)kBandMaxSmem) return cudaErrorInvalidValue;
+  if (src_is64)
+    return fp16 ? launch_split_band_t<double2, true>(bands, work, nwork, cols, rstr, bases, smem, s)
+                : launch_split_band_t<double2, false>(bands, work, nwork, cols, rstr, bases, smem, s);
+  return fp16 ? launch_split_band_t<float2, true>(bands, work, nwork, cols, rstr, bases, smem, s)
+              : launch_split_band_t<float2, false>(bands, work, nwork, cols, rstr, bases, smem, s);
 }
 
 template <typename Tin, typename Tout>
