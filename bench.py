@@ -467,6 +467,21 @@ def run_ours(args, rank, world):
     for _ in range(e2e_steps):
         check(hm.ctx.lib.gtn_map_apply_host(hm.h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr())), ctx.h)
     e2e_rate = e2e_steps / (time.perf_counter() - t0)
+    # the host link alone: the same bytes copied between the page-locked buffers and HBM
+    # (copies in the same direction saturate the link whatever the number of streams)
+    dxc = torch.empty(xh.shape, dtype=xh.dtype, device="cuda")
+    dyc = torch.empty(yh.shape, dtype=yh.dtype, device="cuda")
+    link = {}
+    for name, fn, nbytes in (("h2d_gbs", lambda: dxc.copy_(xh, non_blocking=True), xh.numel() * 16),
+                             ("d2h_gbs", lambda: yh.copy_(dyc, non_blocking=True), yh.numel() * 16)):
+        fn()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        link[name] = 3 * nbytes / (time.perf_counter() - t1) / 1e9
+    del dxc, dyc
 
     # CPU baseline: the oracle on the host cores, bounded sample of the same workload; the
     # oracle's count of the chain's flop checks the library's
@@ -584,7 +599,9 @@ def run_ours(args, rank, world):
                          "sample": f"{cpu_n} eff_h2 application(s) of the same workload, {cpu_el:.1f} s"},
         "e2e": {"value": e2e_rate, "unit": "applies/s", "h2d_bytes_per_step": int(theta.size * 16),
                 "d2h_bytes_per_step": int(np.prod(hm.y_shape) * 16),
-                "path": "gtn_map_apply_host (C ABI), page-locked host buffers: H2D copy, apply, D2H copy"},
+                "path": "gtn_map_apply_host (C ABI), page-locked host buffers: H2D copy, apply, D2H copy",
+                "host_link": link,
+                "copy_ms_per_step": 1e3 * (xh.numel() * 16 / link["h2d_gbs"] + yh.numel() * 16 / link["d2h_gbs"]) / 1e9},
         "gpu_launches": launches,
         "clocks": clocks,
         "tc_tile_choices": tuning,
