@@ -76,6 +76,10 @@ struct gtn_blockmap_s {
   bool use_graph = false;
   int64_t launches_per_run = 0;
   gtn_map proxy = nullptr;       // Krylov operator view (basis storage lives there)
+  // product bands run on a side stream beside the step's split and GEMM launches (they
+  // write other problems' outputs): fork and join events per step
+  cudaStream_t side = nullptr;
+  std::vector<cudaEvent_t> ev_fork, ev_join;
 };
 
 namespace {
@@ -356,13 +360,28 @@ int run(gtn_blockmap bm, const double2* x, double2* y) {
   std::string why;
   for (size_t si = 0; si < bm->steps.size() && e == cudaSuccess; ++si) {
     const BMStep& st = bm->steps[si];
-    if (st.nmjobs > 0) {
+    const bool others = st.nmjobs > 0 || st.ntiles > 0 || st.nswork > 0 || !st.tcp.empty() || !st.simt.empty() ||
+                        !st.skinny.empty();
+    const bool fork = st.nbwork > 0 && others && bm->side && si < bm->ev_fork.size();
+    auto bands = [&](cudaStream_t bs) {
+      ctx->launches++;
+      return launch_block_band(st.bands, st.bwork, st.nbwork, st.cols, st.rstr, bases, st.src_is64, fp64 ? 1 : 0,
+                               st.band_maxn, st.band_smem, bs);
+    };
+    if (fork) {
+      e = cudaEventRecord(bm->ev_fork[si], s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(bm->side, bm->ev_fork[si], 0);
+      if (e != cudaSuccess) break;
+      e = bands(bm->side);
+      const cudaError_t r = cudaEventRecord(bm->ev_join[si], bm->side);  // joined below whatever happens
+      if (e == cudaSuccess) e = r;
+    }
+    if (e == cudaSuccess && st.nmjobs > 0) {
       e = cudaMemsetAsync(bm->amax, 0, (size_t)st.amax_elems * sizeof(float), s);
       if (e == cudaSuccess) e = launch_block_rowmax(st.mjobs, st.mtiles, st.nmtiles, bases, st.src_is64, s);
       ctx->launches++;
-      if (e != cudaSuccess) break;
     }
-    if (st.ntiles > 0) {
+    if (e == cudaSuccess && st.ntiles > 0) {
       e = launch_block_gather(st.jobs, st.tiles, st.ntiles, bases, st.src_is64, s);
       ctx->launches++;
     }
@@ -383,10 +402,10 @@ int run(gtn_blockmap bm, const double2* x, double2* y) {
       e = launch_gemm_skinny_grouped(st.skinny.data(), (int)st.skinny.size(), fp64 ? 1 : 0, s);
       ctx->launches += (int64_t)((st.skinny.size() + kGemmJobMax - 1) / kGemmJobMax);
     }
-    if (e == cudaSuccess && st.nbwork > 0) {
-      e = launch_block_band(st.bands, st.bwork, st.nbwork, st.cols, st.rstr, bases, st.src_is64, fp64 ? 1 : 0,
-                            st.band_maxn, st.band_smem, s);
-      ctx->launches++;
+    if (e == cudaSuccess && st.nbwork > 0 && !fork) e = bands(s);
+    if (fork) {
+      const cudaError_t r = cudaStreamWaitEvent(s, bm->ev_join[si], 0);
+      if (e == cudaSuccess) e = r;
     }
   }
   if (e == cudaSuccess) {
@@ -407,6 +426,12 @@ void bm_free(gtn_blockmap bm) {
   if (bm->graph) cudaGraphDestroy(bm->graph);
   for (void* p : bm->owned) cudaFree(p);
   bm->owned.clear();
+  for (cudaEvent_t e : bm->ev_fork) cudaEventDestroy(e);
+  for (cudaEvent_t e : bm->ev_join) cudaEventDestroy(e);
+  bm->ev_fork.clear();
+  bm->ev_join.clear();
+  if (bm->side) cudaStreamDestroy(bm->side);
+  bm->side = nullptr;
 }
 
 }  // namespace
@@ -761,6 +786,21 @@ int gtn_blockmap_create(gtn_ctx ctx, int nsteps, const int* step_ngather, const 
     }
     bm->fin.src_is64 = fp64 ? 1 : 0;
     if (upload_jobs(bm, jobs, &bm->fin) != cudaSuccess) return fail(GTN_ERR_CUDA, "job table upload");
+  }
+  {
+    const char* ov = std::getenv("GTN_BLOCK_OVERLAP");
+    bool any = false;
+    for (const BMStep& st : bm->steps) any = any || st.nbwork > 0;
+    if (any && !(ov && ov[0] == '0')) {
+      if (cudaStreamCreateWithFlags(&bm->side, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(GTN_ERR_CUDA, "block map side stream");
+      bm->ev_fork.assign(bm->steps.size(), nullptr);
+      bm->ev_join.assign(bm->steps.size(), nullptr);
+      for (size_t i = 0; i < bm->steps.size(); ++i)
+        if (cudaEventCreateWithFlags(&bm->ev_fork[i], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&bm->ev_join[i], cudaEventDisableTiming) != cudaSuccess)
+          return fail(GTN_ERR_CUDA, "block map events");
+    }
   }
   *out = bm;
   return GTN_OK;
