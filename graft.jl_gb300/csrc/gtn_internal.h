@@ -67,6 +67,11 @@ int set_err(gtn_ctx ctx, int code, const std::string& msg);
   } while (0)
 
 cudaError_t ctx_workspace(gtn_ctx ctx, size_t bytes, void** out);
+// Thin QR of a tall-skinny row-major matrix by shifted Cholesky QR with two refinement
+// passes (gtn_tsqr.cu); GTN_ERR_UNSUPPORTED when it does not apply or the matrix is too
+// ill-conditioned for it (the Householder QR then runs).
+bool tsqr_applies(int64_t m, int64_t n);
+int qr_tall_cholesky(gtn_ctx ctx, int64_t m, int64_t n, const double2* A, double2* Q, double2* R);
 cudaError_t ctx_red(gtn_ctx ctx, size_t n2);   // ensure d_red/h_red hold n2 double2
 void linalg_release(gtn_ctx ctx);               // drop the cuSOLVER handle (gtn_linalg.cu)
 

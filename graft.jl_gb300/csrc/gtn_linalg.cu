@@ -602,6 +602,12 @@ extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, i
 extern "C" int gtn_qr(gtn_ctx ctx, int64_t m, int64_t n, const void* A, void* Q, void* R) {
   if (!ctx || !A || !Q || !R || m <= 0 || n <= 0) return set_err(ctx, GTN_ERR_INVALID, "gtn_qr: bad argument");
   if (m > INT32_MAX || n > INT32_MAX) return set_err(ctx, GTN_ERR_UNSUPPORTED, "gtn_qr: matrix too large");
+  const char* ts = std::getenv("GTN_TSQR");
+  if (tsqr_applies(m, n) && !(ts && ts[0] == '0')) {  // tall-skinny: Cholesky QR, else Householder below
+    const int r = qr_tall_cholesky(ctx, m, n, static_cast<const double2*>(A), static_cast<double2*>(Q),
+                                   static_cast<double2*>(R));
+    if (r != GTN_ERR_UNSUPPORTED) return r;
+  }
   cusolverDnHandle_t h;
   int st = handle(ctx, &h);
   if (st != GTN_OK) return st;

@@ -96,6 +96,29 @@ def test_chain_map_all_precisions(ctx):
         hm.close()
 
 
+@pytest.mark.parametrize("m,n,kind", [(4096, 16, "random"), (131072, 16, "random"), (20000, 64, "random"),
+                                       (50000, 24, "cond1e10"), (30000, 16, "rank_deficient"), (8192, 8, "zero")])
+def test_qr_tall_skinny(ctx, m, n, kind):
+    """Tall-skinny thin QR (shifted Cholesky QR with refinement; the Householder QR when the
+    matrix is too ill-conditioned for it): Q orthonormal, A = Q R, R upper triangular."""
+    rng = np.random.default_rng(m + n)
+    a = crandn(rng, (m, n))
+    if kind == "cond1e10":
+        u, _ = np.linalg.qr(a)
+        v, _ = np.linalg.qr(crandn(rng, (n, n)))
+        a = (u * np.logspace(0, -10, n)) @ v.conj().T
+    elif kind == "rank_deficient":
+        a[:, n // 2:] = a[:, : n - n // 2] * (1 + 2j)
+    elif kind == "zero":
+        a[:] = 0
+    Q, R = ctx.qr(ctx.upload(a))
+    Q, R = ctx.download(Q), ctx.download(R)
+    scale = max(np.linalg.norm(a), 1e-300)
+    assert np.linalg.norm(Q @ R - a) <= 1e-13 * scale + (0 if kind != "zero" else 1e-300)
+    assert np.abs(Q.conj().T @ Q - np.eye(n)).max() < 1e-12
+    assert np.allclose(np.tril(R, -1), 0)
+
+
 def test_qr_svd(ctx):
     rng = np.random.default_rng(6)
     for m, n in [(50, 20), (20, 50), (33, 33)]:
