@@ -43,6 +43,49 @@ cudaError_t ctx_workspace(gtn_ctx ctx, size_t bytes, void** out) {
   return cudaSuccess;
 }
 
+// Block sizes: 256-byte multiples below 1 MiB, 1 MiB multiples above; a cached block is
+// reused for a request of at least half its size; the cache holds at most 4 GiB.
+constexpr size_t kBlkCacheMax = size_t(4) << 30;
+
+cudaError_t ctx_blk_alloc(gtn_ctx ctx, size_t bytes, void** out, size_t* got) {
+  size_t sz = bytes < 256 ? 256 : bytes;
+  sz = sz < (size_t(1) << 20) ? (sz + 255) / 256 * 256 : (sz + (size_t(1) << 20) - 1) >> 20 << 20;
+  auto it = ctx->blk_free.lower_bound(sz);
+  if (it != ctx->blk_free.end() && it->first <= 2 * sz) {
+    *out = it->second;
+    *got = it->first;
+    ctx->blk_cached -= it->first;
+    ctx->blk_free.erase(it);
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaMalloc(out, sz);
+  if (e != cudaSuccess && !ctx->blk_free.empty()) {  // memory held by the cache: give it back, retry
+    cudaGetLastError();
+    ctx_blk_flush(ctx);
+    e = cudaMalloc(out, sz);
+  }
+  *got = e == cudaSuccess ? sz : 0;
+  return e;
+}
+
+void ctx_blk_release(gtn_ctx ctx, void* p, size_t bytes) {
+  if (!p) return;
+  if (ctx->blk_cached + bytes > kBlkCacheMax) {
+    cudaFree(p);
+    return;
+  }
+  ctx->blk_free.emplace(bytes, p);
+  ctx->blk_cached += bytes;
+}
+
+void ctx_blk_flush(gtn_ctx ctx) {
+  if (ctx->blk_free.empty()) return;
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& kv : ctx->blk_free) cudaFree(kv.second);
+  ctx->blk_free.clear();
+  ctx->blk_cached = 0;
+}
+
 cudaError_t ctx_red(gtn_ctx ctx, size_t n2) {
   if (n2 > ctx->red_cap) {
     if (ctx->d_red) cudaFree(ctx->d_red);
@@ -111,6 +154,7 @@ int gtn_ctx_destroy(gtn_ctx ctx) {
   if (!ctx) return GTN_ERR_INVALID;
   cudaStreamSynchronize(ctx->stream);
   linalg_release(ctx);
+  ctx_blk_flush(ctx);
   if (ctx->ws) cudaFree(ctx->ws);
   if (ctx->carena) cudaFree(ctx->carena);
   if (ctx->d_red) cudaFree(ctx->d_red);

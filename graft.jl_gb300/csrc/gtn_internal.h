@@ -9,6 +9,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <map>
 #include <memory>
 #include <mutex>
 
@@ -55,6 +56,11 @@ struct gtn_ctx_s {
   // precision of the GEMMs inside the factorisations (Gram SVD route): GTN_PREC_FP64 or
   // GTN_PREC_FP64E (gtn_ctx_set_linalg_precision)
   int linalg_prec = 0;
+  // freed map workspace blocks by size, reused in stream order by later maps on this
+  // context (maps are built and dropped at every node visit of a sweep; cudaMalloc and the
+  // device-synchronising cudaFree made a small map's creation cost about a millisecond)
+  std::multimap<size_t, void*> blk_free;
+  size_t blk_cached = 0;
 };
 
 // ---- status helpers -------------------------------------------------------------
@@ -67,6 +73,12 @@ int set_err(gtn_ctx ctx, int code, const std::string& msg);
   } while (0)
 
 cudaError_t ctx_workspace(gtn_ctx ctx, size_t bytes, void** out);
+// Map workspace blocks through the context's cache: *got is the block's size, to be handed
+// back with the block; release returns it to the cache (or frees it past the cache's bound),
+// flush frees every cached block.
+cudaError_t ctx_blk_alloc(gtn_ctx ctx, size_t bytes, void** out, size_t* got);
+void ctx_blk_release(gtn_ctx ctx, void* p, size_t bytes);
+void ctx_blk_flush(gtn_ctx ctx);
 // Thin QR of a tall-skinny row-major matrix by shifted Cholesky QR with two refinement
 // passes (gtn_tsqr.cu); GTN_ERR_UNSUPPORTED when it does not apply or the matrix is too
 // ill-conditioned for it (the Householder QR then runs).
@@ -449,6 +461,7 @@ struct gtn_map_s {
   void* dx = nullptr; void* dy = nullptr;     // staging for the host-buffer entry point
   int64_t bytes = 0;
   std::vector<void*> owned;
+  std::vector<std::pair<void*, size_t>> blocks;  // workspace from the context's block cache
   // a Krylov operator backed by block-sparse maps instead of a plan (gtn_blockmap_lanczos_*):
   // applications go to bm (its own precision) or, in FP64, to bm64
   struct gtn_blockmap_s* bm = nullptr;

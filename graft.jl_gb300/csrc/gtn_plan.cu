@@ -69,9 +69,10 @@ template <typename T> cudaError_t dalloc(gtn_map map, T** p, size_t bytes) {
     map->arena_spill += sz;
   }
   void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, bytes < 256 ? 256 : bytes);
+  size_t got = 0;
+  cudaError_t e = ctx_blk_alloc(map->ctx, bytes, &q, &got);
   if (e == cudaSuccess) {
-    map->owned.push_back(q);
+    map->blocks.emplace_back(q, got);
     map->bytes += (int64_t)bytes;
   }
   *p = static_cast<T*>(q);
@@ -577,7 +578,10 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
                                          (size_t)map->max_apl * sizeof(__nv_bfloat16));
   size_t freeb = 0, totalb = 0;
   if (map->oneshot) freeb = SIZE_MAX;  // one-shot contraction: the arena or a failing cudaMalloc decides
-  else cudaMemGetInfo(&freeb, &totalb);
+  else {
+    cudaMemGetInfo(&freeb, &totalb);
+    freeb += ctx->blk_cached;  // cached blocks are reused or given back on demand
+  }
   const size_t need = 2 * tbytes + abytes + (size_t)(1u << 30);
   if (need > freeb)
     return set_err(ctx, GTN_ERR_MEMORY, "memory admission refused: map workspace " +
@@ -609,6 +613,8 @@ void map_free(gtn_map map) {
   }
   for (void* p : map->owned) cudaFree(p);
   map->owned.clear();
+  for (auto& b : map->blocks) ctx_blk_release(map->ctx, b.first, b.second);
+  map->blocks.clear();
   if (map->kv) cudaFree(map->kv);
   map->kv = nullptr;
   if (map->kscratch) cudaFree(map->kscratch);

@@ -233,15 +233,26 @@ def _objective(shapes, labels, order, out_weight=8):
     return macs
 
 
+_ORDER_MEMO = {}
+
+
 def choose_order(shapes, labels, order):
     """The given (env-first) order unless the cheapest chain is clearly cheaper (by 1.5x in
     MACs plus written intermediates).  This matters at high-degree nodes, where absorbing
     every environment before the TTNO tensor multiplies the running tensor by w per leg;
-    on binary trees and chains the env-first chain is kept."""
+    on binary trees and chains the env-first chain is kept.  The answer depends only on the
+    shapes, labels and order, so it is remembered (sweeps ask again at every node visit)."""
     if len(labels) > 13:
         return list(order)
-    b = best_order(shapes, labels, order[0])
-    return b if 3 * _objective(shapes, labels, b) < 2 * _objective(shapes, labels, order) else list(order)
+    key = (tuple(tuple(int(d) for d in s) for s in shapes), tuple(tuple(l) for l in labels), tuple(order))
+    got = _ORDER_MEMO.get(key)
+    if got is None:
+        b = best_order(shapes, labels, order[0])
+        got = b if 3 * _objective(shapes, labels, b) < 2 * _objective(shapes, labels, order) else list(order)
+        if len(_ORDER_MEMO) > 100000:
+            _ORDER_MEMO.clear()
+        _ORDER_MEMO[key] = got
+    return list(got)
 
 
 class EffectiveMap:
@@ -466,7 +477,7 @@ class EnvCache:
 
     def invalidate_node(self, n):
         t = self.topo
-        for key in [k for k in self.envs if n in t.subtree_nodes(k[0], k[1])]:
+        for key in [k for k in self.envs if t.in_subtree(n, k[0], k[1])]:
             self._drop(key)
 
     def invalidate_edge(self, n, m):

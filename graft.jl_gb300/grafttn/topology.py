@@ -92,14 +92,26 @@ class TreeTopology:
         return pa[: lca_pos + 1] + list(reversed(pb[: pb.index(lca)]))
 
     def subtree_nodes(self, n, avoiding):
-        acc, stack = [], [(n, avoiding)]
-        while stack:
-            i, frm = stack.pop()
-            acc.append(i)
-            for m in self.neighbors(i):
-                if m != frm:
-                    stack.append((m, i))
-        return acc
+        """The nodes reached from n without crossing to `avoiding` (n first), as a tuple;
+        the topology never changes after construction, so each answer is computed once."""
+        memo = self.__dict__.setdefault("_subtree_memo", {})
+        key = (n, avoiding)
+        got = memo.get(key)
+        if got is None:
+            acc, stack = [], [(n, avoiding)]
+            while stack:
+                i, frm = stack.pop()
+                acc.append(i)
+                for m in self.neighbors(i):
+                    if m != frm:
+                        stack.append((m, i))
+            got = memo[key] = (tuple(acc), frozenset(acc))
+        return got[0]
+
+    def in_subtree(self, x, n, avoiding):
+        """Whether x is among subtree_nodes(n, avoiding) (a set lookup after the first call)."""
+        self.subtree_nodes(n, avoiding)
+        return x in self._subtree_memo[(n, avoiding)][1]
 
 
 def mps_topology(n):

@@ -360,7 +360,7 @@ class U1EnvCache:
 
     def invalidate_node(self, n):
         t = self.topo
-        for key in [k for k in self.envs if n in t.subtree_nodes(k[0], k[1])]:
+        for key in [k for k in self.envs if t.in_subtree(n, k[0], k[1])]:
             del self.envs[key]
 
     def invalidate_edge(self, n, m):
