@@ -1022,7 +1022,7 @@ def main():
                     help="leave out the bounded D=1024 dmrg2 segment (mixed vs FP64) of the default line")
     ap.add_argument("--segment-steps", type=int, default=1)
     ap.add_argument("--tc-tuning", default="measured",
-                    choices=["measured", "ladder", "ps128", "ps128x2", "ps256", "pair256", "persist128"],
+                    choices=["measured", "ladder", "ps128", "ps128x2", "ps256", "pair256", "persist128", "persist256"],
                     help="tile shapes of the tcgen05 steps: timed per problem class (default), the fixed "
                          "ladder, or one variant for every step (fixed launch sequences, for profiler captures)")
     ap.add_argument("--dmrg", action="store_true", help="measure DMRG sweeps instead of map applications")

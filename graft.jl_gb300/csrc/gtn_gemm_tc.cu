@@ -1143,9 +1143,12 @@ enum TcVariant : int {
   TCV_PS256 = 4,    // 128 x 256, one CTA per SM
   TCV_PAIR256 = 5,  // 256 x 256 on an SM pair (cta_group::2)
   TCV_PERSIST128 = 6,  // 128 x 128, persistent (one CTA per SM, epilogue overlapping the next tile)
-  TCV_COUNT = 7
+  TCV_PERSIST256 = 7,  // 128 x 256, persistent (one accumulator set; the operand ring runs on
+                       // across tiles, so the next tile's copies land during the epilogue)
+  TCV_COUNT = 8
 };
-const char* const kTcVariantNames[TCV_COUNT] = {"ps32", "ps64", "ps128", "ps128x2", "ps256", "pair256", "persist128"};
+const char* const kTcVariantNames[TCV_COUNT] = {"ps32",   "ps64",    "ps128",      "ps128x2",
+                                                "ps256",  "pair256", "persist128", "persist256"};
 
 template <int P>
 cudaError_t launch_variant(int v, const TcGemmArgs& a, int* errflag, cudaStream_t s, std::string* why) {
@@ -1156,6 +1159,7 @@ cudaError_t launch_variant(int v, const TcGemmArgs& a, int* errflag, cudaStream_
     case TCV_PS128X2: return launch_ps<128, P, 2>(a, errflag, s, why);
     case TCV_PS256: return launch_ps<256, P>(a, errflag, s, why);
     case TCV_PERSIST128: return launch_grouped_ps<128, P, true>(&a, 1, errflag, s, why);
+    case TCV_PERSIST256: return launch_grouped_ps<256, P, true>(&a, 1, errflag, s, why);
     default: return launch_pair<P>(a, errflag, s, why);
   }
 }
@@ -1177,7 +1181,13 @@ int tc_candidates(int64_t n2, int* out) {
   if (n2 <= 32) out[n++] = TCV_PS32;
   else if (n2 <= 64) out[n++] = TCV_PS64;
   else if (n2 <= 128) { out[n++] = TCV_PS128; out[n++] = TCV_PS128X2; out[n++] = TCV_PERSIST128; }
-  else { out[n++] = TCV_PS256; out[n++] = TCV_PAIR256; out[n++] = TCV_PS128X2; out[n++] = TCV_PERSIST128; }
+  else {
+    out[n++] = TCV_PS256;
+    out[n++] = TCV_PAIR256;
+    out[n++] = TCV_PS128X2;
+    out[n++] = TCV_PERSIST128;
+    out[n++] = TCV_PERSIST256;
+  }
   return n;
 }
 

@@ -124,7 +124,8 @@ def site_labels(desc):
     return out, [order[i] for i in range(n.value)]
 
 
-TC_VARIANTS = {"ps32": 0, "ps64": 1, "ps128": 2, "ps128x2": 3, "ps256": 4, "pair256": 5, "persist128": 6}
+TC_VARIANTS = {"ps32": 0, "ps64": 1, "ps128": 2, "ps128x2": 3, "ps256": 4, "pair256": 5, "persist128": 6,
+               "persist256": 7}
 
 
 class GraftError(RuntimeError):

@@ -141,9 +141,9 @@ int gtn_map_out_shape(gtn_map map, int* rank, int64_t* dims);
  * same order per output element, so the choice never changes results.
  * gtn_tc_tuning(mode, clear): mode 0 = fixed ladder, 1 = measured (default), 2 + v = force
  * variant v (0 ps32, 1 ps64, 2 ps128, 3 ps128x2, 4 ps256, 5 pair256 = 256 x 256 tiles on an
- * SM pair, 6 persist128 = persistent 128 x 128) where it is a candidate; mode -1 keeps the
- * mode.  clear != 0 forgets the cached choices.  Returns the previous mode, or -1 for a mode
- * outside -1 .. 8.  Grouped launches (block-sparse steps, batched maps) always run the
+ * SM pair, 6 persist128 = persistent 128 x 128, 7 persist256 = persistent 128 x 256) where
+ * it is a candidate; mode -1 keeps the mode.  clear != 0 forgets the cached choices.  Returns
+ * the previous mode, or -1 for a mode outside -1 .. 9.  Grouped launches (block-sparse steps, batched maps) always run the
  * persistent kernel; in the measured mode their tile width (the widest problem's ladder width
  * or half of it) is measured per problem list the same way.
  * gtn_tc_tune_report writes one text line per cached class (the candidates' times and the

@@ -43,12 +43,12 @@ def test_tc_variants_match_numpy(ctx, restore_tuning, mkn, prec):
     A, B = crandn(rng, (M, K)), crandn(rng, (K, N))
     ref = A @ B
     outs = {}
-    for v in ("ps256", "pair256", "ps128x2", "persist128"):
+    for v in ("ps256", "pair256", "ps128x2", "persist128", "persist256"):
         _lib.tc_tuning(v)
         outs[v] = contract(ctx, A, B, prec)
         assert rel(outs[v], ref) < RTOL[prec], (v, rel(outs[v], ref))
     # the variants sum the same products per output element: they agree far below the map error
-    for v in ("pair256", "ps128x2", "persist128"):
+    for v in ("pair256", "ps128x2", "persist128", "persist256"):
         assert rel(outs[v], outs["ps256"]) < 1e-6, v
     ctx.sync()
 
