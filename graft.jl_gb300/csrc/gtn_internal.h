@@ -83,6 +83,13 @@ void ctx_blk_flush(gtn_ctx ctx);
 // passes (gtn_tsqr.cu); GTN_ERR_UNSUPPORTED when it does not apply or the matrix is too
 // ill-conditioned for it (the Householder QR then runs).
 bool tsqr_applies(int64_t m, int64_t n);
+// Householder QR of a small matrix (m n and m min(m, n) <= 4096) in one CTA, no host sync.
+bool small_qr_applies(int64_t m, int64_t n);
+// One-sided Jacobi SVD of a small matrix (min(m, n) <= 64, m n <= 4096) in one CTA:
+// S (k, descending), U (m x k row-major), Vh (k x n row-major), k = min(m, n), on the device.
+bool small_svd_applies(int64_t m, int64_t n);
+int svd_small_launch(gtn_ctx ctx, int64_t m, int64_t n, const double2* A, double* S, double2* U, double2* Vh);
+int qr_small(gtn_ctx ctx, int64_t m, int64_t n, const double2* A, double2* Q, double2* R);
 int qr_tall_cholesky(gtn_ctx ctx, int64_t m, int64_t n, const double2* A, double2* Q, double2* R);
 cudaError_t ctx_red(gtn_ctx ctx, size_t n2);   // ensure d_red/h_red hold n2 double2
 void linalg_release(gtn_ctx ctx);               // drop the cuSOLVER handle (gtn_linalg.cu)

@@ -535,6 +535,31 @@ extern "C" int gtn_svd_trunc(gtn_ctx ctx, int64_t m, int64_t n, const void* A, i
     cudaFree(VB);
     return st;
   }
+  const char* ssv = std::getenv("GTN_SMALL_SVD");
+  if (small_svd_applies(m, n) && !(ssv && ssv[0] == '0')) {  // one-CTA Jacobi: no per-shape set-up
+    const size_t bU = align256(m * k * sizeof(double2)), bV = align256(k * n * sizeof(double2)),
+                 bS = align256(k * sizeof(double));
+    void* ws = nullptr;
+    GTN_CUDA_TRY(ctx, ctx_workspace(ctx, bU + bV + bS, &ws));
+    double2* dU = static_cast<double2*>(ws);
+    double2* dV = reinterpret_cast<double2*>(static_cast<char*>(ws) + bU);
+    double* dS = reinterpret_cast<double*>(static_cast<char*>(ws) + bU + bV);
+    st = svd_small_launch(ctx, m, n, static_cast<const double2*>(A), dS, dU, dV);
+    if (st != GTN_OK) return st;
+    std::vector<double> hs(k);
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(hs.data(), dS, k * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GTN_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    const int64_t r = trunc_rank(hs, maxdim, atol, rtol, discarded_weight);
+    double disc = 0;
+    for (int64_t i = r; i < k; ++i) disc += hs[i] * hs[i];
+    for (int64_t i = 0; i < r; ++i) S[i] = hs[i];
+    *rank = r;
+    if (discarded) *discarded = std::sqrt(disc);
+    GTN_CUDA_TRY(ctx, cudaMemcpy2DAsync(U, r * sizeof(double2), dU, k * sizeof(double2), r * sizeof(double2), m,
+                                        cudaMemcpyDeviceToDevice, s));
+    GTN_CUDA_TRY(ctx, cudaMemcpyAsync(Vh, dV, r * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    return gtn_ctx_sync(ctx);
+  }
   // Column-major problem B (rows >= cols): for n >= m, B = A^T (the same buffer); else B =
   // column-major copy of A (a transpose).
   const bool wide = n >= m;
@@ -603,7 +628,10 @@ extern "C" int gtn_qr(gtn_ctx ctx, int64_t m, int64_t n, const void* A, void* Q,
   if (!ctx || !A || !Q || !R || m <= 0 || n <= 0) return set_err(ctx, GTN_ERR_INVALID, "gtn_qr: bad argument");
   if (m > INT32_MAX || n > INT32_MAX) return set_err(ctx, GTN_ERR_UNSUPPORTED, "gtn_qr: matrix too large");
   const char* ts = std::getenv("GTN_TSQR");
-  if (tsqr_applies(m, n) && !(ts && ts[0] == '0')) {  // tall-skinny: Cholesky QR, else Householder below
+  const bool fast = !(ts && ts[0] == '0');
+  if (fast && small_qr_applies(m, n))  // small: Householder in one CTA
+    return qr_small(ctx, m, n, static_cast<const double2*>(A), static_cast<double2*>(Q), static_cast<double2*>(R));
+  if (fast && tsqr_applies(m, n)) {  // tall-skinny: Cholesky QR, else Householder below
     const int r = qr_tall_cholesky(ctx, m, n, static_cast<const double2*>(A), static_cast<double2*>(Q),
                                    static_cast<double2*>(R));
     if (r != GTN_ERR_UNSUPPORTED) return r;

@@ -97,16 +97,20 @@ def test_chain_map_all_precisions(ctx):
 
 
 @pytest.mark.parametrize("m,n,kind", [(4096, 16, "random"), (131072, 16, "random"), (20000, 64, "random"),
-                                       (50000, 24, "cond1e10"), (30000, 16, "rank_deficient"), (8192, 8, "zero")])
+                                       (50000, 24, "cond1e10"), (30000, 16, "rank_deficient"), (8192, 8, "zero"),
+                                       (40, 10, "rank_deficient"), (16, 16, "zero"), (3, 20, "random"),
+                                       (64, 64, "cond1e10"), (1, 1, "random")])
 def test_qr_tall_skinny(ctx, m, n, kind):
-    """Tall-skinny thin QR (shifted Cholesky QR with refinement; the Householder QR when the
-    matrix is too ill-conditioned for it): Q orthonormal, A = Q R, R upper triangular."""
+    """Thin QR on the device paths: one-CTA Householder for small matrices, shifted Cholesky
+    QR with refinement for tall-skinny ones (the cuSOLVER Householder QR when the matrix is
+    too ill-conditioned for it): Q orthonormal, A = Q R, R upper triangular."""
     rng = np.random.default_rng(m + n)
     a = crandn(rng, (m, n))
+    k = min(m, n)
     if kind == "cond1e10":
         u, _ = np.linalg.qr(a)
         v, _ = np.linalg.qr(crandn(rng, (n, n)))
-        a = (u * np.logspace(0, -10, n)) @ v.conj().T
+        a = (u[:, :k] * np.logspace(0, -10, k)) @ v[:k].conj()
     elif kind == "rank_deficient":
         a[:, n // 2:] = a[:, : n - n // 2] * (1 + 2j)
     elif kind == "zero":
@@ -115,8 +119,24 @@ def test_qr_tall_skinny(ctx, m, n, kind):
     Q, R = ctx.download(Q), ctx.download(R)
     scale = max(np.linalg.norm(a), 1e-300)
     assert np.linalg.norm(Q @ R - a) <= 1e-13 * scale + (0 if kind != "zero" else 1e-300)
-    assert np.abs(Q.conj().T @ Q - np.eye(n)).max() < 1e-12
+    assert np.abs(Q.conj().T @ Q - np.eye(k)).max() < 1e-12
     assert np.allclose(np.tril(R, -1), 0)
+
+
+@pytest.mark.parametrize("m,n,rank", [(30, 20, 5), (20, 30, 20), (64, 64, 64), (7, 3, 0), (1, 9, 1)])
+def test_svd_small_jacobi(ctx, m, n, rank):
+    """The one-CTA Jacobi SVD of small matrices (min(m, n) <= 64, m n <= 4096): singular values
+    against numpy, orthonormal factors also for rank-deficient and zero input, reconstruction."""
+    rng = np.random.default_rng(m * 100 + n)
+    k = min(m, n)
+    a = crandn(rng, (m, rank)) @ crandn(rng, (rank, n)) if rank > 0 else np.zeros((m, n), complex)
+    U, S, Vh, disc = ctx.svd_trunc(ctx.upload(a))
+    U, Vh = ctx.download(U), ctx.download(Vh)
+    assert len(S) == k
+    assert np.allclose(S, np.linalg.svd(a, compute_uv=False), rtol=1e-12, atol=1e-12 * max(1.0, np.abs(S).max()))
+    assert np.abs(U.conj().T @ U - np.eye(k)).max() < 1e-12
+    assert np.abs(Vh @ Vh.conj().T - np.eye(k)).max() < 1e-12
+    assert np.linalg.norm((U * S) @ Vh - a) <= 1e-13 * max(np.linalg.norm(a), 1e-300)
 
 
 def test_qr_svd(ctx):
