@@ -672,6 +672,9 @@ def dmrg_segment(ctx, steps, precision, D=1024, refine_tol=1e-8):
                 wm = eff_h2(wc, wpsi, H, n, topo.parent[n], wp)
                 wm(wth)
                 wm.close()
+            # and the split's factorisations of the same shapes (the solver library loads its
+            # kernels on first use; a sweep pays that once, at its first step)
+            split_two_site(wpsi, wth, n, topo.parent[n], trunc, "m")
             del wpsi, wc, wth
             torch.cuda.synchronize()
         for _ in range(steps):
