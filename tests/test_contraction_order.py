@@ -85,3 +85,13 @@ def test_best_order_keeps_the_open_legs():
         sh = [l for l in cur if l > 0 and l in L]
         cur = [l for l in L if l not in sh] + [l for l in cur if l not in sh]
     assert sorted(cur) == sorted(l for lab in labels for l in lab if l < 0)
+
+
+def test_choose_order_is_remembered_per_network():
+    """A repeated question gets the same answer, and callers get their own copy."""
+    shapes, labels, order = h1_network(G.kary_topology(4, 2), 0, 8, 5)
+    first = GC.choose_order(shapes, labels, order)
+    first.append(99)  # a caller's edit must not leak into the remembered answer
+    again = GC.choose_order([tuple(s) for s in shapes], [list(l) for l in labels], list(order))
+    assert again == first[:-1]
+    assert again == GC.best_order(shapes, labels, order[0])

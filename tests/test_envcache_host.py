@@ -70,3 +70,17 @@ def test_invalidate_edge_is_both_endpoints(which):
             for w in topo.neighbors(a):
                 if w != b:
                     assert (w, a) in cache.envs
+
+
+@pytest.mark.parametrize("topo", [G.mps_topology(7), G.binary_topology(3), G.kary_topology(3, 2),
+                                  G.star_topology(3, 2)])
+def test_subtree_sets_match_a_tree_walk(topo):
+    """The remembered subtree of (u, away from v) is u's side of the edge, on every call."""
+    for _ in range(2):  # the second pass reads the remembered answers
+        for u in range(topo.nnodes):
+            for v in topo.neighbors(u):
+                ref = side(topo, u, v)
+                got = topo.subtree_nodes(u, v)
+                assert got[0] == u and set(got) == ref and len(got) == len(ref)
+                for x in range(topo.nnodes):
+                    assert topo.in_subtree(x, u, v) == (x in ref)
