@@ -179,6 +179,8 @@ struct SmallJob {
   void* C;
 };
 cudaError_t launch_gather_grouped(const GatherJob* jobs, int njobs, int in_is64, int out_is64, cudaStream_t s);
+// out[i] = offset of index i of the group (i < n), computed on the device.
+cudaError_t launch_offsets_table(const GroupSpec& g, int64_t n, int64_t* out, cudaStream_t s);
 // Row maxima of the jobs that carry amax (zeroed first), for their fp16 splits.
 cudaError_t launch_rowmax_grouped(const GatherJob* jobs, int njobs, int in_is64, cudaStream_t s);
 // Device-resident gather jobs (block-sparse maps): buffers resolved per launch.
@@ -469,6 +471,12 @@ struct gtn_map_s {
   int64_t bytes = 0;
   std::vector<void*> owned;
   std::vector<std::pair<void*, size_t>> blocks;  // workspace from the context's block cache
+  struct PendingTab {  // offset tables filled on the device once the plan is admitted
+    GroupSpec g;
+    int64_t n;
+    int64_t* d;
+  };
+  std::vector<PendingTab> pending_tabs;
   // a Krylov operator backed by block-sparse maps instead of a plan (gtn_blockmap_lanczos_*):
   // applications go to bm (its own precision) or, in FP64, to bm64
   struct gtn_blockmap_s* bm = nullptr;

@@ -1407,6 +1407,22 @@ cudaError_t launch_block_split_band(const DevBand* bands, const DevBandWork* wor
               : launch_split_band_t<float2, false>(bands, work, nwork, cols, rstr, bases, smem, s);
 }
 
+namespace {
+// out[i] = element offset of index i of an index group (its digits, innermost fastest, times
+// the group's strides): the offset tables of the gathers, computed where they are used.
+__global__ void offsets_table_kernel(GroupSpec g, int64_t n, int64_t* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = decompose(i, g);
+}
+}  // namespace
+
+cudaError_t launch_offsets_table(const GroupSpec& g, int64_t n, int64_t* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 8);
+  offsets_table_kernel<<<(unsigned)blocks, 256, 0, s>>>(g, n, out);
+  return cudaGetLastError();
+}
+
 template <typename Tin, typename Tout>
 static cudaError_t launch_gather_grouped_t(const GatherJob* jobs, int njobs, cudaStream_t s) {
   for (int base = 0; base < njobs; base += kGatherJobMax) {

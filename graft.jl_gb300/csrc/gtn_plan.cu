@@ -87,29 +87,32 @@ bool is_fp16(int precision) { return precision == GTN_PREC_FP16X3; }
 bool is_f64e(int precision) { return precision == GTN_PREC_FP64E; }
 
 // Device table of the element offsets of indices 0..n-1 of an index group (digits outer..
-// inner, the innermost one incremented first), owned by the map.
+// inner, the innermost one incremented first), owned by the map.  Computed by a kernel on
+// the map's stream: a host table copied from pageable memory would make the copy wait for
+// all earlier work on the stream, stalling every map build and one-shot contraction.
+// The fill is queued and launched by fill_offset_tables once the plan has passed its memory
+// admission, so that a refused plan launches nothing but its statics' packing.
 cudaError_t upload_offsets(gtn_map map, const GroupSpec& g, int64_t n, const int64_t** out) {
-  std::vector<int64_t> h((size_t)std::max<int64_t>(n, 1), 0);
-  int64_t dig[GTN_MAXG] = {0};
-  int64_t off = 0;
-  for (int64_t i = 0; i < n; ++i) {
-    h[(size_t)i] = off;
-    for (int j = g.n - 1; j >= 0; --j) {
-      ++dig[j];
-      off += g.str[j];
-      if (dig[j] < g.dim[j]) break;
-      off -= g.str[j] * g.dim[j];
-      dig[j] = 0;
-    }
-  }
   int64_t* d = nullptr;
-  cudaError_t e = dalloc(map, &d, h.size() * sizeof(int64_t));
-  // stream-ordered: the buffer may be arena memory that earlier work on the stream reads
-  // (pageable source: the call returns once the data is staged, so h may go out of scope)
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d, h.data(), h.size() * sizeof(int64_t), cudaMemcpyHostToDevice, map->ctx->stream);
+  cudaError_t e = dalloc(map, &d, (size_t)std::max<int64_t>(n, 1) * sizeof(int64_t));
+  if (e == cudaSuccess) map->pending_tabs.push_back({g, n, d});
   *out = d;
   return e;
+}
+
+int fill_offset_tables(gtn_map map) {
+  cudaError_t e = cudaSuccess;
+  for (const auto& t : map->pending_tabs) {
+    if (t.n > 0) {
+      e = launch_offsets_table(t.g, t.n, t.d, map->ctx->stream);
+      map->ctx->launches++;
+    } else {
+      e = cudaMemsetAsync(t.d, 0, sizeof(int64_t), map->ctx->stream);
+    }
+    if (e != cudaSuccess) break;
+  }
+  map->pending_tabs.clear();
+  return e == cudaSuccess ? GTN_OK : set_err(map->ctx, GTN_ERR_CUDA, std::string("offset tables: ") + cudaGetErrorString(e));
 }
 
 // Offset tables of an [M, K] gather, or none (index-group decomposition) when they would
@@ -564,7 +567,7 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
     }
     map->fp64_alt = alt;
   }
-  if (!alloc_ws) return GTN_OK;
+  if (!alloc_ws) return fill_offset_tables(map);
 
   // ---- workspace admission, then allocation ------------------------------------------
   int64_t max_t = map->max_t, max_a = map->max_a, max_sk = map->max_splitk;
@@ -602,7 +605,7 @@ int plan_build(gtn_ctx ctx, int n, const int* ranks, const int64_t* dims, const 
     map->fp64_alt->abuf = map->abuf;
     map->fp64_alt->skbuf = map->skbuf;
   }
-  return GTN_OK;
+  return fill_offset_tables(map);
 }
 
 void map_free(gtn_map map) {
